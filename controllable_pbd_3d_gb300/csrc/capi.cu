@@ -1,0 +1,380 @@
+// extern "C" entry points of libmgpbd.so (declared in include/mgpbd.h).
+// Every call catches C++ exceptions and returns an MGPBD_E* code; the text
+// of the last error of the calling thread is available from
+// mgpbd_last_error().
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "common.h"
+#include "kernels.cuh"
+#include "solver.h"
+#include "structure.h"
+
+struct mgpbd_solver {
+  mgpbd::Solver impl;
+  explicit mgpbd_solver(const mgpbd_params& p) : impl(p) {}
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template <class F>
+int guarded(F&& f) {
+  try {
+    f();
+    return MGPBD_OK;
+  } catch (const mgpbd::Error& e) {
+    g_last_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    g_last_error = "host allocation failed";
+    return MGPBD_ENOMEM;
+  } catch (const std::invalid_argument& e) {
+    g_last_error = e.what();
+    return MGPBD_EINVAL;
+  } catch (const std::length_error& e) {
+    g_last_error = e.what();
+    return MGPBD_ERANGE;
+  } catch (const std::exception& e) {
+    g_last_error = e.what();
+    return MGPBD_EINVAL;
+  }
+}
+
+cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+}  // namespace
+
+extern "C" {
+
+void mgpbd_default_params(mgpbd_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->dt = 0.0f;
+  p->mu = 1e6f;
+  p->damp = 1.0f;
+  p->maxiter = 20;
+  p->atol = 1e-4f;
+  p->rtol = 1e-2f;
+  p->maxiter_cg = 100;
+  p->tol_cg = 1e-5f;
+  p->n_smooth = 2;
+  p->omega_jacobi = 2.0f / 3.0f;
+  p->setup_interval = 10000;
+  p->use_line_search = 1;
+  p->mode = MGPBD_MODE_PARITY;
+  p->rel_tol_cg = 0.0f;
+  p->coarse_solver = MGPBD_COARSE_JACOBI;
+  p->smoother = MGPBD_SMOOTH_JACOBI;
+  p->max_levels = 0;
+  p->max_coarse = 400;
+  p->kinematic_pins = 0;
+  p->coarse_sweeps = 0;
+}
+
+const char* mgpbd_strerror(int code) {
+  switch (code) {
+    case MGPBD_OK: return "ok";
+    case MGPBD_EINVAL: return "invalid argument";
+    case MGPBD_ECUDA: return "CUDA runtime error";
+    case MGPBD_ENOMEM: return "out of memory";
+    case MGPBD_ESTATE: return "call out of order";
+    case MGPBD_ENUMERIC: return "non-finite value in the solve";
+    case MGPBD_ERANGE: return "size out of range";
+    case MGPBD_ENOTSUP: return "not supported";
+    default: return "unknown error";
+  }
+}
+
+const char* mgpbd_last_error(void) { return g_last_error.c_str(); }
+
+const char* mgpbd_version(void) { return "mgpbd-gb300 0.1 (sm_103a)"; }
+
+int mgpbd_create(const mgpbd_params* params, mgpbd_handle* out) {
+  if (!params || !out) return MGPBD_EINVAL;
+  *out = nullptr;
+  return guarded([&] { *out = new mgpbd_solver(*params); });
+}
+
+void mgpbd_destroy(mgpbd_handle h) { delete h; }
+
+int mgpbd_set_stream(mgpbd_handle h, void* stream) {
+  if (!h) return MGPBD_EINVAL;
+  h->impl.set_stream(as_stream(stream));
+  return MGPBD_OK;
+}
+
+int mgpbd_set_mesh(mgpbd_handle h, const float* x_ref, const float* invm, const int32_t* t_i,
+                   int32_t nv, int32_t nt, float* x, float* v) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.set_mesh(x_ref, invm, t_i, nv, nt, x, v); });
+}
+
+int mgpbd_init(mgpbd_handle h) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.init(); });
+}
+
+int mgpbd_step(mgpbd_handle h, int32_t frame) {
+  if (!h) return MGPBD_EINVAL;
+  int rc = guarded([&] { h->impl.step(frame); });
+  if (rc == MGPBD_OK && (h->impl.status() & MGPBD_STATUS_NAN)) return MGPBD_ENUMERIC;
+  return rc;
+}
+
+int mgpbd_make_prediction(mgpbd_handle h) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.make_prediction(); });
+}
+
+int mgpbd_solve(mgpbd_handle h, int32_t frame) {
+  if (!h) return MGPBD_EINVAL;
+  int rc = guarded([&] { h->impl.solve(frame); });
+  if (rc == MGPBD_OK && (h->impl.status() & MGPBD_STATUS_NAN)) return MGPBD_ENUMERIC;
+  return rc;
+}
+
+int mgpbd_update_vel(mgpbd_handle h) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.update_vel(); });
+}
+
+int mgpbd_get_stats(mgpbd_handle h, mgpbd_stats* out) {
+  if (!h || !out) return MGPBD_EINVAL;
+  *out = h->impl.stats();
+  return MGPBD_OK;
+}
+
+int mgpbd_get_status(mgpbd_handle h, uint32_t* status) {
+  if (!h || !status) return MGPBD_EINVAL;
+  *status = h->impl.status();
+  return MGPBD_OK;
+}
+
+int mgpbd_field(mgpbd_handle h, int32_t field, void** dev_ptr, int64_t* count) {
+  if (!h || !dev_ptr || !count) return MGPBD_EINVAL;
+  return guarded([&] { *dev_ptr = h->impl.field(field, count); });
+}
+
+int mgpbd_level_csr(mgpbd_handle h, int32_t level, int32_t* n_rows, int64_t* nnz, int32_t** indptr,
+                    int32_t** indices, float** data, float** diag_inv) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] {
+    const mgpbd::Level& L = h->impl.level(level);
+    if (n_rows) *n_rows = L.n;
+    if (nnz) *nnz = L.nnz;
+    if (indptr) *indptr = L.indptr.p;
+    if (indices) *indices = L.indices.p;
+    if (data) *data = L.data.p;
+    if (diag_inv) *diag_inv = L.diag_inv.p;
+  });
+}
+
+int mgpbd_level_agg(mgpbd_handle h, int32_t level, int32_t** agg_ids) {
+  if (!h || !agg_ids) return MGPBD_EINVAL;
+  return guarded([&] {
+    const mgpbd::Level& L = h->impl.level(level);
+    mgpbd::require(L.agg.p != nullptr, MGPBD_EINVAL, "level has no coarser level");
+    *agg_ids = L.agg.p;
+  });
+}
+
+int mgpbd_level_count(mgpbd_handle h, int32_t* n_levels) {
+  if (!h || !n_levels) return MGPBD_EINVAL;
+  return guarded([&] { *n_levels = h->impl.n_levels(); });
+}
+
+int mgpbd_compute_constraints(mgpbd_handle h) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.compute_constraints(); });
+}
+
+int mgpbd_fill_matrices(mgpbd_handle h) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.fill_matrices(); });
+}
+
+int mgpbd_compute_rhs(mgpbd_handle h, double* residual_norm) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] {
+    double r = h->impl.compute_rhs();
+    if (residual_norm) *residual_norm = r;
+  });
+}
+
+int mgpbd_pcg(mgpbd_handle h, const float* b, float* x, int32_t* cg_iters) {
+  if (!h || !b || !x) return MGPBD_EINVAL;
+  return guarded([&] {
+    int32_t it = h->impl.pcg(b, x);
+    if (cg_iters) *cg_iters = it;
+  });
+}
+
+int mgpbd_vcycle(mgpbd_handle h, const float* r, float* z) {
+  if (!h || !r || !z) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.vcycle_into(r, z); });
+}
+
+int mgpbd_scatter(mgpbd_handle h, const float* dlam) {
+  if (!h || !dlam) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.scatter(dlam); });
+}
+
+int mgpbd_line_search(mgpbd_handle h, double* omega) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] {
+    double w = h->impl.line_search();
+    if (omega) *omega = w;
+  });
+}
+
+int mgpbd_apply_dpos(mgpbd_handle h, double omega) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.apply_dpos(omega); });
+}
+
+int mgpbd_synchronize(mgpbd_handle h) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { MGPBD_CUDA(cudaStreamSynchronize(h->impl.stream())); });
+}
+
+// ---- standalone sparse kernels --------------------------------------------
+int mgpbd_csr_spmv(int32_t n_rows, const int32_t* indptr, const int32_t* indices, const float* data,
+                   const float* x, float* y, void* stream) {
+  if (n_rows < 0 || (n_rows > 0 && (!indptr || !indices || !data || !x || !y))) return MGPBD_EINVAL;
+  return guarded([&] {
+    mgpbd::CsrView a;
+    a.n = n_rows;
+    int32_t nnz = 0;
+    if (n_rows > 0)
+      MGPBD_CUDA(cudaMemcpyAsync(&nnz, indptr + n_rows, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                 as_stream(stream)));
+    MGPBD_CUDA(cudaStreamSynchronize(as_stream(stream)));
+    a.nnz = nnz;
+    a.indptr = indptr;
+    a.indices = indices;
+    a.data = data;
+    mgpbd::launch_spmv(a, x, y, as_stream(stream));
+  });
+}
+
+int mgpbd_csr_jacobi(int32_t n_rows, const int32_t* indptr, const int32_t* indices,
+                     const float* data, const float* diag_inv, const float* b, const float* x,
+                     float* x_new, float omega, void* stream) {
+  if (n_rows < 0 || (n_rows > 0 && (!indptr || !indices || !data || !diag_inv || !b || !x || !x_new)))
+    return MGPBD_EINVAL;
+  return guarded([&] {
+    mgpbd::CsrView a;
+    a.n = n_rows;
+    int32_t nnz = 0;
+    if (n_rows > 0)
+      MGPBD_CUDA(cudaMemcpyAsync(&nnz, indptr + n_rows, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                 as_stream(stream)));
+    MGPBD_CUDA(cudaStreamSynchronize(as_stream(stream)));
+    a.nnz = nnz;
+    a.indptr = indptr;
+    a.indices = indices;
+    a.data = data;
+    a.diag_inv = diag_inv;
+    mgpbd::launch_jacobi(a, b, x, x_new, omega, as_stream(stream));
+  });
+}
+
+int mgpbd_csr_diag_inv(int32_t n_rows, const int32_t* indptr, const int32_t* indices,
+                       const float* data, float* diag_inv, void* stream) {
+  if (n_rows < 0 || (n_rows > 0 && (!indptr || !indices || !data || !diag_inv))) return MGPBD_EINVAL;
+  return guarded([&] { mgpbd::launch_diag_inv_scan(indptr, indices, data, n_rows, diag_inv, as_stream(stream)); });
+}
+
+int mgpbd_dot(int32_t n, const float* a, const float* b, double* out, void* stream) {
+  if (n < 0 || !out || (n > 0 && (!a || !b))) return MGPBD_EINVAL;
+  return guarded([&] {
+    int blocks = mgpbd::reduce_blocks(n);
+    mgpbd::DevBuf<double> part(blocks + 1);
+    cudaStream_t s = as_stream(stream);
+    mgpbd::launch_dot_partials(a, b, n, part.p, s);
+    mgpbd::launch_finalize(part.p, blocks, 1, part.p + blocks, s);
+    MGPBD_CUDA(cudaMemcpyAsync(out, part.p + blocks, sizeof(double), cudaMemcpyDeviceToHost, s));
+    MGPBD_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int mgpbd_axpy(int32_t n, float alpha, const float* x, float* y, void* stream) {
+  if (n < 0 || (n > 0 && (!x || !y))) return MGPBD_EINVAL;
+  return guarded([&] { mgpbd::launch_axpy(alpha, x, y, n, as_stream(stream)); });
+}
+
+int mgpbd_xpay(int32_t n, float alpha, const float* x, float* y, void* stream) {
+  if (n < 0 || (n > 0 && (!x || !y))) return MGPBD_EINVAL;
+  return guarded([&] { mgpbd::launch_xpay(alpha, x, y, n, as_stream(stream)); });
+}
+
+// ---- host structure builders ----------------------------------------------
+int mgpbd_host_pattern(const int32_t* t_i, int32_t nt, int64_t* nnz, int32_t* indptr,
+                       int32_t* indices) {
+  if (!t_i || nt < 0 || !nnz) return MGPBD_EINVAL;
+  return guarded([&] {
+    mgpbd::Csr p = mgpbd::build_pattern(t_i, nt);
+    *nnz = p.nnz();
+    if (indptr) {
+      mgpbd::require(indices != nullptr, MGPBD_EINVAL, "indices buffer missing");
+      std::memcpy(indptr, p.indptr.data(), sizeof(int32_t) * p.indptr.size());
+      std::memcpy(indices, p.indices.data(), sizeof(int32_t) * p.indices.size());
+    }
+  });
+}
+
+int mgpbd_host_aggregate(const int32_t* t_i, int32_t nt, int32_t max_agg_size, int32_t* agg_ids,
+                         int32_t* n_agg) {
+  if (!t_i || nt < 0 || !agg_ids || !n_agg || max_agg_size < 1) return MGPBD_EINVAL;
+  return guarded([&] {
+    std::vector<int32_t> a;
+    *n_agg = mgpbd::tet_aggregate(t_i, nt, max_agg_size, a);
+    std::memcpy(agg_ids, a.data(), sizeof(int32_t) * a.size());
+  });
+}
+
+int mgpbd_host_tet_hierarchy(const int32_t* t_i, int32_t nt, int32_t max_coarse,
+                             int32_t max_levels, int32_t* n_levels, int32_t* sizes,
+                             int32_t* agg_ids) {
+  if (!t_i || nt < 0 || !n_levels || !sizes || !agg_ids) return MGPBD_EINVAL;
+  return guarded([&] {
+    std::vector<int32_t> sz;
+    std::vector<std::vector<int32_t>> aggs;
+    mgpbd::tet_hierarchy(t_i, nt, max_coarse, max_levels, sz, aggs);
+    *n_levels = static_cast<int32_t>(sz.size());
+    std::memcpy(sizes, sz.data(), sizeof(int32_t) * sz.size());
+    if (!aggs.empty()) std::memcpy(agg_ids, aggs[0].data(), sizeof(int32_t) * aggs[0].size());
+  });
+}
+
+int mgpbd_host_galerkin(int32_t n, const int32_t* indptr, const int32_t* indices, const float* data,
+                        const int32_t* agg_ids, int32_t n_agg, int64_t* c_nnz, int64_t* n_contrib,
+                        int32_t* c_indptr, int32_t* c_indices, int32_t* contrib_idx,
+                        int32_t* contrib_off) {
+  if (n < 0 || !indptr || !indices || !data || !agg_ids || n_agg < 0 || !c_nnz || !n_contrib)
+    return MGPBD_EINVAL;
+  return guarded([&] {
+    mgpbd::Csr f;
+    f.n_rows = f.n_cols = n;
+    f.indptr.assign(indptr, indptr + n + 1);
+    f.indices.assign(indices, indices + indptr[n]);
+    mgpbd::Galerkin g = mgpbd::galerkin(f, data, agg_ids, n_agg);
+    *c_nnz = g.coarse.nnz();
+    *n_contrib = static_cast<int64_t>(g.contrib_idx.size());
+    if (c_indptr) {
+      mgpbd::require(c_indices && contrib_idx && contrib_off, MGPBD_EINVAL, "output buffer missing");
+      std::memcpy(c_indptr, g.coarse.indptr.data(), sizeof(int32_t) * g.coarse.indptr.size());
+      std::memcpy(c_indices, g.coarse.indices.data(), sizeof(int32_t) * g.coarse.indices.size());
+      std::memcpy(contrib_idx, g.contrib_idx.data(), sizeof(int32_t) * g.contrib_idx.size());
+      std::memcpy(contrib_off, g.contrib_off.data(), sizeof(int32_t) * g.contrib_off.size());
+    }
+  });
+}
+
+}  // extern "C"

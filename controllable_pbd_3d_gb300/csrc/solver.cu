@@ -1,0 +1,673 @@
+// MGPBD solver: the Newton loop of MGPBDSolverGPU (cons/mgpbd_gpu.py:397-446)
+// around the multigrid-preconditioned CG of GPUMultigridSolver
+// (cons/mgpcg_gpu.py:214-329), on one CUDA stream.
+#include "solver.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+namespace mgpbd {
+
+namespace {
+
+template <class T>
+void upload(DevBuf<T>& d, const std::vector<T>& h, cudaStream_t s) {
+  d.alloc(static_cast<int64_t>(h.size()));
+  if (!h.empty())
+    MGPBD_CUDA(cudaMemcpyAsync(d.p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, s));
+}
+
+// Power-iteration estimate of lambda_max(D^-1 A); the weight written to
+// *omega is min(omega_cap, 4 / (3 * 1.1 * lambda)).
+__global__ void k_pw_init(float* v, int32_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t h = static_cast<uint32_t>(i) * 2654435761u;
+    h ^= h >> 15;
+    v[i] = 0.5f + (h & 0xffff) * (1.0f / 65536.0f);
+  }
+}
+
+__global__ void k_pw_step(int32_t n, const int32_t* __restrict__ indptr,
+                          const int32_t* __restrict__ indices, const float* __restrict__ data,
+                          const float* __restrict__ dinv, const float* __restrict__ x,
+                          float* __restrict__ y, double* __restrict__ partials) {
+  __shared__ double sh[32];
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float s = 0.0f;
+    for (int32_t k = indptr[i]; k < indptr[i + 1]; ++k) s += data[k] * x[indices[k]];
+    float v = dinv[i] * s;
+    y[i] = v;
+    acc += (double)v * v;
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    acc = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+  }
+}
+
+__global__ void k_pw_scale(float* __restrict__ v, int32_t n, const double* __restrict__ nrm2) {
+  double s = nrm2[0];
+  float inv = s > 0.0 ? (float)(1.0 / sqrt(s)) : 0.0f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    v[i] *= inv;
+}
+
+__global__ void k_pw_weight(const double* __restrict__ nrm2, float omega_cap, float* omega) {
+  double lam = sqrt(nrm2[0]);
+  float w = omega_cap;
+  if (lam > 0.0 && isfinite(lam)) {
+    float safe = (float)(4.0 / (3.0 * 1.1 * lam));
+    w = safe < omega_cap ? safe : omega_cap;
+  }
+  *omega = w;
+}
+
+__global__ void k_set_cond(cudaGraphConditionalHandle h, const CgState* st) {
+  cudaGraphSetConditional(h, st->done ? 0u : 1u);
+}
+
+__global__ void k_fill_f32(float* p, float v, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = v;
+}
+
+}  // namespace
+
+Solver::Solver(const mgpbd_params& p) : p_(p) {
+  require(p.dt > 0.0f, MGPBD_EINVAL, "dt must be positive");
+  require(p.n_smooth >= 0 && p.maxiter >= 0 && p.maxiter_cg >= 0, MGPBD_EINVAL,
+          "iteration counts must be non-negative");
+  require(p.mode == MGPBD_MODE_PARITY || p.mode == MGPBD_MODE_FAST, MGPBD_EINVAL, "unknown mode");
+  MGPBD_CUDA(cudaMallocHost(&h_buf_, sizeof(double) * 64));
+  MGPBD_CUDA(cudaMallocHost(&h_state_, sizeof(CgState)));
+}
+
+Solver::~Solver() {
+  if (cg_exec_) cudaGraphExecDestroy(cg_exec_);
+  if (h_buf_) cudaFreeHost(h_buf_);
+  if (h_state_) cudaFreeHost(h_state_);
+}
+
+void Solver::require_init() const {
+  require(inited_, MGPBD_ESTATE, "mgpbd_init has not been called");
+}
+
+void Solver::set_mesh(const float* x_ref, const float* invm, const int32_t* t_i, int32_t nv,
+                      int32_t nt, float* x, float* v) {
+  require(x_ref && invm && t_i && x && v, MGPBD_EINVAL, "null mesh pointer");
+  require(nv > 0 && nt > 0, MGPBD_EINVAL, "empty mesh");
+  require(static_cast<int64_t>(nt) * 4 < INT32_MAX, MGPBD_ERANGE, "too many tets for int32 indices");
+  x_ref_ = x_ref;
+  invm_ = invm;
+  t_i_ = t_i;
+  nv_ = nv;
+  nt_ = nt;
+  x_ = x;
+  v_ = v;
+  inited_ = false;
+  if (cg_exec_) {
+    cudaGraphExecDestroy(cg_exec_);
+    cg_exec_ = nullptr;
+  }
+}
+
+void Solver::sync_read(void* host, const void* dev, size_t bytes) {
+  MGPBD_CUDA(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, stream_));
+  MGPBD_CUDA(cudaStreamSynchronize(stream_));
+}
+
+double Solver::finalize_read(const double* partials, int blocks) {
+  launch_finalize(partials, blocks, 1, scalars_.p, stream_);
+  sync_read(h_buf_, scalars_.p, sizeof(double));
+  return h_buf_[0];
+}
+
+// ---------------------------------------------------------------------------
+// MGPBDSolverGPU.init (cons/mgpbd_gpu.py:92-114)
+void Solver::init() {
+  require(x_ && t_i_, MGPBD_ESTATE, "mgpbd_set_mesh has not been called");
+  cudaStream_t s = stream_;
+  x_old_.alloc(3LL * nv_);
+  x_pred_.alloc(3LL * nv_);
+  dpos_.alloc(3LL * nv_);
+  dm_inv_.alloc(9LL * nt_);
+  rest_vol_.alloc(nt_);
+  alpha_.alloc(nt_);
+  lambda_.alloc(nt_);
+  C_.alloc(nt_);
+  gradC_.alloc(12LL * nt_);
+  rhs_.alloc(nt_);
+  dlam_.alloc(nt_);
+  MGPBD_CUDA(cudaMemsetAsync(lambda_.p, 0, sizeof(float) * nt_, s));
+  MGPBD_CUDA(cudaMemsetAsync(dpos_.p, 0, sizeof(float) * 3 * nv_, s));
+  MGPBD_CUDA(cudaMemsetAsync(x_old_.p, 0, sizeof(float) * 3 * nv_, s));
+  MGPBD_CUDA(cudaMemsetAsync(x_pred_.p, 0, sizeof(float) * 3 * nv_, s));
+  partials_.alloc(static_cast<int64_t>(kMaxReduceBlocks) * 16);
+  scalars_.alloc(64);
+  omegas_.alloc(16);
+  cg_state_.alloc(1);
+
+  launch_rest_shape(x_ref_, t_i_, nt_, p_.mu, p_.dt, dm_inv_.p, rest_vol_.p, alpha_.p, s);
+
+  std::vector<int32_t> t_host(4LL * nt_);
+  MGPBD_CUDA(cudaMemcpyAsync(t_host.data(), t_i_, sizeof(int32_t) * t_host.size(),
+                             cudaMemcpyDeviceToHost, s));
+  MGPBD_CUDA(cudaStreamSynchronize(s));
+  for (int32_t v : t_host)
+    require(v >= 0 && v < nv_, MGPBD_EINVAL, "t_i holds a vertex id outside [0, nv)");
+
+  // level-0 pattern (cons/mgpbd_gpu.py:153-194)
+  levels_.clear();
+  levels_.emplace_back();
+  Level& L0 = levels_[0];
+  L0.host = build_pattern(t_host.data(), nt_);
+  L0.n = nt_;
+  L0.nnz = L0.host.nnz();
+  upload(L0.indptr, L0.host.indptr, s);
+  upload(L0.indices, L0.host.indices, s);
+  L0.data.alloc(L0.nnz);
+  L0.diag_inv.alloc(nt_);
+
+  std::vector<int32_t> ip, ie;
+  vertex_incidence(t_host.data(), nt_, nv_, ip, ie);
+  upload(inc_ptr_, ip, s);
+  upload(inc_ent_, ie, s);
+
+  // first A at the current positions (cons/mgpbd_gpu.py:98-100)
+  launch_constraints(x_, t_i_, dm_inv_.p, nt_, C_.p, gradC_.p, s);
+  launch_fill_A(L0.indptr.p, L0.indices.p, t_i_, invm_, gradC_.p, alpha_.p, nt_, L0.data.p,
+                L0.diag_inv.p, s);
+  std::vector<float> a0(L0.nnz);
+  MGPBD_CUDA(cudaMemcpyAsync(a0.data(), L0.data.p, sizeof(float) * a0.size(),
+                             cudaMemcpyDeviceToHost, s));
+  MGPBD_CUDA(cudaStreamSynchronize(s));
+
+  build_hierarchy(t_host, a0);
+  alloc_work();
+  MGPBD_CUDA(cudaStreamSynchronize(s));
+  inited_ = true;
+  stats_ = mgpbd_stats{};
+  stats_.n_levels = n_levels();
+  for (int32_t l = 0; l < n_levels() && l < 8; ++l) {
+    stats_.rows[l] = levels_[l].n;
+    stats_.nnz[l] = levels_[l].nnz;
+  }
+}
+
+void Solver::build_hierarchy(const std::vector<int32_t>& t_host, const std::vector<float>& a0) {
+  cudaStream_t s = stream_;
+  int32_t max_coarse = p_.max_coarse > 0 ? p_.max_coarse : 400;
+  // tet hierarchy (cons/tet_aggregation.py:145-211, max_levels = 4)
+  std::vector<int32_t> sizes;
+  std::vector<std::vector<int32_t>> aggs;
+  tet_hierarchy(t_host.data(), nt_, max_coarse, 4, sizes, aggs);
+  std::vector<float> fine_vals = a0;
+  for (size_t l = 0; l < aggs.size(); ++l) {
+    Level& F = levels_[l];
+    int32_t n_agg = sizes[l + 1];
+    Galerkin g = galerkin(F.host, fine_vals.data(), aggs[l].data(), n_agg);
+    upload(F.agg, aggs[l], s);
+    std::vector<int32_t> mp(n_agg + 1, 0), mr(F.n);
+    for (int32_t i = 0; i < F.n; ++i) mp[aggs[l][i] + 1]++;
+    for (int32_t a = 0; a < n_agg; ++a) mp[a + 1] += mp[a];
+    {
+      std::vector<int32_t> cur(mp.begin(), mp.end() - 1);
+      for (int32_t i = 0; i < F.n; ++i) mr[cur[aggs[l][i]]++] = i;
+    }
+    upload(F.mem_ptr, mp, s);
+    upload(F.mem_rows, mr, s);
+    // host values of the coarse level (only needed if another value-based
+    // level follows; the tet hierarchy never has one)
+    std::vector<float> cv(g.coarse.nnz(), 0.0f);
+    for (int64_t c = 0; c < g.coarse.nnz(); ++c) {
+      float acc = 0.0f;
+      for (int32_t k = g.contrib_off[c]; k < g.contrib_off[c + 1]; ++k) acc += fine_vals[g.contrib_idx[k]];
+      cv[c] = acc;
+    }
+    levels_.emplace_back();
+    Level& C = levels_.back();
+    C.n = n_agg;
+    C.nnz = g.coarse.nnz();
+    upload(C.indptr, g.coarse.indptr, s);
+    upload(C.indices, g.coarse.indices, s);
+    upload(C.diag_pos, g.diag_pos, s);
+    upload(C.contrib_off, g.contrib_off, s);
+    upload(C.contrib_idx, g.contrib_idx, s);
+    C.data.alloc(C.nnz);
+    C.diag_inv.alloc(C.n);
+    C.host = std::move(g.coarse);
+    fine_vals.swap(cv);
+  }
+  // optional extra levels by matrix-graph aggregation (not in the reference,
+  // whose tet hierarchy stops at two levels)
+  int32_t extra = 0;
+  while (extra < p_.max_levels && levels_.back().n > max_coarse) {
+    Level& F = levels_.back();
+    std::vector<int32_t> agg;
+    int32_t n_agg = graph_aggregate(F.host, 8, agg);
+    if (n_agg >= F.n || n_agg <= 0) break;
+    Galerkin g = galerkin_structural(F.host, agg.data(), n_agg);
+    upload(F.agg, agg, s);
+    std::vector<int32_t> mp(n_agg + 1, 0), mr(F.n);
+    for (int32_t i = 0; i < F.n; ++i) mp[agg[i] + 1]++;
+    for (int32_t a = 0; a < n_agg; ++a) mp[a + 1] += mp[a];
+    {
+      std::vector<int32_t> cur(mp.begin(), mp.end() - 1);
+      for (int32_t i = 0; i < F.n; ++i) mr[cur[agg[i]]++] = i;
+    }
+    upload(F.mem_ptr, mp, s);
+    upload(F.mem_rows, mr, s);
+    levels_.emplace_back();
+    Level& C = levels_.back();
+    C.n = n_agg;
+    C.nnz = g.coarse.nnz();
+    upload(C.indptr, g.coarse.indptr, s);
+    upload(C.indices, g.coarse.indices, s);
+    upload(C.diag_pos, g.diag_pos, s);
+    upload(C.contrib_off, g.contrib_off, s);
+    upload(C.contrib_idx, g.contrib_idx, s);
+    C.data.alloc(C.nnz);
+    C.diag_inv.alloc(C.n);
+    C.host = std::move(g.coarse);
+    ++extra;
+  }
+  require(levels_.size() <= 8, MGPBD_ERANGE, "more than 8 multigrid levels");
+}
+
+void Solver::alloc_work() {
+  cudaStream_t s = stream_;
+  for (Level& L : levels_) {
+    L.b.alloc(L.n);
+    L.xa.alloc(L.n);
+    L.xb.alloc(L.n);
+    L.r.alloc(L.n);
+    L.omega.alloc(1);
+    k_fill_f32<<<1, 32, 0, s>>>(L.omega.p, p_.omega_jacobi, 1);
+    MGPBD_CHECK_LAUNCH();
+  }
+  cg_r_.alloc(nt_);
+  cg_z_.alloc(nt_);
+  cg_p_.alloc(nt_);
+  cg_ap_.alloc(nt_);
+  if (p_.smoother == MGPBD_SMOOTH_JACOBI_SAFE) {
+    int32_t nmax = 0;
+    for (Level& L : levels_) nmax = std::max(nmax, L.n);
+    pw_a_.alloc(static_cast<int64_t>(nmax) * levels_.size());
+    pw_b_.alloc(nmax);
+    int64_t off = 0;
+    for (Level& L : levels_) {
+      k_pw_init<<<std::max(1, ceil_div(L.n, 256)), 256, 0, s>>>(pw_a_.p + off, L.n);
+      MGPBD_CHECK_LAUNCH();
+      off += nmax;
+    }
+  }
+  if (p_.coarse_solver == MGPBD_COARSE_DENSE_F64) {
+    int32_t n = levels_.back().n;
+    require(n <= 4096, MGPBD_ERANGE, "coarsest level too large for the dense solve");
+    chol_.alloc(static_cast<int64_t>(n) * n);
+    chol_info_.alloc(1);
+  }
+}
+
+// ---------------------------------------------------------------------------
+void Solver::make_prediction() {
+  require_init();
+  launch_predict(x_, v_, x_old_.p, x_pred_.p, invm_, nv_, p_.dt, p_.gravity, p_.damp,
+                 p_.kinematic_pins, stream_);
+}
+
+void Solver::update_vel() {
+  require_init();
+  launch_update_vel(x_, x_old_.p, v_, nv_, p_.dt, p_.damp, stream_);
+}
+
+void Solver::step(int32_t frame) {
+  make_prediction();
+  solve(frame);
+  update_vel();
+}
+
+void Solver::compute_constraints() {
+  require_init();
+  launch_constraints(x_, t_i_, dm_inv_.p, nt_, C_.p, gradC_.p, stream_);
+}
+
+// _fill_A_and_update_gpu (cons/mgpbd_gpu.py:320-324)
+void Solver::fill_matrices() {
+  require_init();
+  cudaStream_t s = stream_;
+  Level& L0 = levels_[0];
+  launch_fill_A(L0.indptr.p, L0.indices.p, t_i_, invm_, gradC_.p, alpha_.p, nt_, L0.data.p,
+                L0.diag_inv.p, s);
+  for (size_t l = 1; l < levels_.size(); ++l) {
+    Level& C = levels_[l];
+    launch_rap_refill(C.contrib_off.p, C.contrib_idx.p, levels_[l - 1].data.p, C.nnz, C.data.p, s);
+    launch_diag_inv_pos(C.diag_pos.p, C.data.p, C.n, C.diag_inv.p, s);
+  }
+  if (p_.smoother == MGPBD_SMOOTH_JACOBI_SAFE) update_smoother_weights();
+  if (p_.coarse_solver == MGPBD_COARSE_DENSE_F64) factor_coarsest();
+}
+
+void Solver::update_smoother_weights() {
+  cudaStream_t s = stream_;
+  int32_t nmax = static_cast<int32_t>(pw_b_.n);
+  int64_t off = 0;
+  for (Level& L : levels_) {
+    int blocks = std::min(kMaxReduceBlocks, std::max(1, ceil_div(L.n, 256)));
+    float* a = pw_a_.p + off;
+    for (int it = 0; it < 6; ++it) {
+      k_pw_step<<<blocks, 256, 0, s>>>(L.n, L.indptr.p, L.indices.p, L.data.p, L.diag_inv.p, a,
+                                       pw_b_.p, partials_.p);
+      MGPBD_CHECK_LAUNCH();
+      launch_finalize(partials_.p, blocks, 1, scalars_.p + 8, s);
+      MGPBD_CUDA(cudaMemcpyAsync(a, pw_b_.p, sizeof(float) * L.n, cudaMemcpyDeviceToDevice, s));
+      k_pw_scale<<<blocks, 256, 0, s>>>(a, L.n, scalars_.p + 8);
+      MGPBD_CHECK_LAUNCH();
+    }
+    k_pw_weight<<<1, 1, 0, s>>>(scalars_.p + 8, p_.omega_jacobi, L.omega.p);
+    MGPBD_CHECK_LAUNCH();
+    off += nmax;
+  }
+}
+
+void Solver::factor_coarsest() {
+  Level& L = levels_.back();
+  launch_dense_chol_factor(L.view(), chol_.p, L.n, chol_info_.p, stream_);
+}
+
+double Solver::compute_rhs() {
+  require_init();
+  int blocks = reduce_blocks(nt_);
+  launch_rhs(C_.p, alpha_.p, lambda_.p, nt_, rhs_.p, partials_.p, stream_);
+  return std::sqrt(finalize_read(partials_.p, blocks));
+}
+
+// ---------------------------------------------------------------------------
+// Jacobi sweeps on level l (cons/sparse_gpu.py:134-144 + gpu_copy); cur holds
+// the iterate, nxt the scratch, and they swap after each sweep.
+void Solver::smooth_level(int32_t l, const float* b, float*& cur, float*& nxt, int sweeps,
+                          bool from_zero, const CgState* guard) {
+  Level& L = levels_[l];
+  CsrView A = L.view();
+  for (int it = 0; it < sweeps; ++it) {
+    bool zero = from_zero && it == 0 && p_.mode == MGPBD_MODE_FAST;
+    if (from_zero && it == 0 && !zero)
+      MGPBD_CUDA(cudaMemsetAsync(cur, 0, sizeof(float) * L.n, stream_));
+    launch_jacobi_gw(guard, A, b, zero ? nullptr : cur, nxt, p_.omega_jacobi, L.omega.p, stream_);
+    std::swap(cur, nxt);
+  }
+  if (sweeps == 0 && from_zero) MGPBD_CUDA(cudaMemsetAsync(cur, 0, sizeof(float) * L.n, stream_));
+}
+
+// GPUMultigridSolver.vcycle (cons/mgpcg_gpu.py:214-259) with a zero initial
+// guess; the result ends in levels_[l].xa.
+void Solver::vcycle(int32_t l, const float* b, const CgState* guard) {
+  Level& L = levels_[l];
+  float* cur = L.xa.p;
+  float* nxt = L.xb.p;
+  if (l == n_levels() - 1) {
+    if (p_.coarse_solver == MGPBD_COARSE_DENSE_F64) {
+      launch_dense_chol_solve(guard, chol_.p, L.n, b, L.xa.p, stream_);
+      return;
+    }
+    int sweeps = p_.coarse_sweeps > 0 ? p_.coarse_sweeps : std::min(50, L.n);
+    smooth_level(l, b, cur, nxt, sweeps, true, guard);
+  } else {
+    smooth_level(l, b, cur, nxt, p_.n_smooth, true, guard);
+    Level& C = levels_[l + 1];
+    launch_residual_g(guard, L.view(), b, cur, L.r.p, stream_);
+    launch_restrict_g(guard, L.mem_ptr.p, L.mem_rows.p, L.r.p, C.n, C.b.p, stream_);
+    vcycle(l + 1, C.b.p, guard);
+    launch_prolong_add_g(guard, L.agg.p, C.xa.p, L.n, cur, stream_);
+    smooth_level(l, b, cur, nxt, p_.n_smooth, false, guard);
+  }
+  if (cur != L.xa.p)
+    MGPBD_CUDA(cudaMemcpyAsync(L.xa.p, cur, sizeof(float) * L.n, cudaMemcpyDeviceToDevice, stream_));
+}
+
+void Solver::vcycle_into(const float* r, float* z) {
+  require_init();
+  vcycle(0, r, nullptr);
+  MGPBD_CUDA(cudaMemcpyAsync(z, levels_[0].xa.p, sizeof(float) * nt_, cudaMemcpyDeviceToDevice,
+                             stream_));
+}
+
+// One CG iteration (cons/mgpcg_gpu.py:289-327) on device scalars.
+void Solver::cg_body(const float* b, float* x) {
+  (void)b;
+  cudaStream_t s = stream_;
+  CgState* st = cg_state_.p;
+  int64_t n = nt_;
+  int blocks = reduce_blocks(n);
+  launch_spmv_dot_g(st, levels_[0].view(), cg_p_.p, cg_ap_.p, partials_.p, s);
+  launch_cg_alpha(st, partials_.p, blocks, s);
+  launch_cg_update_xr(st, cg_p_.p, cg_ap_.p, x, cg_r_.p, n, partials_.p, s);
+  launch_cg_check(st, partials_.p, blocks, s);
+  vcycle(0, cg_r_.p, st);
+  launch_dot_partials_g(st, cg_r_.p, levels_[0].xa.p, n, partials_.p, s);
+  launch_cg_beta(st, partials_.p, blocks, s);
+  launch_cg_update_p(st, levels_[0].xa.p, cg_p_.p, n, s);
+}
+
+// GPUMultigridSolver.solve (cons/mgpcg_gpu.py:261-329)
+int32_t Solver::pcg(const float* b, float* x) {
+  require_init();
+  if (p_.mode == MGPBD_MODE_FAST && b == rhs_.p && x == dlam_.p) return pcg_graph(b, x);
+  cudaStream_t s = stream_;
+  int64_t n = nt_;
+  int blocks = reduce_blocks(n);
+  MGPBD_CUDA(cudaMemsetAsync(x, 0, sizeof(float) * n, s));
+  MGPBD_CUDA(cudaMemcpyAsync(cg_r_.p, b, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+  vcycle(0, cg_r_.p, nullptr);
+  MGPBD_CUDA(cudaMemcpyAsync(cg_p_.p, levels_[0].xa.p, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+  launch_dot_partials(cg_r_.p, levels_[0].xa.p, n, partials_.p, s);
+  launch_dot_partials(b, b, n, partials_.p + blocks, s);
+  launch_cg_init(cg_state_.p, partials_.p, blocks, p_.tol_cg, p_.rel_tol_cg, p_.maxiter_cg, s);
+  for (int32_t k = 0; k < p_.maxiter_cg; ++k) {
+    cg_body(b, x);
+    sync_read(h_state_, cg_state_.p, sizeof(CgState));
+    if (h_state_->done) break;
+  }
+  sync_read(h_state_, cg_state_.p, sizeof(CgState));
+  status_ |= static_cast<uint32_t>(h_state_->status);
+  return h_state_->iters;
+}
+
+// FAST mode: the whole CG loop is one CUDA graph whose iterations run under a
+// device-side while condition (no host round trip per iteration).  The loop
+// is bounded on the device by maxiter_cg (k_cg_beta sets done).
+int32_t Solver::pcg_graph(const float* b, float* x) {
+  cudaStream_t outer = stream_;
+  if (!cg_exec_ || cg_graph_b_ != b || cg_graph_x_ != x) {
+    if (cg_exec_) {
+      cudaGraphExecDestroy(cg_exec_);
+      cg_exec_ = nullptr;
+    }
+    cudaStream_t cs, bs;
+    MGPBD_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    MGPBD_CUDA(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking));
+    cudaGraph_t graph = nullptr;
+    try {
+      int64_t n = nt_;
+      int blocks = reduce_blocks(n);
+      MGPBD_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+      stream_ = cs;
+      MGPBD_CUDA(cudaMemsetAsync(x, 0, sizeof(float) * n, cs));
+      MGPBD_CUDA(cudaMemcpyAsync(cg_r_.p, b, sizeof(float) * n, cudaMemcpyDeviceToDevice, cs));
+      vcycle(0, cg_r_.p, nullptr);
+      MGPBD_CUDA(cudaMemcpyAsync(cg_p_.p, levels_[0].xa.p, sizeof(float) * n, cudaMemcpyDeviceToDevice, cs));
+      launch_dot_partials(cg_r_.p, levels_[0].xa.p, n, partials_.p, cs);
+      launch_dot_partials(b, b, n, partials_.p + blocks, cs);
+      launch_cg_init(cg_state_.p, partials_.p, blocks, p_.tol_cg, p_.rel_tol_cg, p_.maxiter_cg, cs);
+      cudaStreamCaptureStatus cst;
+      const cudaGraphNode_t* deps = nullptr;
+      size_t ndeps = 0;
+      MGPBD_CUDA(cudaStreamGetCaptureInfo(cs, &cst, nullptr, &graph, &deps, nullptr, &ndeps));
+      cudaGraphConditionalHandle handle;
+      MGPBD_CUDA(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
+      cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+      cp.conditional.handle = handle;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      cudaGraphNode_t cond;
+      MGPBD_CUDA(cudaGraphAddNode(&cond, graph, deps, nullptr, ndeps, &cp));
+      cudaGraph_t body = cp.conditional.phGraph_out[0];
+      MGPBD_CUDA(cudaStreamUpdateCaptureDependencies(cs, &cond, nullptr, 1, cudaStreamSetCaptureDependencies));
+      MGPBD_CUDA(cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+      stream_ = bs;
+      cg_body(b, x);
+      k_set_cond<<<1, 1, 0, bs>>>(handle, cg_state_.p);
+      MGPBD_CHECK_LAUNCH();
+      MGPBD_CUDA(cudaStreamEndCapture(bs, &body));
+      stream_ = outer;
+      MGPBD_CUDA(cudaStreamEndCapture(cs, &graph));
+      MGPBD_CUDA(cudaGraphInstantiate(&cg_exec_, graph, 0));
+      cudaGraphDestroy(graph);
+    } catch (...) {
+      stream_ = outer;
+      cudaStreamCaptureStatus cst;
+      if (cudaStreamIsCapturing(bs, &cst) == cudaSuccess && cst != cudaStreamCaptureStatusNone) {
+        cudaGraph_t g2;
+        cudaStreamEndCapture(bs, &g2);
+      }
+      if (cudaStreamIsCapturing(cs, &cst) == cudaSuccess && cst != cudaStreamCaptureStatusNone) {
+        cudaGraph_t g2 = nullptr;
+        cudaStreamEndCapture(cs, &g2);
+        if (g2) cudaGraphDestroy(g2);
+      }
+      cudaGetLastError();
+      cudaStreamDestroy(cs);
+      cudaStreamDestroy(bs);
+      throw;
+    }
+    cudaStreamDestroy(cs);
+    cudaStreamDestroy(bs);
+    cg_graph_b_ = b;
+    cg_graph_x_ = x;
+  }
+  MGPBD_CUDA(cudaGraphLaunch(cg_exec_, outer));
+  sync_read(h_state_, cg_state_.p, sizeof(CgState));
+  status_ |= static_cast<uint32_t>(h_state_->status);
+  return h_state_->iters;
+}
+
+// _zero_dpos + _scatter_dlam_gpu (cons/mgpbd_gpu.py:330-355)
+void Solver::scatter(const float* dlam) {
+  require_init();
+  launch_lambda_update(lambda_.p, dlam, nt_, stream_);
+  launch_scatter(inc_ptr_.p, inc_ent_.p, invm_, dlam, gradC_.p, dpos_.p, nv_, stream_);
+}
+
+// _line_search (cons/mgpbd_gpu.py:379-391): backtracking from omega = 1 by
+// halves, at most 10 trials, accept the first trial whose dual residual is
+// below the one at the current positions (with the updated lambda).  The
+// current norm reuses C of this Newton iteration (same positions, same
+// arithmetic as recomputing it); trials 2..10 are evaluated in one pass
+// only when trial 1 fails.
+double Solver::line_search() {
+  require_init();
+  cudaStream_t s = stream_;
+  int blocks = reduce_blocks(nt_);
+  h_buf_[0] = 1.0;
+  MGPBD_CUDA(cudaMemcpyAsync(omegas_.p, h_buf_, sizeof(double), cudaMemcpyHostToDevice, s));
+  launch_dual_sq(C_.p, alpha_.p, lambda_.p, nt_, partials_.p, s);
+  launch_dual_trial(x_, dpos_.p, omegas_.p, 1, t_i_, dm_inv_.p, alpha_.p, lambda_.p, nt_,
+                    partials_.p + blocks, s);
+  launch_finalize(partials_.p, blocks, 2, scalars_.p, s);
+  sync_read(h_buf_, scalars_.p, 2 * sizeof(double));
+  double current = std::sqrt(h_buf_[0]);
+  double trial = std::sqrt(h_buf_[1]);
+  if (trial < current) return 1.0;
+  double om[9];
+  for (int k = 0; k < 9; ++k) om[k] = std::ldexp(1.0, -(k + 1));
+  std::memcpy(h_buf_, om, sizeof(om));
+  MGPBD_CUDA(cudaMemcpyAsync(omegas_.p, h_buf_, sizeof(om), cudaMemcpyHostToDevice, s));
+  launch_dual_trial(x_, dpos_.p, omegas_.p, 9, t_i_, dm_inv_.p, alpha_.p, lambda_.p, nt_,
+                    partials_.p, s);
+  launch_finalize(partials_.p, blocks, 9, scalars_.p, s);
+  sync_read(h_buf_, scalars_.p, 9 * sizeof(double));
+  for (int k = 0; k < 9; ++k)
+    if (std::sqrt(h_buf_[k]) < current) return om[k];
+  return std::ldexp(1.0, -10);
+}
+
+void Solver::apply_dpos(double omega) {
+  require_init();
+  launch_apply(x_, dpos_.p, invm_, nv_, static_cast<float>(omega), stream_);
+}
+
+// MGPBDSolverGPU.solve (cons/mgpbd_gpu.py:397-446)
+void Solver::solve(int32_t frame) {
+  (void)frame;
+  require_init();
+  status_ = 0;
+  MGPBD_CUDA(cudaMemsetAsync(lambda_.p, 0, sizeof(float) * nt_, stream_));
+  double r0 = 0.0;
+  stats_.newton_iters = 0;
+  stats_.cg_iters_total = 0;
+  stats_.cg_iters_last = 0;
+  stats_.omega_last = 1.0;
+  for (int32_t ite = 0; ite < p_.maxiter; ++ite) {
+    compute_constraints();
+    double r = compute_rhs();
+    if (ite == 0) {
+      r0 = r;
+      stats_.residual0 = r;
+    }
+    stats_.residual = r;
+    if (!std::isfinite(r)) {
+      status_ |= MGPBD_STATUS_NAN;
+      break;
+    }
+    if (r < p_.atol || (r0 > 1e-12 && r < p_.rtol * r0)) break;
+    fill_matrices();
+    int32_t it = pcg(rhs_.p, dlam_.p);
+    scatter(dlam_.p);
+    double omega = p_.use_line_search ? line_search() : 1.0;
+    apply_dpos(omega);
+    stats_.newton_iters = ite + 1;
+    stats_.cg_iters_total += it;
+    stats_.cg_iters_last = it;
+    stats_.omega_last = omega;
+    if (ite + 1 == p_.maxiter) status_ |= MGPBD_STATUS_NEWTON_MAXITER;
+  }
+  stats_.status = status_;
+}
+
+void* Solver::field(int32_t id, int64_t* count) {
+  require_init();
+  switch (id) {
+    case MGPBD_FIELD_LAMBDA: *count = nt_; return lambda_.p;
+    case MGPBD_FIELD_CONSTRAINTS: *count = nt_; return C_.p;
+    case MGPBD_FIELD_GRADC: *count = 12LL * nt_; return gradC_.p;
+    case MGPBD_FIELD_ALPHA_TILDE: *count = nt_; return alpha_.p;
+    case MGPBD_FIELD_REST_VOL: *count = nt_; return rest_vol_.p;
+    case MGPBD_FIELD_DM_INV: *count = 9LL * nt_; return dm_inv_.p;
+    case MGPBD_FIELD_X_OLD: *count = 3LL * nv_; return x_old_.p;
+    case MGPBD_FIELD_X_PREDICT: *count = 3LL * nv_; return x_pred_.p;
+    case MGPBD_FIELD_DPOS: *count = 3LL * nv_; return dpos_.p;
+    case MGPBD_FIELD_RHS: *count = nt_; return rhs_.p;
+    case MGPBD_FIELD_DLAMBDA: *count = nt_; return dlam_.p;
+    case MGPBD_FIELD_A_DATA: *count = levels_[0].nnz; return levels_[0].data.p;
+    default: throw Error(MGPBD_EINVAL, "unknown field id");
+  }
+}
+
+const Level& Solver::level(int32_t l) const {
+  require_init();
+  require(l >= 0 && l < n_levels(), MGPBD_EINVAL, "level out of range");
+  return levels_[l];
+}
+
+}  // namespace mgpbd

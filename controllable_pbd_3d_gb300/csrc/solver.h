@@ -1,0 +1,123 @@
+// The MGPBD solver object behind the C ABI (one body, one stream).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <vector>
+
+#include "common.h"
+#include "kernels.cuh"
+#include "structure.h"
+
+namespace mgpbd {
+
+struct Level {
+  int32_t n = 0;
+  int64_t nnz = 0;
+  DevBuf<int32_t> indptr, indices, diag_pos;
+  DevBuf<float> data, diag_inv;
+  // transfer to level+1 (absent on the coarsest level)
+  DevBuf<int32_t> agg, mem_ptr, mem_rows;
+  // Galerkin refill of this level from level-1 values (absent on level 0)
+  DevBuf<int32_t> contrib_off, contrib_idx;
+  // work vectors of the V-cycle
+  DevBuf<float> b, xa, xb, r;
+  // smoother weight used by the Jacobi sweeps of this level (device scalar)
+  DevBuf<float> omega;
+  // host copies of the structure (kept for the level below)
+  Csr host;
+  CsrView view() const {
+    CsrView v;
+    v.n = n;
+    v.nnz = nnz;
+    v.indptr = indptr.p;
+    v.indices = indices.p;
+    v.data = data.p;
+    v.diag_inv = diag_inv.p;
+    return v;
+  }
+};
+
+class Solver {
+ public:
+  explicit Solver(const mgpbd_params& p);
+  ~Solver();
+
+  void set_stream(cudaStream_t s) { stream_ = s; }
+  void set_mesh(const float* x_ref, const float* invm, const int32_t* t_i, int32_t nv, int32_t nt,
+                float* x, float* v);
+  void init();
+  void step(int32_t frame);
+  void make_prediction();
+  void solve(int32_t frame);
+  void update_vel();
+
+  // per-stage entry points
+  void compute_constraints();
+  void fill_matrices();
+  double compute_rhs();
+  int32_t pcg(const float* b, float* x);
+  void vcycle_into(const float* r, float* z);
+  void scatter(const float* dlam);
+  double line_search();
+  void apply_dpos(double omega);
+
+  const mgpbd_stats& stats() const { return stats_; }
+  uint32_t status() const { return status_; }
+  void* field(int32_t id, int64_t* count);
+  const Level& level(int32_t l) const;
+  int32_t n_levels() const { return static_cast<int32_t>(levels_.size()); }
+  cudaStream_t stream() const { return stream_; }
+
+ private:
+  void require_init() const;
+  void build_hierarchy(const std::vector<int32_t>& t_i_host, const std::vector<float>& a0);
+  void alloc_work();
+  // V-cycle on `l` with rhs b_l (device) and zero initial guess; the result
+  // is left in levels_[l].xa.
+  void vcycle(int32_t l, const float* b, const CgState* guard);
+  void smooth_level(int32_t l, const float* b, float*& cur, float*& nxt, int sweeps,
+                    bool from_zero, const CgState* guard);
+  void update_smoother_weights();
+  void factor_coarsest();
+  void cg_body(const float* b, float* x);
+  int32_t pcg_graph(const float* b, float* x);
+  void sync_read(void* host, const void* dev, size_t bytes);
+  double finalize_read(const double* partials, int blocks);
+
+  mgpbd_params p_;
+  cudaStream_t stream_ = nullptr;
+  const float* x_ref_ = nullptr;
+  const float* invm_ = nullptr;
+  const int32_t* t_i_ = nullptr;
+  float* x_ = nullptr;
+  float* v_ = nullptr;
+  int32_t nv_ = 0, nt_ = 0;
+  bool inited_ = false;
+
+  DevBuf<float> x_old_, x_pred_, dpos_;
+  DevBuf<float> dm_inv_, rest_vol_, alpha_, lambda_, C_, gradC_, rhs_, dlam_;
+  DevBuf<int32_t> inc_ptr_, inc_ent_;
+  std::vector<Level> levels_;
+
+  DevBuf<float> cg_r_, cg_z_, cg_p_, cg_ap_;
+  DevBuf<double> partials_, scalars_, omegas_;
+  DevBuf<CgState> cg_state_;
+  DevBuf<double> chol_;
+  DevBuf<int32_t> chol_info_;
+  DevBuf<float> pw_a_, pw_b_;  // power-iteration vectors
+  double* h_buf_ = nullptr;    // pinned host scratch
+  CgState* h_state_ = nullptr;
+
+  // captured CG loop (FAST mode)
+  cudaGraphExec_t cg_exec_ = nullptr;
+  const float* cg_graph_b_ = nullptr;
+  float* cg_graph_x_ = nullptr;
+
+  mgpbd_stats stats_{};
+  uint32_t status_ = 0;
+};
+
+}  // namespace mgpbd

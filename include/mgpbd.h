@@ -1,0 +1,248 @@
+/*
+ * mgpbd.h - C ABI of libmgpbd.so, a GB300 (sm_103a) implementation of the
+ * MGPBD global XPBD step of JamesYang-7/Controllable_PBD_3D.
+ *
+ * The reference exposes this step as the Python class `MGPBDSolverGPU`
+ * (cons/mgpbd_gpu.py:20-446) backed by `GPUMultigridSolver`
+ * (cons/mgpcg_gpu.py:17-329), `GPUSparseMatrix` and free BLAS-1 kernels
+ * (cons/sparse_gpu.py:18-144) and the host hierarchy builder
+ * (cons/tet_aggregation.py:11-211).  Each entry point below names the
+ * reference symbol it replaces.
+ *
+ * Conventions
+ *  - Every function returns 0 on success or a negative MGPBD_E* code;
+ *    mgpbd_strerror() turns it into text.  Nothing throws across the ABI.
+ *  - Array arguments documented as "device" are CUDA device pointers owned
+ *    by the caller; they must stay valid while the handle uses them.  Arrays
+ *    documented as "host" are ordinary host memory.
+ *  - A handle is used from one host thread at a time and issues its work on
+ *    the stream given to mgpbd_set_stream (default: the legacy stream).
+ *    Separate handles are independent.
+ *  - Layouts follow the reference's Taichi fields: positions (NV,3) float32,
+ *    flat tet indices t_i (4*NT) int32, per-tet gradients (NT,4,3) float32,
+ *    CSR matrices as (indptr int32[n+1], indices int32[nnz], data float32[nnz]).
+ */
+#ifndef MGPBD_H_
+#define MGPBD_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- error codes -------------------------------------------------------- */
+#define MGPBD_OK 0
+#define MGPBD_EINVAL -1      /* bad argument (null pointer, size, order)      */
+#define MGPBD_ECUDA -2       /* a CUDA runtime call failed                    */
+#define MGPBD_ENOMEM -3      /* device or host allocation failed              */
+#define MGPBD_ESTATE -4      /* call out of order (e.g. step before init)     */
+#define MGPBD_ENUMERIC -5    /* NaN/Inf met in the solve (status word set)    */
+#define MGPBD_ERANGE -6      /* size beyond an index-type or table limit      */
+#define MGPBD_ENOTSUP -7     /* option not supported by this build            */
+
+/* ---- device status word bits (mgpbd_get_status) ------------------------- */
+#define MGPBD_STATUS_NAN 1u          /* non-finite residual / scalar seen      */
+#define MGPBD_STATUS_PAP_NONPOS 2u   /* CG curvature p.Ap <= 0                 */
+#define MGPBD_STATUS_CG_MAXITER 4u   /* a CG solve hit maxiter_cg              */
+#define MGPBD_STATUS_NEWTON_MAXITER 8u /* the Newton loop hit maxiter          */
+#define MGPBD_STATUS_STALL 16u       /* CG residual stopped decreasing         */
+
+/* ---- solver options ------------------------------------------------------ */
+/* Algorithm variants.  PARITY reproduces the reference step
+ * (cons/mgpbd_gpu.py:397-446 with cons/mgpcg_gpu.py:214-329): weighted
+ * Jacobi smoothing with omega_jacobi, min(50, n) Jacobi sweeps on the
+ * coarsest level, absolute CG tolerance tol_cg, host-checked loops.
+ * FAST keeps the same Newton/PCG structure but runs every loop on the device
+ * (scalars never leave the GPU inside a CG solve), smooths with a weight set
+ * from an estimate of lambda_max(D^-1 A) so the smoother cannot diverge on
+ * stiff material, solves the coarsest level densely in float64 and stops CG
+ * on the relative residual rel_tol_cg as well as tol_cg. */
+#define MGPBD_MODE_PARITY 0
+#define MGPBD_MODE_FAST 1
+
+#define MGPBD_COARSE_JACOBI 0    /* min(50,n) weighted Jacobi sweeps (ref)    */
+#define MGPBD_COARSE_DENSE_F64 1 /* float64 Cholesky of the coarsest matrix   */
+
+#define MGPBD_SMOOTH_JACOBI 0    /* x += w D^-1 (b - A x), w = omega_jacobi   */
+#define MGPBD_SMOOTH_JACOBI_SAFE 1 /* same, w = min(omega, 4/(3 lmax)) per level */
+
+typedef struct mgpbd_params {
+  /* reference constructor arguments (cons/mgpbd_gpu.py:22-42) */
+  float dt;
+  float mu;
+  float damp;
+  float gravity[3];
+  int32_t maxiter;
+  float atol;
+  float rtol;
+  int32_t maxiter_cg;
+  float tol_cg;
+  int32_t n_smooth;
+  float omega_jacobi;
+  int32_t setup_interval; /* accepted, unused (as in the reference GPU path) */
+  int32_t use_line_search;
+  /* extensions (defaults from mgpbd_default_params reproduce the reference) */
+  int32_t mode;           /* MGPBD_MODE_*                                     */
+  float rel_tol_cg;       /* 0: absolute tol_cg only (reference)              */
+  int32_t coarse_solver;  /* MGPBD_COARSE_*                                   */
+  int32_t smoother;       /* MGPBD_SMOOTH_*                                   */
+  int32_t max_levels;     /* extra levels by matrix-graph aggregation (0=ref) */
+  int32_t max_coarse;     /* coarsest-level target size (reference: 400)      */
+  int32_t kinematic_pins; /* 1: invm==0 vertices skip the prediction          */
+  int32_t coarse_sweeps;  /* coarsest Jacobi sweeps, 0 = min(50,n) (ref)      */
+} mgpbd_params;
+
+typedef struct mgpbd_stats {
+  int32_t newton_iters;     /* Newton iterations run in the last solve        */
+  int32_t cg_iters_total;   /* CG iterations summed over those                */
+  int32_t cg_iters_last;    /* CG iterations of the last Newton iteration     */
+  int32_t n_levels;         /* multigrid levels                               */
+  double residual0;         /* dual residual norm at Newton iteration 0       */
+  double residual;          /* dual residual norm at the last check           */
+  double omega_last;        /* last line-search step                          */
+  uint32_t status;          /* MGPBD_STATUS_* bits of the last solve          */
+  int64_t nnz[8];           /* nonzeros per level                             */
+  int64_t rows[8];          /* rows per level                                 */
+} mgpbd_stats;
+
+typedef struct mgpbd_solver* mgpbd_handle;
+
+/* Fill *p with the reference's defaults (cons/mgpbd_gpu.py:30-41):
+ * mu 1e6, damp 1, maxiter 20, atol 1e-4, rtol 1e-2, maxiter_cg 100,
+ * tol_cg 1e-5, n_smooth 2, omega 2/3, setup_interval 10000, line search on,
+ * PARITY mode; dt and gravity are zeroed and must be set by the caller. */
+void mgpbd_default_params(mgpbd_params* p);
+
+const char* mgpbd_strerror(int code);
+/* Text of the last error raised on the calling thread (empty if none). */
+const char* mgpbd_last_error(void);
+const char* mgpbd_version(void);
+
+/* Replaces MGPBDSolverGPU.__init__ (cons/mgpbd_gpu.py:22-90). */
+int mgpbd_create(const mgpbd_params* params, mgpbd_handle* out);
+void mgpbd_destroy(mgpbd_handle h);
+/* cudaStream_t passed as void* so the header needs no CUDA include. */
+int mgpbd_set_stream(mgpbd_handle h, void* stream);
+
+/* Bind the caller's mesh (device): rest positions x_ref (nv,3), inverse
+ * masses invm (nv), tet indices t_i (4*nt), and the state arrays the step
+ * mutates: positions x (nv,3) and velocities v (nv,3).  Replaces the
+ * constructor's field arguments (cons/mgpbd_gpu.py:22-28,43-49). */
+int mgpbd_set_mesh(mgpbd_handle h, const float* x_ref, const float* invm,
+                   const int32_t* t_i, int32_t nv, int32_t nt, float* x,
+                   float* v);
+
+/* Replaces MGPBDSolverGPU.init (cons/mgpbd_gpu.py:92-114): rest shape,
+ * sparsity pattern, first A, tet hierarchy, multigrid setup. */
+int mgpbd_init(mgpbd_handle h);
+
+/* Replaces MGPBDSolverGPU.step / make_prediction / solve / update_vel
+ * (cons/mgpbd_gpu.py:200-219,397-446). */
+int mgpbd_step(mgpbd_handle h, int32_t frame);
+int mgpbd_make_prediction(mgpbd_handle h);
+int mgpbd_solve(mgpbd_handle h, int32_t frame);
+int mgpbd_update_vel(mgpbd_handle h);
+
+int mgpbd_get_stats(mgpbd_handle h, mgpbd_stats* out);
+/* Block until the handle's stream has finished its queued work. */
+int mgpbd_synchronize(mgpbd_handle h);
+/* Status bits of the last solve (0 = clean). */
+int mgpbd_get_status(mgpbd_handle h, uint32_t* status);
+
+/* Device pointer and element count of a solver-owned field, so a caller can
+ * read or (for alpha_tilde, lambda) modify it in place.  Field ids: */
+#define MGPBD_FIELD_LAMBDA 0      /* (nt)      lambdaf                         */
+#define MGPBD_FIELD_CONSTRAINTS 1 /* (nt)      constraints                     */
+#define MGPBD_FIELD_GRADC 2       /* (nt,4,3)  gradC                           */
+#define MGPBD_FIELD_ALPHA_TILDE 3 /* (nt)      alpha_tilde                     */
+#define MGPBD_FIELD_REST_VOL 4    /* (nt)      rest_vol                        */
+#define MGPBD_FIELD_DM_INV 5      /* (nt,3,3)  Dm_inv                          */
+#define MGPBD_FIELD_X_OLD 6       /* (nv,3)    v_p_old                         */
+#define MGPBD_FIELD_X_PREDICT 7   /* (nv,3)    v_predict                       */
+#define MGPBD_FIELD_DPOS 8        /* (nv,3)    dpos                            */
+#define MGPBD_FIELD_RHS 9         /* (nt)      _b_gpu                          */
+#define MGPBD_FIELD_DLAMBDA 10    /* (nt)      _dlam_gpu                       */
+#define MGPBD_FIELD_A_DATA 11     /* (nnz0)    level-0 matrix values           */
+int mgpbd_field(mgpbd_handle h, int32_t field, void** dev_ptr, int64_t* count);
+
+/* CSR arrays of multigrid level `level` (device pointers, library-owned).
+ * Level 0 keeps the reference's pattern: per row the sorted neighbours,
+ * then the diagonal last (cons/mgpbd_gpu.py:153-194). */
+int mgpbd_level_csr(mgpbd_handle h, int32_t level, int32_t* n_rows, int64_t* nnz,
+                    int32_t** indptr, int32_t** indices, float** data,
+                    float** diag_inv);
+/* Number of multigrid levels after mgpbd_init. */
+int mgpbd_level_count(mgpbd_handle h, int32_t* n_levels);
+/* Aggregate id of each row of `level` (device, length n_rows(level)). */
+int mgpbd_level_agg(mgpbd_handle h, int32_t level, int32_t** agg_ids);
+
+/* ---- per-stage calls (the reference's separately callable kernels) ------ */
+/* _compute_C_and_gradC (cons/mgpbd_gpu.py:225-247) at the bound positions */
+int mgpbd_compute_constraints(mgpbd_handle h);
+/* _fill_A_and_update_gpu (cons/mgpbd_gpu.py:320-324): A values, diag^-1,
+ * coarse values by the contribution map (cons/mgpcg_gpu.py:175-212) */
+int mgpbd_fill_matrices(mgpbd_handle h);
+/* _compute_rhs_gpu + _residual_norm_gpu (cons/mgpbd_gpu.py:253-267) */
+int mgpbd_compute_rhs(mgpbd_handle h, double* residual_norm);
+/* GPUMultigridSolver.solve (cons/mgpcg_gpu.py:261-329): solves A x = b on
+ * level 0 for device vectors b, x (nt); returns the CG iteration count. */
+int mgpbd_pcg(mgpbd_handle h, const float* b, float* x, int32_t* cg_iters);
+/* GPUMultigridSolver.vcycle(0) (cons/mgpcg_gpu.py:214-259): z = M^-1 r */
+int mgpbd_vcycle(mgpbd_handle h, const float* r, float* z);
+/* _zero_dpos + _scatter_dlam_gpu (cons/mgpbd_gpu.py:330-355) for dlam */
+int mgpbd_scatter(mgpbd_handle h, const float* dlam);
+/* _line_search (cons/mgpbd_gpu.py:379-391); returns omega */
+int mgpbd_line_search(mgpbd_handle h, double* omega);
+/* _apply_dpos (cons/mgpbd_gpu.py:345-349) */
+int mgpbd_apply_dpos(mgpbd_handle h, double omega);
+
+/* ---- standalone sparse kernels on caller CSR (device arrays) ------------ */
+/* GPUSparseMatrix.spmv (cons/sparse_gpu.py:123-132): y = A x */
+int mgpbd_csr_spmv(int32_t n_rows, const int32_t* indptr, const int32_t* indices,
+                   const float* data, const float* x, float* y, void* stream);
+/* GPUSparseMatrix.jacobi_smooth (cons/sparse_gpu.py:134-144):
+ * x_new = x + omega * diag_inv * (b - A x) */
+int mgpbd_csr_jacobi(int32_t n_rows, const int32_t* indptr, const int32_t* indices,
+                     const float* data, const float* diag_inv, const float* b,
+                     const float* x, float* x_new, float omega, void* stream);
+/* GPUSparseMatrix.cache_diag_inv (cons/sparse_gpu.py:107-121) */
+int mgpbd_csr_diag_inv(int32_t n_rows, const int32_t* indptr, const int32_t* indices,
+                       const float* data, float* diag_inv, void* stream);
+/* gpu_dot (cons/sparse_gpu.py:18-23); float64 accumulation, fixed order */
+int mgpbd_dot(int32_t n, const float* a, const float* b, double* out, void* stream);
+/* gpu_axpy (:26-30) y += alpha x ; gpu_xpay (:33-37) y = x + alpha y */
+int mgpbd_axpy(int32_t n, float alpha, const float* x, float* y, void* stream);
+int mgpbd_xpay(int32_t n, float alpha, const float* x, float* y, void* stream);
+
+/* ---- host-side structure builders (host arrays, no GPU needed) ---------- */
+/* _build_sparsity_pattern (cons/mgpbd_gpu.py:153-194).  Call with indptr ==
+ * NULL to get *nnz, then again with indptr (nt+1) and indices (*nnz). */
+int mgpbd_host_pattern(const int32_t* t_i, int32_t nt, int64_t* nnz,
+                       int32_t* indptr, int32_t* indices);
+/* tet_geometry_aggregation pass 1 (cons/tet_aggregation.py:40-127), with
+ * the reference's tie order reproduced; agg_ids has nt entries. */
+int mgpbd_host_aggregate(const int32_t* t_i, int32_t nt, int32_t max_agg_size,
+                         int32_t* agg_ids, int32_t* n_agg);
+/* build_tet_hierarchy (cons/tet_aggregation.py:145-211): level sizes
+ * (sizes[0] = nt) and the level-0 aggregate ids; returns *n_levels (1 or 2). */
+int mgpbd_host_tet_hierarchy(const int32_t* t_i, int32_t nt, int32_t max_coarse,
+                             int32_t max_levels, int32_t* n_levels,
+                             int32_t* sizes, int32_t* agg_ids);
+/* Galerkin coarse pattern of P^T A P with scipy's exact-zero dropping and
+ * the contribution map of cons/mgpcg_gpu.py:46-99 for piecewise-constant P.
+ * Call with c_indptr == NULL to get *c_nnz and *n_contrib, then again with
+ * c_indptr (n_agg+1), c_indices (*c_nnz), contrib_idx (*n_contrib) and
+ * contrib_off (*c_nnz+1). */
+int mgpbd_host_galerkin(int32_t n, const int32_t* indptr, const int32_t* indices,
+                        const float* data, const int32_t* agg_ids, int32_t n_agg,
+                        int64_t* c_nnz, int64_t* n_contrib, int32_t* c_indptr,
+                        int32_t* c_indices, int32_t* contrib_idx,
+                        int32_t* contrib_off);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MGPBD_H_ */

@@ -1,0 +1,340 @@
+"""Generate the golden fixtures by running the reference's own solver code.
+
+Usage (needs a checkout of JamesYang-7/Controllable_PBD_3D; not available on
+the GPU machines, which only read the committed `.npz` files):
+
+    python tests/golden/make_golden.py --ref /root/reference [--only structure|step]
+
+Taichi is not installed, so `taichi_cpu_shim` stands in for it (see that
+module's docstring for what it can and cannot reproduce).  The reference
+modules are imported unmodified:
+
+* `cons/tet_aggregation.py` (pure numpy/scipy) gives the aggregation;
+* `cons/mgpbd_gpu.py` (`MGPBDSolverGPU`) gives the sparsity pattern
+  (`_build_sparsity_pattern`), the per-tet precompute, constraint
+  gradients, matrix fill, the GPU multigrid setup (`cons/mgpcg_gpu.py`) and
+  whole substeps.
+
+One intervention, applied only to the `step` fixtures and to the coarse
+structure: scipy's `astype` canonicalises (sorts) CSR indices whenever the
+dtype changes.  `GPUMultigridSolver.setup` (`cons/mgpcg_gpu.py:43,104`) calls
+`astype`, so the level-0 matrix is uploaded with sorted columns while
+`_fill_A_kernel` (`cons/mgpbd_gpu.py:273-324`) keeps writing values in the
+diagonal-last order of `_build_sparsity_pattern` (`:153-194`): the fine matrix
+is scrambled from the first Newton iteration on.  The fixtures record the
+intended semantics (values and columns in the same diagonal-last order) by
+making `astype` keep the index order; `asshipped_*` keys record the
+unpatched behaviour as evidence.
+"""
+
+from __future__ import annotations
+
+import argparse
+import hashlib
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, HERE)
+sys.path.insert(0, ROOT)
+
+from controllable_pbd_3d_gb300 import meshgen  # noqa: E402
+
+
+def sha(*arrays):
+  h = hashlib.sha256()
+  for a in arrays:
+    h.update(np.ascontiguousarray(np.asarray(a, dtype=np.int64)).tobytes())
+  return h.hexdigest()
+
+
+# ----------------------------------------------------------------------------
+# loading the reference under the shim
+# ----------------------------------------------------------------------------
+
+_ORIG_ASTYPE = None
+
+
+def load_reference(ref):
+  import taichi_cpu_shim
+  taichi_cpu_shim.install()
+  sys.path.insert(0, ref)
+  import cons.mgpbd_gpu as mg  # noqa: F401
+  import cons.tet_aggregation as ta  # noqa: F401
+  return sys.modules['cons.mgpbd_gpu'], sys.modules['cons.tet_aggregation']
+
+
+def set_astype_keeps_order(on: bool):
+  """Toggle scipy's canonicalise-on-astype (see module docstring)."""
+  import scipy.sparse._data as d
+  global _ORIG_ASTYPE
+  if _ORIG_ASTYPE is None:
+    _ORIG_ASTYPE = d._data_matrix.astype
+
+  def astype_keep_order(self, dtype, casting='unsafe', copy=True):
+    dtype = np.dtype(dtype)
+    if self.dtype != dtype:
+      return self._with_data(self.data.astype(dtype, casting=casting, copy=True), copy=True)
+    return self.copy() if copy else self
+
+  d._data_matrix.astype = astype_keep_order if on else _ORIG_ASTYPE
+
+
+# ----------------------------------------------------------------------------
+# cases
+# ----------------------------------------------------------------------------
+
+
+def grid_case(nx, ny, nz, jitter, seed, ball=False):
+  """Rest shape = regular grid (optionally ball-projected); start = jittered."""
+  xr, t = meshgen.hex_grid_tets(nx, ny, nz)
+  x0, _ = meshgen.hex_grid_tets(nx, ny, nz, jitter=jitter, seed=seed)
+  if ball:
+    xr = meshgen.ball_project(xr)
+    x0 = meshgen.ball_project(x0)
+  invm = np.ones(len(xr), np.float32)
+  invm[meshgen.grid_face_vertices(nx, ny, nz, axis=1, side='max')] = 0.0
+  return xr, x0, t, invm
+
+
+def asset_case(ref, rel, fixed):
+  v, t, _ = meshgen.parse_medit_mesh(os.path.join(ref, 'assets', rel))
+  invm = meshgen.lumped_inverse_mass(v, t)
+  invm[np.asarray(fixed, np.int64)] = 0.0
+  return v, v.copy(), t, invm
+
+
+STRUCTURE_CASES = {
+    # name: (builder, full_coarse) ; full_coarse -> also coarse pattern + map
+    'box5x4x5': (lambda ref: grid_case(5, 4, 5, 0.01, 1), True),
+    'cube6': (lambda ref: grid_case(6, 6, 6, 0.01, 0), True),
+    'box12x3x7': (lambda ref: grid_case(12, 3, 7, 0.01, 3), True),
+    'ball8': (lambda ref: grid_case(8, 8, 8, 0.01, 2, ball=True), False),
+    'cube10': (lambda ref: grid_case(10, 10, 10, 0.01, 0), False),
+    'cube20': (lambda ref: grid_case(20, 20, 20, 0.01, 0), False),
+    'simple_sphere': (lambda ref: asset_case(ref, 'simple_sphere/simple_sphere.mesh', [0, 11]), False),
+    'spot': (lambda ref: asset_case(ref, 'spot/spot.mesh', [0]), False),
+    'cube_tet': (lambda ref: asset_case(ref, 'cube_tet/cube_tet.mesh', [0]), False),
+}
+
+
+class _Rec:
+  """SolverBenchmark-shaped recorder (`utils/bench.py:24-55`)."""
+
+  def __init__(self):
+    self.frames = []
+
+  def begin_frame(self, f):
+    self.frames.append([])
+
+  def record_iteration(self, ite, r, cg_iters=0, omega=1.0):
+    self.frames[-1].append((ite, float(r), int(cg_iters), float(omega)))
+
+  def end_frame(self):
+    pass
+
+
+def make_solver(mg, ti, xr, x0, t, invm, **kw):
+  n = len(xr)
+  v_p = ti.Vector.field(3, dtype=ti.f32, shape=n)
+  v_p.from_numpy(x0)
+  v_p_ref = ti.Vector.field(3, dtype=ti.f32, shape=n)
+  v_p_ref.from_numpy(xr)
+  v_invm = ti.field(ti.f32, n)
+  v_invm.from_numpy(invm)
+  t_i = ti.field(ti.i32, len(t))
+  t_i.from_numpy(t)
+  t_m = ti.field(ti.f32, len(t) // 4)
+  g = kw.pop('gravity', (0.0, -9.8, 0.0))
+  dt = kw.pop('dt', 1.0 / 300.0)
+  s = mg.MGPBDSolverGPU(v_p, v_p_ref, v_invm, t_i, t_m, ti.Vector(list(g)), dt, **kw)
+  return s
+
+
+def csr_of(m):
+  return m.indptr.to_numpy(), m.indices.to_numpy(), m.data.to_numpy()
+
+
+def structure_fixtures(ref, mg, ta, out):
+  import taichi as ti
+  res = {}
+  for name, (build, full) in STRUCTURE_CASES.items():
+    t0 = time.time()
+    xr, x0, t, invm = build(ref)
+    nt = len(t) // 4
+    res[f'{name}/t_i_sha'] = np.array(sha(t))
+    res[f'{name}/x_ref'] = xr
+    res[f'{name}/t_i'] = t
+    # level-0 pattern through the reference method
+    s = make_solver(mg, ti, xr, x0, t, invm, mu=1e5)
+    s._build_sparsity_pattern()
+    res[f'{name}/nnz'] = np.array(s._nnz)
+    res[f'{name}/pattern_sha'] = np.array(sha(s._A_indptr, s._A_indices))
+    if nt <= 2000:
+      res[f'{name}/indptr'] = s._A_indptr
+      res[f'{name}/indices'] = s._A_indices
+    # hierarchy through the reference module
+    Ps, sizes = ta.build_tet_hierarchy(t.copy(), xr.copy(), nt)
+    res[f'{name}/sizes'] = np.array(sizes, np.int64)
+    if Ps:
+      res[f'{name}/agg_ids'] = Ps[0].indices.astype(np.int32)
+      adj = ta.build_tet_face_adjacency(t, nt)
+      res[f'{name}/adj_deg'] = np.array([len(adj[i]) for i in range(nt)], np.int32)
+    if full and Ps:
+      set_astype_keeps_order(True)
+      s2 = make_solver(mg, ti, xr, x0, t, invm, mu=1e5)
+      s2.init()
+      gs = s2._gpu_solver
+      res[f'{name}/A0_data'] = s2._A_data.copy()
+      ip, ix, _ = csr_of(gs._gpu_As[1])
+      res[f'{name}/coarse_indptr'] = ip
+      res[f'{name}/coarse_indices'] = ix
+      res[f'{name}/contrib_fine_idx'] = gs._contrib_maps[0]['fine_idx']
+      res[f'{name}/contrib_offsets'] = gs._contrib_offsets[0]
+      set_astype_keeps_order(False)
+    print(f'[structure] {name}: nt={nt} sizes={sizes} ({time.time() - t0:.1f}s)', flush=True)
+  np.savez_compressed(os.path.join(out, 'structure.npz'), **res)
+
+
+STEP_CASES = {
+    # name: (builder, solver kwargs, substeps)
+    'box5x4x5_mu1e5': (lambda ref: grid_case(5, 4, 5, 0.01, 1),
+                       dict(mu=1e5, damp=0.993), 3),
+    'box5x4x5_ls': (lambda ref: grid_case(5, 4, 5, 0.3, 7),
+                    dict(mu=1e5, damp=0.993, maxiter=4), 1),
+    'cube6_mu3e4': (lambda ref: grid_case(6, 6, 6, 0.02, 5),
+                    dict(mu=3e4, damp=0.993, maxiter=3), 1),
+}
+
+
+def step_fixture(ref, mg, name, build, kw, substeps, out):
+  import taichi as ti
+  t0 = time.time()
+  xr, x0, t, invm = build(ref)
+  res = {'x_ref': xr, 'x0': x0, 't_i': t, 'invm': invm,
+         'gravity': np.array([0.0, -9.8, 0.0], np.float32), 'dt': np.array(1.0 / 300.0)}
+  for k, v in kw.items():
+    res['param_' + k] = np.array(v)
+
+  # as-shipped evidence: level-0 columns after setup vs. the fill order
+  set_astype_keeps_order(False)
+  s_bad = make_solver(mg, ti, xr, x0, t, invm, **kw)
+  s_bad.init()
+  res['asshipped_level0_indices_match'] = np.array(
+      np.array_equal(s_bad._gpu_solver._gpu_As[0].indices.to_numpy(), s_bad._A_indices))
+
+  set_astype_keeps_order(True)
+  rec = _Rec()
+  s = make_solver(mg, ti, xr, x0, t, invm, benchmark=rec, **kw)
+  s.init()
+  gs = s._gpu_solver
+  res['Dm_inv'] = s.Dm_inv.to_numpy()
+  res['rest_vol'] = s.rest_vol.to_numpy()
+  res['alpha_tilde'] = s.alpha_tilde.to_numpy()
+  res['A0_data'] = s._A_data.copy()
+  res['indptr'] = s._A_indptr
+  res['indices'] = s._A_indices
+  res['agg_ids'] = s._amg_Ps[0].indices.astype(np.int32) if s._amg_Ps else np.zeros(0, np.int32)
+  ip, ix, dd = csr_of(gs._gpu_As[1])
+  res['coarse_indptr'], res['coarse_indices'], res['coarse_data0'] = ip, ix, dd
+  res['contrib_fine_idx'] = gs._contrib_maps[0]['fine_idx']
+  res['contrib_offsets'] = gs._contrib_offsets[0]
+
+  # --- first Newton iteration of substep 0, captured around reference calls
+  snap = {}
+  orig_cg = gs.solve
+  orig_ls = s._line_search
+  orig_fill = s._fill_A_and_update_gpu
+
+  def fill():
+    orig_fill()
+    if 'A_data' not in snap:
+      snap['constraints'] = s.constraints.to_numpy()
+      snap['gradC'] = s.gradC.to_numpy()
+      snap['lambda_pre'] = s.lambdaf.to_numpy()
+      snap['x_pred'] = s.v_p.to_numpy()
+      snap['A_data'] = gs._gpu_As[0].data.to_numpy()
+      snap['diag_inv0'] = gs._gpu_As[0].diag_inv.to_numpy()
+      snap['coarse_data'] = gs._gpu_As[1].data.to_numpy()
+      snap['diag_inv1'] = gs._gpu_As[1].diag_inv.to_numpy()
+
+  def cg(b, x):
+    first = 'b' not in snap
+    if first:
+      snap['b'] = b.to_numpy()
+      # one V-cycle on r = b from zero, through the reference's vcycle
+      n = gs._level_sizes[0]
+      gs._b[0].from_numpy(b.to_numpy())
+      gs._x[0].fill(0.0)
+      gs.vcycle(0)
+      snap['vcycle_z'] = gs._x[0].to_numpy()
+      # level SpMV / Jacobi with a seeded vector
+      rng = np.random.default_rng(11)
+      for lvl, A in enumerate(gs._gpu_As):
+        xv = ti.field(ti.f32, A.n_rows)
+        xv.from_numpy(rng.standard_normal(A.n_rows).astype(np.float32))
+        yv = ti.field(ti.f32, A.n_rows)
+        A.spmv(xv, yv)
+        snap[f'spmv_x{lvl}'] = xv.to_numpy()
+        snap[f'spmv_y{lvl}'] = yv.to_numpy()
+        bv = ti.field(ti.f32, A.n_rows)
+        bv.from_numpy(rng.standard_normal(A.n_rows).astype(np.float32))
+        A.jacobi_smooth(bv, xv, yv, gs.omega_jacobi)
+        snap[f'jac_b{lvl}'] = bv.to_numpy()
+        snap[f'jac_y{lvl}'] = yv.to_numpy()
+      del n
+    it = orig_cg(b, x)
+    if first:
+      snap['dlam'] = x.to_numpy()
+      snap['cg_iters'] = np.array(it)
+    return it
+
+  def ls():
+    om = orig_ls()
+    if 'omega' not in snap:
+      snap['dpos'] = s.dpos.to_numpy()
+      snap['lambda_post'] = s.lambdaf.to_numpy()
+      snap['omega'] = np.array(om)
+    return om
+
+  gs.solve = cg
+  s._line_search = ls
+  s._fill_A_and_update_gpu = fill
+  traj = []
+  for k in range(substeps):
+    s.step(k)
+    traj.append(s.v_p.to_numpy())
+    if k == 0:
+      snap['x_after_substep0'] = s.v_p.to_numpy()
+  for k, v in snap.items():
+    res['it0_' + k] = v
+  res['x_traj'] = np.stack(traj)
+  res['v_final'] = s.v_v.to_numpy()
+  res['lambda_final'] = s.lambdaf.to_numpy()
+  recs = [(f, *r) for f, fr in enumerate(rec.frames) for r in fr]
+  res['newton_log'] = np.array(recs, np.float64).reshape(-1, 5)
+  set_astype_keeps_order(False)
+  np.savez_compressed(os.path.join(out, f'step_{name}.npz'), **res)
+  print(f'[step] {name}: {len(recs)} newton iterations ({time.time() - t0:.1f}s)', flush=True)
+
+
+def main():
+  ap = argparse.ArgumentParser()
+  ap.add_argument('--ref', default='/root/reference')
+  ap.add_argument('--only', default=None)
+  ap.add_argument('--out', default=HERE)
+  a = ap.parse_args()
+  mg, ta = load_reference(a.ref)
+  if a.only in (None, 'structure'):
+    structure_fixtures(a.ref, mg, ta, a.out)
+  if a.only in (None, 'step'):
+    for name, (build, kw, n) in STEP_CASES.items():
+      step_fixture(a.ref, mg, name, build, kw, n, a.out)
+
+
+if __name__ == '__main__':
+  main()
