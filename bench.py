@@ -1,0 +1,342 @@
+#!/usr/bin/env python3
+"""MGPBD substeps/sec on GB300 (one JSON line on stdout).
+
+Workload (one "step" = one MGPBD substep = prediction + Newton/PCG solve +
+velocity update): a 40x40x40 hex cube, 5 tets per hex (68,921 vertices,
+320,000 tets, 25.9M level-0 nonzeros), rest shape the regular grid, start
+positions jittered U(+-0.01 h) from seed 0, unit vertex mass, top face
+pinned (kinematic), gravity -9.8, dt = 1/60 / 5 substeps, compliance drawn
+log-uniform in [1e-9, 1e-4] from the seed (alpha~ = compliance / dt^2), PCG
+to relative residual 1e-6.  Synthetic data: the reference's experiment
+meshes are not available.  The level-0 matrix (207 MB) exceeds the 129 MB
+L2, so no L2 flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = 'MGPBD substeps/sec @ rel-res 1e-6: learned+mixed+batched vs plain FP32 AMG-PCG'
+UNIT = 'substeps/s'
+
+
+def peaks():
+  p = os.path.join(HERE, 'MEASURED_PEAKS.json')
+  if os.path.exists(p):
+    d = json.load(open(p))
+    return float(d['hbm_gbs']), 'measured'
+  return 6800.0, 'fallback'
+
+
+def workload(n, seed=0):
+  from controllable_pbd_3d_gb300 import meshgen
+  xr, t = meshgen.hex_grid_tets(n, n, n)
+  x0, _ = meshgen.hex_grid_tets(n, n, n, jitter=0.01, seed=seed)
+  invm = np.ones(len(xr), np.float32)
+  invm[meshgen.grid_face_vertices(n, n, n, axis=1, side='max')] = 0.0
+  rng = np.random.default_rng(seed)
+  compliance = float(10.0 ** rng.uniform(-9.0, -4.0))
+  return xr, x0, t, invm, compliance
+
+
+SOLVER_KW = dict(damp=1.0, maxiter=20, atol=1e-4, rtol=1e-2, maxiter_cg=200, tol_cg=1e-12,
+                 rel_tol_cg=1e-6, n_smooth=2, kinematic_pins=True)
+FAST_KW = dict(mode='fast', smoother='safe', coarse_solver='jacobi')
+DT = 1.0 / 60.0 / 5.0
+
+
+class ClockSampler:
+  """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+
+  def __init__(self, index=0):
+    self.index = index
+    self.proc = None
+    self.lines = []
+
+  def __enter__(self):
+    try:
+      self.proc = subprocess.Popen(
+          ['nvidia-smi', f'--id={self.index}',
+           '--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,'
+           'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+           'clocks_event_reasons.sw_power_cap', '--format=csv,noheader,nounits', '-lms', '100'],
+          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+      self.t = threading.Thread(target=self._read, daemon=True)
+      self.t.start()
+    except (OSError, FileNotFoundError):
+      self.proc = None
+    return self
+
+  def _read(self):
+    for ln in self.proc.stdout:
+      self.lines.append(ln.strip())
+
+  def __exit__(self, *a):
+    if self.proc is not None:
+      self.proc.terminate()
+      try:
+        self.proc.wait(timeout=5)
+      except subprocess.TimeoutExpired:
+        self.proc.kill()
+
+  def summary(self):
+    sm, mx, reasons = [], [], set()
+    names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+    for ln in self.lines:
+      f = [x.strip() for x in ln.split(',')]
+      if len(f) < 6:
+        continue
+      try:
+        sm.append(float(f[0]))
+        mx.append(float(f[1]))
+      except ValueError:
+        continue
+      for name, v in zip(names, f[2:6]):
+        if v.lower().startswith('active'):
+          reasons.add(name)
+    if not sm:
+      return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': [], 'samples': 0}
+    return {'sm_mhz': statistics.median(sm), 'sm_max_mhz': max(mx), 'reasons': sorted(reasons),
+            'samples': len(sm)}
+
+
+def dist_init(args):
+  ws = int(os.environ.get('WORLD_SIZE', '1'))
+  rank = int(os.environ.get('RANK', '0'))
+  local = int(os.environ.get('LOCAL_RANK', '0'))
+  import torch
+  if ws > 1:
+    import torch.distributed as dist
+    dist.init_process_group('nccl' if torch.cuda.is_available() else 'gloo')
+  return ws, rank, local
+
+
+def barrier(ws):
+  if ws > 1:
+    import torch.distributed as dist
+    dist.barrier()
+
+
+def max_over_ranks(ws, v):
+  if ws == 1:
+    return v
+  import torch
+  import torch.distributed as dist
+  t = torch.tensor([v], dtype=torch.float64, device='cuda')
+  dist.all_reduce(t, op=dist.ReduceOp.MAX)
+  return float(t.item())
+
+
+def make_solver(torch, n, kw):
+  from controllable_pbd_3d_gb300.mgpbd_gpu import MGPBDSolverGPU
+  xr, x0, t, invm, compliance = workload(n)
+  x = torch.tensor(x0, device='cuda')
+  s = MGPBDSolverGPU(x, torch.tensor(xr, device='cuda'), torch.tensor(invm, device='cuda'),
+                     torch.tensor(t, device='cuda'), None, [0.0, -9.8, 0.0], DT,
+                     compliance=compliance, **kw)
+  s.init()
+  return s, x, compliance
+
+
+def time_steps(torch, s, k, first):
+  stream = torch.cuda.current_stream()
+  st = []
+  e0 = torch.cuda.Event(enable_timing=True)
+  e1 = torch.cuda.Event(enable_timing=True)
+  torch.cuda.synchronize()
+  e0.record(stream)
+  for i in range(k):
+    s.step(first + i)
+    st.append(s.stats())
+  e1.record(stream)
+  torch.cuda.synchronize()
+  return e0.elapsed_time(e1) / 1e3, st
+
+
+def kernel_roofline(torch, s, hbm_peak, peak_kind, reps=40):
+  """Level-0 weighted Jacobi sweep (the dominant launch: 4 per CG
+  iteration) timed with CUDA events on the current stream."""
+  from controllable_pbd_3d_gb300 import _native as N
+  A = s._gpu_solver._gpu_As[0]
+  n, nnz = A.n_rows, A.nnz
+  b = torch.randn(n, device='cuda')
+  x = torch.randn(n, device='cuda')
+  y = torch.empty_like(x)
+  L = N.lib()
+  stream = torch.cuda.current_stream()
+
+  def launch():
+    N.check(L.mgpbd_csr_jacobi(n, A.indptr.data_ptr(), A.indices.data_ptr(), A.data.data_ptr(),
+                               A.diag_inv.data_ptr(), b.data_ptr(), x.data_ptr(), y.data_ptr(),
+                               0.5, C.c_void_p(stream.cuda_stream)), 'mgpbd_csr_jacobi')
+  for _ in range(5):
+    launch()
+  e0 = torch.cuda.Event(enable_timing=True)
+  e1 = torch.cuda.Event(enable_timing=True)
+  torch.cuda.synchronize()
+  e0.record(stream)
+  for _ in range(reps):
+    launch()
+  e1.record(stream)
+  torch.cuda.synchronize()
+  dt = e0.elapsed_time(e1) / 1e3 / reps
+  # algorithmic bytes: values + column ids + row pointers + x gathered once,
+  # b, 1/diag read, x_new written
+  bytes_ = 8 * nnz + 4 * (n + 1) + 4 * n * 4
+  achieved = bytes_ / dt / 1e9
+  return {'kernel': 'k_csr_rows<32,kJacobi> (level-0 weighted Jacobi sweep)', 'bound': 'hbm',
+          'achieved': round(achieved, 1), 'peak': hbm_peak, 'unit': 'GB/s',
+          'frac': round(achieved / hbm_peak, 4), 'peak_kind': peak_kind,
+          'algorithmic_bytes_per_launch': bytes_, 'launch_us': round(dt * 1e6, 2),
+          'traffic': None}
+
+
+def cpu_baseline_sample(n, budget_s=30.0):
+  """The oracle (float32 numpy restatement of the reference step) on the
+  same workload: setup excluded, one Newton iteration timed; returns the
+  measured Newton iteration time."""
+  from oracle.mgpbd_oracle import MGPBDOracle
+  xr, x0, t, invm, compliance = workload(n)
+  o = MGPBDOracle(x0, xr, invm, t, [0.0, -9.8, 0.0], DT, dtype=np.float32, compliance=compliance,
+                  smoother='safe', maxiter=1, atol=1e-4, rtol=1e-2, maxiter_cg=200, tol_cg=1e-12,
+                  rel_tol_cg=1e-6, kinematic_pins=True)
+  o.init()
+  t0 = time.perf_counter()
+  o.step(0)
+  dt = time.perf_counter() - t0
+  return dt, o.log
+
+
+def run_ours(args):
+  import torch
+  ws, rank, local = dist_init(args)
+  torch.cuda.set_device(local)
+  from controllable_pbd_3d_gb300 import _native as N
+  hbm, kind = peaks()
+  kw = dict(SOLVER_KW)
+  kw.update(FAST_KW)
+  s, x, compliance = make_solver(torch, args.size, kw)
+  for i in range(args.warmup):
+    s.step(i)
+  torch.cuda.synchronize()
+  barrier(ws)
+  L = N.lib()
+  c0 = L.mgpbd_launch_count()
+  with ClockSampler(local) as clk:
+    t, st = time_steps(torch, s, args.steps, args.warmup)
+  launches = L.mgpbd_launch_count() - c0
+  barrier(ws)
+  t_max = max_over_ranks(ws, t)
+  newton = sum(x['newton_iters'] for x in st)
+  cg = sum(x['cg_iters_total'] for x in st)
+  value = ws * args.steps / t_max
+
+  # end to end through the public API with host buffers
+  xh = torch.empty_like(x, device='cpu').pin_memory()
+  xh.copy_(x)
+  vh = torch.empty_like(x, device='cpu').pin_memory()
+  vh.copy_(s.v_v)
+  torch.cuda.synchronize()
+  barrier(ws)
+  t0 = time.perf_counter()
+  for i in range(args.steps):
+    x.copy_(xh, non_blocking=True)
+    s.v_v.copy_(vh, non_blocking=True)
+    s.step(args.warmup + args.steps + i)
+    xh.copy_(x, non_blocking=True)
+    vh.copy_(s.v_v, non_blocking=True)
+    torch.cuda.synchronize()
+  t_e2e = max_over_ranks(ws, time.perf_counter() - t0)
+  e2e = {'value': round(ws * args.steps / t_e2e, 3), 'unit': UNIT,
+         'h2d_bytes_per_step': 2 * x.numel() * 4, 'd2h_bytes_per_step': 2 * x.numel() * 4}
+
+  roof = kernel_roofline(torch, s, hbm, kind)
+  st0 = st[-1]
+  out = {
+      'metric': METRIC, 'value': round(value, 3), 'unit': UNIT, 'n_gpus': ws,
+      'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(t_max * 1e3 / args.steps, 3),
+      'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+      'data': 'synthetic (seeded hex-grid cube; reference meshes unavailable)',
+      'config': {'workload': f'{args.size}^3 hex cube, 5 tets/hex', 'n_verts': s.n_verts,
+                 'n_tets': s.n_tets, 'nnz_level0': st0['nnz'][0], 'levels': st0['rows'],
+                 'compliance': compliance, 'dt': DT, 'rel_res_cg': 1e-6, 'mode': 'fast',
+                 'l2': 'level-0 matrix 207 MB > L2, no flush', 'parallelism': f'replicas{ws}'},
+      'newton_iters_per_step': newton / args.steps, 'cg_iters_per_step': cg / args.steps,
+      'cg_iters_per_s': round(ws * cg / t_max, 1), 'gpu_launches': int(launches),
+      'clocks': clk.summary(), 'e2e': e2e, 'roofline': roof,
+  }
+  if rank == 0 and not args.no_cpu_baseline:
+    t_it, log = cpu_baseline_sample(args.size)
+    per_sub = max(newton / args.steps, 1e-9)
+    out['cpu_baseline'] = {
+        'value': round(1.0 / (t_it * per_sub), 5), 'unit': UNIT, 'cores': 1, 'kind': 'port',
+        'sample': f'one Newton iteration of substep 0 on the same workload '
+                  f'({t_it:.1f} s, {log[0][2] if log else 0} CG iterations), scaled by the '
+                  f'{per_sub:.2f} Newton iterations per substep of the GPU run; numpy/scipy '
+                  'float32 restatement, setup excluded'}
+  if rank == 0:
+    print(json.dumps(out), flush=True)
+  if ws > 1:
+    import torch.distributed as dist
+    dist.destroy_process_group()
+
+
+def run_reference(args):
+  ws = int(os.environ.get('WORLD_SIZE', '1'))
+  rank = int(os.environ.get('RANK', '0'))
+  if rank != 0:
+    return
+  times = []
+  n_newton = None
+  for i in range(args.warmup + args.steps):
+    t_it, log = cpu_baseline_sample(args.size)
+    if i >= args.warmup:
+      times.append(t_it)
+  t_it = float(np.mean(times))
+  # per-substep Newton count of this workload, from the oracle run to
+  # convergence on a 10^3 body of the same construction
+  n_newton = 1.0
+  value = 1.0 / (t_it * n_newton)
+  out = {'metric': METRIC, 'value': round(value, 5), 'unit': UNIT, 'n_gpus': ws, 'steps': args.steps,
+         'warmup': args.warmup, 'ms_per_step': round(t_it * 1e3, 1), 'higher_is_better': True,
+         'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic', 'impl': 'reference',
+         'config': {'workload': f'{args.size}^3 hex cube, 5 tets/hex'},
+         'cpu_baseline': {'value': round(value, 5), 'unit': UNIT, 'cores': 1, 'kind': 'port',
+                          'sample': 'one Newton iteration per step (numpy float32 oracle)'},
+         'e2e': {'value': round(value, 5), 'unit': UNIT, 'h2d_bytes_per_step': 0,
+                 'd2h_bytes_per_step': 0}}
+  print(json.dumps(out), flush=True)
+
+
+def main():
+  ap = argparse.ArgumentParser()
+  ap.add_argument('--gpus', type=int, default=1)
+  ap.add_argument('--steps', type=int, default=10)
+  ap.add_argument('--warmup', type=int, default=3)
+  ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+  ap.add_argument('--size', type=int, default=40)
+  ap.add_argument('--no-cpu-baseline', action='store_true')
+  args = ap.parse_args()
+  if args.impl == 'reference':
+    run_reference(args)
+  else:
+    run_ours(args)
+
+
+if __name__ == '__main__':
+  main()

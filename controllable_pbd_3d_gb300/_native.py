@@ -48,7 +48,8 @@ class Params(C.Structure):
       ('atol', f32), ('rtol', f32), ('maxiter_cg', i32), ('tol_cg', f32), ('n_smooth', i32),
       ('omega_jacobi', f32), ('setup_interval', i32), ('use_line_search', i32), ('mode', i32),
       ('rel_tol_cg', f32), ('coarse_solver', i32), ('smoother', i32), ('max_levels', i32),
-      ('max_coarse', i32), ('kinematic_pins', i32), ('coarse_sweeps', i32),
+      ('max_coarse', i32), ('kinematic_pins', i32), ('coarse_sweeps', i32), ('cg_alias', i32),
+      ('compliance', f32),
   ]
 
 
@@ -74,6 +75,7 @@ _SIGS = {
     'mgpbd_strerror': (C.c_char_p, [C.c_int]),
     'mgpbd_last_error': (C.c_char_p, []),
     'mgpbd_version': (C.c_char_p, []),
+    'mgpbd_launch_count': (C.c_int64, []),
     'mgpbd_create': (C.c_int, [C.POINTER(Params), C.POINTER(vp)]),
     'mgpbd_destroy': (None, [vp]),
     'mgpbd_set_stream': (C.c_int, [vp, vp]),
@@ -86,6 +88,7 @@ _SIGS = {
     'mgpbd_get_stats': (C.c_int, [vp, C.POINTER(Stats)]),
     'mgpbd_synchronize': (C.c_int, [vp]),
     'mgpbd_get_status': (C.c_int, [vp, P_u32]),
+    'mgpbd_newton_log': (C.c_int, [vp, i32, vp, P_i32]),
     'mgpbd_field': (C.c_int, [vp, i32, C.POINTER(vp), P_i64]),
     'mgpbd_level_csr': (C.c_int, [vp, i32, P_i32, P_i64, C.POINTER(vp), C.POINTER(vp),
                                   C.POINTER(vp), C.POINTER(vp)]),
@@ -105,6 +108,8 @@ _SIGS = {
     'mgpbd_dot': (C.c_int, [i32, vp, vp, P_f64, vp]),
     'mgpbd_axpy': (C.c_int, [i32, f32, vp, vp, vp]),
     'mgpbd_xpay': (C.c_int, [i32, f32, vp, vp, vp]),
+    'mgpbd_scale': (C.c_int, [i32, f32, vp, vp]),
+    'mgpbd_refill_coarse': (C.c_int, [vp]),
     'mgpbd_host_pattern': (C.c_int, [vp, i32, P_i64, vp, vp]),
     'mgpbd_host_aggregate': (C.c_int, [vp, i32, i32, vp, P_i32]),
     'mgpbd_host_tet_hierarchy': (C.c_int, [vp, i32, i32, i32, P_i32, vp, vp]),

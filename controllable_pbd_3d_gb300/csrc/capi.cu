@@ -4,6 +4,7 @@
 // mgpbd_last_error().
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <new>
 #include <string>
@@ -75,6 +76,8 @@ void mgpbd_default_params(mgpbd_params* p) {
   p->max_coarse = 400;
   p->kinematic_pins = 0;
   p->coarse_sweeps = 0;
+  p->cg_alias = 0;
+  p->compliance = 0.0f;
 }
 
 const char* mgpbd_strerror(int code) {
@@ -94,6 +97,8 @@ const char* mgpbd_strerror(int code) {
 const char* mgpbd_last_error(void) { return g_last_error.c_str(); }
 
 const char* mgpbd_version(void) { return "mgpbd-gb300 0.1 (sm_103a)"; }
+
+int64_t mgpbd_launch_count(void) { return mgpbd::g_launches.load(); }
 
 int mgpbd_create(const mgpbd_params* params, mgpbd_handle* out) {
   if (!params || !out) return MGPBD_EINVAL;
@@ -150,6 +155,16 @@ int mgpbd_get_stats(mgpbd_handle h, mgpbd_stats* out) {
   return MGPBD_OK;
 }
 
+int mgpbd_newton_log(mgpbd_handle h, int32_t max_rows, double* rows, int32_t* n_rows) {
+  if (!h || !n_rows || max_rows < 0 || (max_rows > 0 && !rows)) return MGPBD_EINVAL;
+  const auto& log = h->impl.newton_log();
+  *n_rows = static_cast<int32_t>(log.size());
+  int32_t m = std::min<int32_t>(max_rows, *n_rows);
+  for (int32_t i = 0; i < m; ++i)
+    for (int k = 0; k < 5; ++k) rows[5 * i + k] = log[i][k];
+  return MGPBD_OK;
+}
+
 int mgpbd_get_status(mgpbd_handle h, uint32_t* status) {
   if (!h || !status) return MGPBD_EINVAL;
   *status = h->impl.status();
@@ -197,6 +212,11 @@ int mgpbd_compute_constraints(mgpbd_handle h) {
 int mgpbd_fill_matrices(mgpbd_handle h) {
   if (!h) return MGPBD_EINVAL;
   return guarded([&] { h->impl.fill_matrices(); });
+}
+
+int mgpbd_refill_coarse(mgpbd_handle h) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.refill_coarse(); });
 }
 
 int mgpbd_compute_rhs(mgpbd_handle h, double* residual_norm) {
@@ -312,6 +332,11 @@ int mgpbd_axpy(int32_t n, float alpha, const float* x, float* y, void* stream) {
 int mgpbd_xpay(int32_t n, float alpha, const float* x, float* y, void* stream) {
   if (n < 0 || (n > 0 && (!x || !y))) return MGPBD_EINVAL;
   return guarded([&] { mgpbd::launch_xpay(alpha, x, y, n, as_stream(stream)); });
+}
+
+int mgpbd_scale(int32_t n, float alpha, float* x, void* stream) {
+  if (n < 0 || (n > 0 && !x)) return MGPBD_EINVAL;
+  return guarded([&] { mgpbd::launch_scale(alpha, x, n, as_stream(stream)); });
 }
 
 // ---- host structure builders ----------------------------------------------

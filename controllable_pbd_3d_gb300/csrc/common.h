@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -25,7 +26,15 @@ struct Error : std::runtime_error {
                                             cudaGetErrorString(err_));             \
   } while (0)
 
-#define MGPBD_CHECK_LAUNCH() MGPBD_CUDA(cudaGetLastError())
+// Every kernel launch of the library goes through this macro, which also
+// counts it (mgpbd_launch_count).  Launches recorded into a CUDA graph are
+// counted when the graph runs (see Solver::pcg_graph).
+extern std::atomic<long long> g_launches;
+#define MGPBD_CHECK_LAUNCH()                                  \
+  do {                                                        \
+    ::mgpbd::g_launches.fetch_add(1, std::memory_order_relaxed); \
+    MGPBD_CUDA(cudaGetLastError());                           \
+  } while (0)
 
 inline void require(bool ok, int code, const char* msg) {
   if (!ok) throw Error(code, msg);

@@ -20,10 +20,11 @@
 
 namespace mgpbd {
 
+std::atomic<long long> g_launches{0};
+
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kSMs = 152;
 
 inline int grid_for(int64_t work_items, int per_block) {
   int64_t g = (work_items + per_block - 1) / per_block;
@@ -90,7 +91,8 @@ __global__ void k_rest_shape(const float* __restrict__ x_ref, const int4* __rest
     o[8] = (D[0][0] * D[1][1] - D[0][1] * D[1][0]) * inv;
     float vol = fabsf(det) / 6.0f;
     rest_vol[t] = vol;
-    alpha[t] = 1.0f / (mu * dt * dt * vol);
+    // mu < 0 carries a compliance: alpha~ = compliance / dt^2
+    alpha[t] = mu < 0.0f ? (-mu) / (dt * dt) : 1.0f / (mu * dt * dt * vol);
   }
 }
 
@@ -489,6 +491,12 @@ __global__ void k_axpy(float alpha, const float* __restrict__ x, float* __restri
     y[i] += alpha * x[i];
 }
 
+__global__ void k_scale(float alpha, float* __restrict__ x, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[i] *= alpha;
+}
+
 __global__ void k_xpay(float alpha, const float* __restrict__ x, float* __restrict__ y, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -525,6 +533,7 @@ __global__ void k_cg_init(CgState* st, const double* __restrict__ p, int blocks,
     st->done = maxiter <= 0;
     st->status = isfinite(rz) ? 0 : MGPBD_STATUS_NAN;
     st->maxiter = maxiter;
+    st->body_runs = 0;
     st->alpha = st->beta = st->pap = st->rr = st->rz_new = 0.0;
   }
 }
@@ -844,6 +853,11 @@ void launch_dot_partials(const float* a, const float* b, int64_t n, double* part
 void launch_axpy(float alpha, const float* x, float* y, int64_t n, cudaStream_t s) {
   if (n <= 0) return;
   k_axpy<<<grid_for(n, kThreads), kThreads, 0, s>>>(alpha, x, y, n);
+  MGPBD_CHECK_LAUNCH();
+}
+void launch_scale(float alpha, float* x, int64_t n, cudaStream_t s) {
+  if (n <= 0) return;
+  k_scale<<<grid_for(n, kThreads), kThreads, 0, s>>>(alpha, x, n);
   MGPBD_CHECK_LAUNCH();
 }
 void launch_xpay(float alpha, const float* x, float* y, int64_t n, cudaStream_t s) {

@@ -87,6 +87,7 @@ void launch_dot_partials(const float* a, const float* b, int64_t n, double* part
                          cudaStream_t s);
 void launch_axpy(float alpha, const float* x, float* y, int64_t n, cudaStream_t s);
 void launch_xpay(float alpha, const float* x, float* y, int64_t n, cudaStream_t s);
+void launch_scale(float alpha, float* x, int64_t n, cudaStream_t s);
 // sums `count` groups of `blocks` partials each into out[g] (float64, fixed order)
 void launch_finalize(const double* partials, int blocks, int count, double* out, cudaStream_t s);
 
@@ -94,6 +95,8 @@ void launch_finalize(const double* partials, int blocks, int count, double* out,
 struct CgState {
   double rz, rz_new, pap, alpha, beta, rr, rr0, tol2;
   int32_t iters, done, status, maxiter;
+  int32_t body_runs;  // executions of the captured loop body
+  int32_t pad;
 };
 // the fused vector kernels read the device state; all return early once done
 void launch_cg_init(CgState* st, const double* partials_rz, int blocks, double tol_abs,

@@ -4,6 +4,7 @@
 #include "solver.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -72,7 +73,8 @@ __global__ void k_pw_weight(const double* __restrict__ nrm2, float omega_cap, fl
   *omega = w;
 }
 
-__global__ void k_set_cond(cudaGraphConditionalHandle h, const CgState* st) {
+__global__ void k_set_cond(cudaGraphConditionalHandle h, CgState* st) {
+  st->body_runs += 1;
   cudaGraphSetConditional(h, st->done ? 0u : 1u);
 }
 
@@ -89,8 +91,8 @@ Solver::Solver(const mgpbd_params& p) : p_(p) {
   require(p.n_smooth >= 0 && p.maxiter >= 0 && p.maxiter_cg >= 0, MGPBD_EINVAL,
           "iteration counts must be non-negative");
   require(p.mode == MGPBD_MODE_PARITY || p.mode == MGPBD_MODE_FAST, MGPBD_EINVAL, "unknown mode");
-  MGPBD_CUDA(cudaMallocHost(&h_buf_, sizeof(double) * 64));
-  MGPBD_CUDA(cudaMallocHost(&h_state_, sizeof(CgState)));
+  // no CUDA call here: a handle can be created (and its host-side
+  // validation exercised) on a machine without a GPU
 }
 
 Solver::~Solver() {
@@ -138,6 +140,8 @@ double Solver::finalize_read(const double* partials, int blocks) {
 void Solver::init() {
   require(x_ && t_i_, MGPBD_ESTATE, "mgpbd_set_mesh has not been called");
   cudaStream_t s = stream_;
+  if (!h_buf_) MGPBD_CUDA(cudaMallocHost(&h_buf_, sizeof(double) * 64));
+  if (!h_state_) MGPBD_CUDA(cudaMallocHost(&h_state_, sizeof(CgState)));
   x_old_.alloc(3LL * nv_);
   x_pred_.alloc(3LL * nv_);
   dpos_.alloc(3LL * nv_);
@@ -158,14 +162,18 @@ void Solver::init() {
   omegas_.alloc(16);
   cg_state_.alloc(1);
 
-  launch_rest_shape(x_ref_, t_i_, nt_, p_.mu, p_.dt, dm_inv_.p, rest_vol_.p, alpha_.p, s);
-
+  // validate every vertex id before any kernel gathers through t_i
   std::vector<int32_t> t_host(4LL * nt_);
   MGPBD_CUDA(cudaMemcpyAsync(t_host.data(), t_i_, sizeof(int32_t) * t_host.size(),
                              cudaMemcpyDeviceToHost, s));
   MGPBD_CUDA(cudaStreamSynchronize(s));
   for (int32_t v : t_host)
     require(v >= 0 && v < nv_, MGPBD_EINVAL, "t_i holds a vertex id outside [0, nv)");
+  require((reinterpret_cast<uintptr_t>(t_i_) & 15) == 0 && (reinterpret_cast<uintptr_t>(x_) & 3) == 0,
+          MGPBD_EINVAL, "t_i must be 16-byte aligned (read as int4)");
+
+  launch_rest_shape(x_ref_, t_i_, nt_, p_.compliance > 0.0f ? -p_.compliance : p_.mu, p_.dt,
+                    dm_inv_.p, rest_vol_.p, alpha_.p, s);
 
   // level-0 pattern (cons/mgpbd_gpu.py:153-194)
   levels_.clear();
@@ -350,6 +358,14 @@ void Solver::fill_matrices() {
   Level& L0 = levels_[0];
   launch_fill_A(L0.indptr.p, L0.indices.p, t_i_, invm_, gradC_.p, alpha_.p, nt_, L0.data.p,
                 L0.diag_inv.p, s);
+  refill_coarse();
+}
+
+// update_all_coarse_matrices (cons/mgpcg_gpu.py:200-212) from the current
+// level-0 values, then the per-level smoother weights and coarse factor.
+void Solver::refill_coarse() {
+  require_init();
+  cudaStream_t s = stream_;
   for (size_t l = 1; l < levels_.size(); ++l) {
     Level& C = levels_[l];
     launch_rap_refill(C.contrib_off.p, C.contrib_idx.p, levels_[l - 1].data.p, C.nnz, C.data.p, s);
@@ -426,14 +442,28 @@ void Solver::vcycle(int32_t l, const float* b, const CgState* guard) {
   } else {
     smooth_level(l, b, cur, nxt, p_.n_smooth, true, guard);
     Level& C = levels_[l + 1];
-    launch_residual_g(guard, L.view(), b, cur, L.r.p, stream_);
-    launch_restrict_g(guard, L.mem_ptr.p, L.mem_rows.p, L.r.p, C.n, C.b.p, stream_);
+    // with cg_alias the level-0 residual lands in the CG residual vector, as
+    // in the reference (cons/mgpcg_gpu.py:239-240 with :275)
+    float* res = (l == 0 && p_.cg_alias) ? cg_r_.p : L.r.p;
+    launch_residual_g(guard, L.view(), b, cur, res, stream_);
+    launch_restrict_g(guard, L.mem_ptr.p, L.mem_rows.p, res, C.n, C.b.p, stream_);
     vcycle(l + 1, C.b.p, guard);
     launch_prolong_add_g(guard, L.agg.p, C.xa.p, L.n, cur, stream_);
     smooth_level(l, b, cur, nxt, p_.n_smooth, false, guard);
   }
   if (cur != L.xa.p)
     MGPBD_CUDA(cudaMemcpyAsync(L.xa.p, cur, sizeof(float) * L.n, cudaMemcpyDeviceToDevice, stream_));
+}
+
+void Solver::precondition(const CgState* guard) {
+  const float* b0 = cg_r_.p;
+  if (p_.cg_alias && n_levels() > 1) {
+    // the reference copies r into _b[0] before vcycle(0) (cons/mgpcg_gpu.py:278,311)
+    MGPBD_CUDA(cudaMemcpyAsync(levels_[0].b.p, cg_r_.p, sizeof(float) * nt_,
+                               cudaMemcpyDeviceToDevice, stream_));
+    b0 = levels_[0].b.p;
+  }
+  vcycle(0, b0, guard);
 }
 
 void Solver::vcycle_into(const float* r, float* z) {
@@ -454,7 +484,7 @@ void Solver::cg_body(const float* b, float* x) {
   launch_cg_alpha(st, partials_.p, blocks, s);
   launch_cg_update_xr(st, cg_p_.p, cg_ap_.p, x, cg_r_.p, n, partials_.p, s);
   launch_cg_check(st, partials_.p, blocks, s);
-  vcycle(0, cg_r_.p, st);
+  precondition(st);
   launch_dot_partials_g(st, cg_r_.p, levels_[0].xa.p, n, partials_.p, s);
   launch_cg_beta(st, partials_.p, blocks, s);
   launch_cg_update_p(st, levels_[0].xa.p, cg_p_.p, n, s);
@@ -469,7 +499,7 @@ int32_t Solver::pcg(const float* b, float* x) {
   int blocks = reduce_blocks(n);
   MGPBD_CUDA(cudaMemsetAsync(x, 0, sizeof(float) * n, s));
   MGPBD_CUDA(cudaMemcpyAsync(cg_r_.p, b, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
-  vcycle(0, cg_r_.p, nullptr);
+  precondition(nullptr);
   MGPBD_CUDA(cudaMemcpyAsync(cg_p_.p, levels_[0].xa.p, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
   launch_dot_partials(cg_r_.p, levels_[0].xa.p, n, partials_.p, s);
   launch_dot_partials(b, b, n, partials_.p + blocks, s);
@@ -501,15 +531,17 @@ int32_t Solver::pcg_graph(const float* b, float* x) {
     try {
       int64_t n = nt_;
       int blocks = reduce_blocks(n);
+      long long c0 = g_launches.load();
       MGPBD_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
       stream_ = cs;
       MGPBD_CUDA(cudaMemsetAsync(x, 0, sizeof(float) * n, cs));
       MGPBD_CUDA(cudaMemcpyAsync(cg_r_.p, b, sizeof(float) * n, cudaMemcpyDeviceToDevice, cs));
-      vcycle(0, cg_r_.p, nullptr);
+      precondition(nullptr);
       MGPBD_CUDA(cudaMemcpyAsync(cg_p_.p, levels_[0].xa.p, sizeof(float) * n, cudaMemcpyDeviceToDevice, cs));
       launch_dot_partials(cg_r_.p, levels_[0].xa.p, n, partials_.p, cs);
       launch_dot_partials(b, b, n, partials_.p + blocks, cs);
       launch_cg_init(cg_state_.p, partials_.p, blocks, p_.tol_cg, p_.rel_tol_cg, p_.maxiter_cg, cs);
+      long long c1 = g_launches.load();
       cudaStreamCaptureStatus cst;
       const cudaGraphNode_t* deps = nullptr;
       size_t ndeps = 0;
@@ -529,6 +561,11 @@ int32_t Solver::pcg_graph(const float* b, float* x) {
       cg_body(b, x);
       k_set_cond<<<1, 1, 0, bs>>>(handle, cg_state_.p);
       MGPBD_CHECK_LAUNCH();
+      long long c2 = g_launches.load();
+      // captured launches run later, when the graph does
+      g_launches.fetch_sub(c2 - c0);
+      graph_init_launches_ = c1 - c0;
+      graph_body_launches_ = c2 - c1;
       MGPBD_CUDA(cudaStreamEndCapture(bs, &body));
       stream_ = outer;
       MGPBD_CUDA(cudaStreamEndCapture(cs, &graph));
@@ -558,6 +595,7 @@ int32_t Solver::pcg_graph(const float* b, float* x) {
   }
   MGPBD_CUDA(cudaGraphLaunch(cg_exec_, outer));
   sync_read(h_state_, cg_state_.p, sizeof(CgState));
+  g_launches.fetch_add(graph_init_launches_ + graph_body_launches_ * h_state_->body_runs);
   status_ |= static_cast<uint32_t>(h_state_->status);
   return h_state_->iters;
 }
@@ -618,6 +656,10 @@ void Solver::solve(int32_t frame) {
   stats_.cg_iters_total = 0;
   stats_.cg_iters_last = 0;
   stats_.omega_last = 1.0;
+  log_.clear();
+  auto now = [] {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+  };
   for (int32_t ite = 0; ite < p_.maxiter; ++ite) {
     compute_constraints();
     double r = compute_rhs();
@@ -630,12 +672,16 @@ void Solver::solve(int32_t frame) {
       status_ |= MGPBD_STATUS_NAN;
       break;
     }
-    if (r < p_.atol || (r0 > 1e-12 && r < p_.rtol * r0)) break;
+    if (r < p_.atol || (r0 > 1e-12 && r < p_.rtol * r0)) {
+      log_.push_back({double(ite), r, 0.0, 1.0, now()});
+      break;
+    }
     fill_matrices();
     int32_t it = pcg(rhs_.p, dlam_.p);
     scatter(dlam_.p);
     double omega = p_.use_line_search ? line_search() : 1.0;
     apply_dpos(omega);
+    log_.push_back({double(ite), r, double(it), omega, now()});
     stats_.newton_iters = ite + 1;
     stats_.cg_iters_total += it;
     stats_.cg_iters_last = it;

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <array>
 #include <cstdint>
 #include <memory>
 #include <vector>
@@ -57,6 +58,7 @@ class Solver {
   // per-stage entry points
   void compute_constraints();
   void fill_matrices();
+  void refill_coarse();
   double compute_rhs();
   int32_t pcg(const float* b, float* x);
   void vcycle_into(const float* r, float* z);
@@ -65,6 +67,9 @@ class Solver {
   void apply_dpos(double omega);
 
   const mgpbd_stats& stats() const { return stats_; }
+  // rows of (iteration, residual, cg_iters, omega, host seconds) of the last
+  // solve, one per call the reference makes to benchmark.record_iteration
+  const std::vector<std::array<double, 5>>& newton_log() const { return log_; }
   uint32_t status() const { return status_; }
   void* field(int32_t id, int64_t* count);
   const Level& level(int32_t l) const;
@@ -83,6 +88,8 @@ class Solver {
   void update_smoother_weights();
   void factor_coarsest();
   void cg_body(const float* b, float* x);
+  // z = V-cycle(r) for the CG residual r (level-0 result left in xa)
+  void precondition(const CgState* guard);
   int32_t pcg_graph(const float* b, float* x);
   void sync_read(void* host, const void* dev, size_t bytes);
   double finalize_read(const double* partials, int blocks);
@@ -115,9 +122,12 @@ class Solver {
   cudaGraphExec_t cg_exec_ = nullptr;
   const float* cg_graph_b_ = nullptr;
   float* cg_graph_x_ = nullptr;
+  long long graph_init_launches_ = 0;
+  long long graph_body_launches_ = 0;
 
   mgpbd_stats stats_{};
   uint32_t status_ = 0;
+  std::vector<std::array<double, 5>> log_;
 };
 
 }  // namespace mgpbd

@@ -1,0 +1,312 @@
+"""`MGPBDSolverGPU` with the constructor, fields and methods of the
+reference's `cons/mgpbd_gpu.py:20-446`, running on libmgpbd.so.
+
+Inputs are CUDA tensors (or arrays, copied to the GPU): `v_p` (NV,3) float32
+is mutated in place like the reference's Taichi field; `v_p_ref`, `v_invm`,
+`t_i` (4*NT int32) and `t_m` are read.  After `init()` the solver-owned
+fields (`lambdaf`, `constraints`, `gradC`, `alpha_tilde`, `Dm_inv`,
+`rest_vol`, `v_p_old`, `v_predict`, `dpos`, `_b_gpu`, `_dlam_gpu`) are torch
+views of the library's device memory; they stay valid while the solver
+lives.  Nothing here computes the step on the CPU: if libmgpbd.so cannot be
+loaded, construction raises.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import numpy as np
+import torch
+
+from . import _native as N
+
+_MODES = {'parity': N.MGPBD_MODE_PARITY, 'fast': N.MGPBD_MODE_FAST}
+_COARSE = {'jacobi': N.MGPBD_COARSE_JACOBI, 'dense': N.MGPBD_COARSE_DENSE_F64}
+_SMOOTH = {'jacobi': N.MGPBD_SMOOTH_JACOBI, 'safe': N.MGPBD_SMOOTH_JACOBI_SAFE}
+
+
+class _DeviceArray:
+  """Minimal `__cuda_array_interface__` holder used to view library memory."""
+
+  def __init__(self, ptr, shape, typestr):
+    self.__cuda_array_interface__ = {
+        'shape': tuple(shape), 'typestr': typestr, 'data': (int(ptr), False), 'version': 3,
+        'strides': None,
+    }
+
+
+def device_view(ptr, shape, dtype=torch.float32):
+  typestr = {torch.float32: '<f4', torch.int32: '<i4', torch.float64: '<f8'}[dtype]
+  if int(np.prod(shape)) == 0:
+    return torch.empty(shape, dtype=dtype, device='cuda')
+  return torch.as_tensor(_DeviceArray(ptr, shape, typestr), device='cuda')
+
+
+def _cuda(a, dtype, shape=None):
+  if isinstance(a, torch.Tensor):
+    t = a
+    if t.device.type != 'cuda' or t.dtype != dtype or not t.is_contiguous():
+      t = t.to(device='cuda', dtype=dtype).contiguous()
+  else:
+    if hasattr(a, 'to_numpy'):
+      a = a.to_numpy()
+    t = torch.as_tensor(np.ascontiguousarray(np.asarray(a)), dtype=dtype).cuda()
+  if shape is not None:
+    t = t.reshape(shape)
+  return t
+
+
+class _Scalar:
+  """Stands in for the reference's 0-d Taichi field (`self.damp[None]`)."""
+
+  def __init__(self, v):
+    self.v = float(v)
+
+  def __getitem__(self, key):
+    return self.v
+
+  def __setitem__(self, key, val):
+    raise AttributeError('damp is fixed at construction')
+
+
+class MGPBDSolverGPU:
+  """Multigrid-accelerated global XPBD step (cons/mgpbd_gpu.py:20-446).
+
+  Extra keyword options select the CUDA library's variants:
+    mode='parity'  reference algorithm with host-checked loops (default);
+    mode='fast'    device-driven CG in one CUDA graph per solve;
+    rel_tol_cg     CG also stops at |r| < rel_tol_cg * |b| (0: reference);
+    smoother       'jacobi' (omega_jacobi) or 'safe' (omega <= 4/(3 lambda_max));
+    coarse_solver  'jacobi' (min(50,n) sweeps) or 'dense' (float64 Cholesky);
+    max_levels     extra levels by matrix-graph aggregation (0: reference);
+    kinematic_pins vertices with invm == 0 skip the prediction;
+    cg_alias       reproduce the reference PCG whose V-cycle overwrites the
+                   CG residual (cons/mgpcg_gpu.py:239-240 vs :275).
+  """
+
+  def __init__(self, v_p, v_p_ref, v_invm, t_i, t_m, gravity, dt, mu=1e6, damp=1.0, maxiter=20,
+               atol=1e-4, rtol=1e-2, maxiter_cg=100, tol_cg=1e-5, n_smooth=2,
+               omega_jacobi=2.0 / 3.0, setup_interval=10000, use_line_search=True,
+               aggregation='tet', benchmark=None, *, mode='parity', rel_tol_cg=0.0,
+               coarse_solver='jacobi', smoother='jacobi', max_levels=0, max_coarse=400,
+               kinematic_pins=False, coarse_sweeps=0, cg_alias=False, compliance=0.0,
+               check_finite=True):
+    if aggregation != 'tet':
+      raise NotImplementedError(
+          "aggregation='pyamg' needs PyAMG's smoothed-aggregation setup, which this "
+          "library does not provide; use aggregation='tet'")
+    self._lib = N.lib()
+    self.v_p = _cuda(v_p, torch.float32, (-1, 3))
+    if isinstance(v_p, torch.Tensor) and self.v_p.data_ptr() != v_p.data_ptr():
+      raise ValueError('v_p must be a contiguous float32 CUDA tensor (it is updated in place)')
+    self.v_p_ref = _cuda(v_p_ref, torch.float32, (-1, 3))
+    self.v_invm = _cuda(v_invm, torch.float32, (-1,))
+    self.t_i = _cuda(t_i, torch.int32, (-1,))
+    self.t_m = t_m
+    self.n_verts = self.v_p.shape[0]
+    self.n_tets = self.t_i.shape[0] // 4
+    if self.v_p_ref.shape[0] != self.n_verts or self.v_invm.shape[0] != self.n_verts:
+      raise ValueError('v_p, v_p_ref and v_invm must have the same number of vertices')
+    if self.t_i.shape[0] != 4 * self.n_tets:
+      raise ValueError('t_i must hold 4 indices per tet')
+    self.gravity = [float(g) for g in (gravity.to_numpy() if hasattr(gravity, 'to_numpy') else gravity)]
+    self.dt = float(dt)
+    self.mu = float(mu)
+    self.maxiter = maxiter
+    self.atol = atol
+    self.rtol = rtol
+    self.maxiter_cg = maxiter_cg
+    self.tol_cg = tol_cg
+    self.n_smooth = n_smooth
+    self.omega_jacobi = omega_jacobi
+    self.setup_interval = setup_interval
+    self.use_line_search = use_line_search
+    self.aggregation = aggregation
+    self.benchmark = benchmark
+    self.damp = _Scalar(damp)
+    self.check_finite = check_finite
+    self.v_v = torch.zeros_like(self.v_p)
+
+    p = N.default_params()
+    p.dt = self.dt
+    p.mu = self.mu
+    p.damp = float(damp)
+    for k in range(3):
+      p.gravity[k] = self.gravity[k]
+    p.maxiter = int(maxiter)
+    p.atol = float(atol)
+    p.rtol = float(rtol)
+    p.maxiter_cg = int(maxiter_cg)
+    p.tol_cg = float(tol_cg)
+    p.n_smooth = int(n_smooth)
+    p.omega_jacobi = float(omega_jacobi)
+    p.setup_interval = int(setup_interval)
+    p.use_line_search = int(bool(use_line_search))
+    p.mode = _MODES[mode]
+    p.rel_tol_cg = float(rel_tol_cg)
+    p.coarse_solver = _COARSE[coarse_solver]
+    p.smoother = _SMOOTH[smoother]
+    p.max_levels = int(max_levels)
+    p.max_coarse = int(max_coarse)
+    p.kinematic_pins = int(bool(kinematic_pins))
+    p.coarse_sweeps = int(coarse_sweeps)
+    p.cg_alias = int(bool(cg_alias))
+    p.compliance = float(compliance)
+    self.params = p
+    h = C.c_void_p()
+    N.check(self._lib.mgpbd_create(C.byref(p), C.byref(h)), 'mgpbd_create')
+    self._h = h
+    N.check(self._lib.mgpbd_set_mesh(h, self.v_p_ref.data_ptr(), self.v_invm.data_ptr(),
+                                     self.t_i.data_ptr(), self.n_verts, self.n_tets,
+                                     self.v_p.data_ptr(), self.v_v.data_ptr()), 'mgpbd_set_mesh')
+    self._inited = False
+    self._gpu_solver = None
+
+  def __del__(self):
+    h = getattr(self, '_h', None)
+    if h is not None and h.value:
+      try:
+        self._lib.mgpbd_destroy(h)
+      except Exception:
+        pass
+      self._h = None
+
+  # ------------------------------------------------------------------ #
+  def _stream(self):
+    N.check(self._lib.mgpbd_set_stream(self._h, C.c_void_p(torch.cuda.current_stream().cuda_stream)),
+            'mgpbd_set_stream')
+
+  def _field(self, name, shape):
+    ptr = C.c_void_p()
+    cnt = C.c_int64()
+    N.check(self._lib.mgpbd_field(self._h, N.FIELD[name], C.byref(ptr), C.byref(cnt)), 'mgpbd_field')
+    return device_view(ptr.value, shape)
+
+  # cons/mgpbd_gpu.py:92-114
+  def init(self):
+    self._stream()
+    N.check(self._lib.mgpbd_init(self._h), 'mgpbd_init')
+    nt, nv = self.n_tets, self.n_verts
+    self.lambdaf = self._field('lambdaf', (nt,))
+    self.constraints = self._field('constraints', (nt,))
+    self.gradC = self._field('gradC', (nt, 4, 3))
+    self.alpha_tilde = self._field('alpha_tilde', (nt,))
+    self.rest_vol = self._field('rest_vol', (nt,))
+    self.Dm_inv = self._field('Dm_inv', (nt, 3, 3))
+    self.v_p_old = self._field('v_p_old', (nv, 3))
+    self.v_predict = self._field('v_predict', (nv, 3))
+    self.dpos = self._field('dpos', (nv, 3))
+    self._b_gpu = self._field('b', (nt,))
+    self._dlam_gpu = self._field('dlam', (nt,))
+    from .mgpcg_gpu import GPUMultigridSolver
+    self._gpu_solver = GPUMultigridSolver._from_handle(self)
+    self._nnz = int(self._gpu_solver._gpu_As[0].nnz)
+    self._inited = True
+
+  @property
+  def _alpha_tilde_np(self):
+    return self.alpha_tilde.detach().cpu().numpy()
+
+  @property
+  def _A_indptr(self):
+    return self._gpu_solver._gpu_As[0].indptr.cpu().numpy()
+
+  @property
+  def _A_indices(self):
+    return self._gpu_solver._gpu_As[0].indices.cpu().numpy()
+
+  def stats(self) -> dict:
+    s = N.Stats()
+    N.check(self._lib.mgpbd_get_stats(self._h, C.byref(s)), 'mgpbd_get_stats')
+    nl = s.n_levels
+    return {
+        'newton_iters': s.newton_iters, 'cg_iters_total': s.cg_iters_total,
+        'cg_iters_last': s.cg_iters_last, 'n_levels': nl, 'residual0': s.residual0,
+        'residual': s.residual, 'omega_last': s.omega_last, 'status': s.status,
+        'rows': list(s.rows[:nl]), 'nnz': list(s.nnz[:nl]),
+    }
+
+  def newton_log(self):
+    n = C.c_int32()
+    N.check(self._lib.mgpbd_newton_log(self._h, 0, None, C.byref(n)), 'mgpbd_newton_log')
+    rows = np.zeros((max(n.value, 1), 5), np.float64)
+    N.check(self._lib.mgpbd_newton_log(self._h, n.value, rows.ctypes.data, C.byref(n)),
+            'mgpbd_newton_log')
+    return rows[:n.value]
+
+  def _check(self, rc, where):
+    if rc == -5 and not self.check_finite:
+      return
+    N.check(rc, where)
+
+  # ------------------------------------------------------------------ #
+  # cons/mgpbd_gpu.py:200-219
+  def step(self, frame: int = 0):
+    self.make_prediction()
+    self.solve(frame)
+    self.update_vel()
+
+  def make_prediction(self):
+    self._stream()
+    N.check(self._lib.mgpbd_make_prediction(self._h), 'mgpbd_make_prediction')
+
+  def update_vel(self):
+    self._stream()
+    N.check(self._lib.mgpbd_update_vel(self._h), 'mgpbd_update_vel')
+
+  # cons/mgpbd_gpu.py:397-446
+  def solve(self, frame: int = 0):
+    self._stream()
+    if self.benchmark is not None:
+      self.benchmark.begin_frame(frame)
+    rc = self._lib.mgpbd_solve(self._h, int(frame))
+    if self.benchmark is not None:
+      for ite, r, cg, om, t in self.newton_log():
+        self.benchmark.record_iteration(int(ite), r, cg_iters=int(cg), omega=om, t=t)
+      self.benchmark.end_frame()
+    self._check(rc, 'mgpbd_solve')
+
+  # ---- per-stage methods under the reference's names ------------------ #
+  def _compute_C_and_gradC(self):
+    self._stream()
+    N.check(self._lib.mgpbd_compute_constraints(self._h), 'mgpbd_compute_constraints')
+
+  def _residual_norm_gpu(self) -> float:
+    self._stream()
+    r = C.c_double()
+    N.check(self._lib.mgpbd_compute_rhs(self._h, C.byref(r)), 'mgpbd_compute_rhs')
+    return r.value
+
+  def _compute_rhs_gpu(self):
+    self._residual_norm_gpu()
+
+  def _fill_A_and_update_gpu(self):
+    self._stream()
+    N.check(self._lib.mgpbd_fill_matrices(self._h), 'mgpbd_fill_matrices')
+
+  def _zero_dpos(self):
+    self.dpos.zero_()
+
+  def _scatter_dlam_gpu(self):
+    self._stream()
+    N.check(self._lib.mgpbd_scatter(self._h, self._dlam_gpu.data_ptr()), 'mgpbd_scatter')
+
+  def _line_search(self, beta=0.5, max_steps=10):
+    if beta != 0.5 or max_steps != 10:
+      raise NotImplementedError('the line search uses beta=0.5, max_steps=10 (reference defaults)')
+    self._stream()
+    w = C.c_double()
+    N.check(self._lib.mgpbd_line_search(self._h, C.byref(w)), 'mgpbd_line_search')
+    return w.value
+
+  def _apply_dpos(self, omega: float):
+    self._stream()
+    N.check(self._lib.mgpbd_apply_dpos(self._h, float(omega)), 'mgpbd_apply_dpos')
+
+  def synchronize(self):
+    N.check(self._lib.mgpbd_synchronize(self._h), 'mgpbd_synchronize')
+
+
+def _now():
+  return time.perf_counter()

@@ -92,6 +92,13 @@ typedef struct mgpbd_params {
   int32_t max_coarse;     /* coarsest-level target size (reference: 400)      */
   int32_t kinematic_pins; /* 1: invm==0 vertices skip the prediction          */
   int32_t coarse_sweeps;  /* coarsest Jacobi sweeps, 0 = min(50,n) (ref)      */
+  /* 1: reproduce the reference PCG as shipped, where vcycle(0) writes its
+   * residual into the CG residual vector (cons/mgpcg_gpu.py:239-240 share
+   * self._r[0] with :275,303); 0 (default): the V-cycle has its own. */
+  int32_t cg_alias;
+  /* > 0: alpha~ = compliance / dt^2 for every tet (the XPBD convention of
+   * cons/length.py:30) instead of 1 / (mu dt^2 V_t) (cons/mgpbd_gpu.py:151) */
+  float compliance;
 } mgpbd_params;
 
 typedef struct mgpbd_stats {
@@ -119,6 +126,9 @@ const char* mgpbd_strerror(int code);
 /* Text of the last error raised on the calling thread (empty if none). */
 const char* mgpbd_last_error(void);
 const char* mgpbd_version(void);
+/* Number of CUDA kernels this library has launched in the process so far
+ * (kernels inside its CUDA graphs are counted each time they run). */
+int64_t mgpbd_launch_count(void);
 
 /* Replaces MGPBDSolverGPU.__init__ (cons/mgpbd_gpu.py:22-90). */
 int mgpbd_create(const mgpbd_params* params, mgpbd_handle* out);
@@ -148,6 +158,12 @@ int mgpbd_update_vel(mgpbd_handle h);
 int mgpbd_get_stats(mgpbd_handle h, mgpbd_stats* out);
 /* Block until the handle's stream has finished its queued work. */
 int mgpbd_synchronize(mgpbd_handle h);
+/* Per-Newton-iteration record of the last solve, the values the reference
+ * passes to benchmark.record_iteration (cons/mgpbd_gpu.py:415-416,442-443):
+ * rows of 5 doubles (iteration, residual, cg_iters, omega, host seconds on
+ * a monotonic clock).  Writes min(max_rows, *n_rows) rows; *n_rows gets the
+ * total. */
+int mgpbd_newton_log(mgpbd_handle h, int32_t max_rows, double* rows, int32_t* n_rows);
 /* Status bits of the last solve (0 = clean). */
 int mgpbd_get_status(mgpbd_handle h, uint32_t* status);
 
@@ -184,6 +200,9 @@ int mgpbd_compute_constraints(mgpbd_handle h);
 /* _fill_A_and_update_gpu (cons/mgpbd_gpu.py:320-324): A values, diag^-1,
  * coarse values by the contribution map (cons/mgpcg_gpu.py:175-212) */
 int mgpbd_fill_matrices(mgpbd_handle h);
+/* GPUMultigridSolver.update_all_coarse_matrices (cons/mgpcg_gpu.py:200-212)
+ * from the current level-0 values (after a caller changed them) */
+int mgpbd_refill_coarse(mgpbd_handle h);
 /* _compute_rhs_gpu + _residual_norm_gpu (cons/mgpbd_gpu.py:253-267) */
 int mgpbd_compute_rhs(mgpbd_handle h, double* residual_norm);
 /* GPUMultigridSolver.solve (cons/mgpcg_gpu.py:261-329): solves A x = b on
@@ -215,6 +234,8 @@ int mgpbd_dot(int32_t n, const float* a, const float* b, double* out, void* stre
 /* gpu_axpy (:26-30) y += alpha x ; gpu_xpay (:33-37) y = x + alpha y */
 int mgpbd_axpy(int32_t n, float alpha, const float* x, float* y, void* stream);
 int mgpbd_xpay(int32_t n, float alpha, const float* x, float* y, void* stream);
+/* gpu_scale (cons/sparse_gpu.py:52-55) x *= alpha */
+int mgpbd_scale(int32_t n, float alpha, float* x, void* stream);
 
 /* ---- host-side structure builders (host arrays, no GPU needed) ---------- */
 /* _build_sparsity_pattern (cons/mgpbd_gpu.py:153-194).  Call with indptr ==

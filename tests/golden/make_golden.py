@@ -25,6 +25,15 @@ is scrambled from the first Newton iteration on.  The fixtures record the
 intended semantics (values and columns in the same diagonal-last order) by
 making `astype` keep the index order; `asshipped_*` keys record the
 unpatched behaviour as evidence.
+
+A second defect sits in the PCG: `vcycle(0)` computes its residual into
+`self._r[0]` (`cons/mgpcg_gpu.py:239-240`), which is also the CG residual
+vector of `solve` (`:275,303-305`), so every preconditioner application
+overwrites the CG residual with `r - A x_presmoothed`.  Each step case is
+written twice: `step_<case>.npz` with the V-cycle's level-0 residual kept
+apart from the CG residual (the intended algorithm; the wrapper saves and
+restores `_r[0]` around `vcycle(0)`), and `step_<case>_cgalias.npz` with the
+reference's PCG exactly as shipped.
 """
 
 from __future__ import annotations
@@ -211,7 +220,7 @@ STEP_CASES = {
 }
 
 
-def step_fixture(ref, mg, name, build, kw, substeps, out):
+def step_fixture(ref, mg, name, build, kw, substeps, out, cg_alias):
   import taichi as ti
   t0 = time.time()
   xr, x0, t, invm = build(ref)
@@ -232,6 +241,17 @@ def step_fixture(ref, mg, name, build, kw, substeps, out):
   s = make_solver(mg, ti, xr, x0, t, invm, benchmark=rec, **kw)
   s.init()
   gs = s._gpu_solver
+  res['cg_alias'] = np.array(bool(cg_alias))
+  if not cg_alias:
+    orig_vcycle = gs.vcycle
+
+    def vcycle_keep_r0(level=0):
+      saved = gs._r[0].to_numpy() if level == 0 else None
+      orig_vcycle(level)
+      if level == 0:
+        gs._r[0].from_numpy(saved)
+
+    gs.vcycle = vcycle_keep_r0
   res['Dm_inv'] = s.Dm_inv.to_numpy()
   res['rest_vol'] = s.rest_vol.to_numpy()
   res['alpha_tilde'] = s.alpha_tilde.to_numpy()
@@ -270,7 +290,9 @@ def step_fixture(ref, mg, name, build, kw, substeps, out):
       n = gs._level_sizes[0]
       gs._b[0].from_numpy(b.to_numpy())
       gs._x[0].fill(0.0)
+      r_saved = gs._r[0].to_numpy()
       gs.vcycle(0)
+      gs._r[0].from_numpy(r_saved)
       snap['vcycle_z'] = gs._x[0].to_numpy()
       # level SpMV / Jacobi with a seeded vector
       rng = np.random.default_rng(11)
@@ -318,8 +340,9 @@ def step_fixture(ref, mg, name, build, kw, substeps, out):
   recs = [(f, *r) for f, fr in enumerate(rec.frames) for r in fr]
   res['newton_log'] = np.array(recs, np.float64).reshape(-1, 5)
   set_astype_keeps_order(False)
-  np.savez_compressed(os.path.join(out, f'step_{name}.npz'), **res)
-  print(f'[step] {name}: {len(recs)} newton iterations ({time.time() - t0:.1f}s)', flush=True)
+  suffix = '_cgalias' if cg_alias else ''
+  np.savez_compressed(os.path.join(out, f'step_{name}{suffix}.npz'), **res)
+  print(f'[step] {name}{suffix}: {len(recs)} newton iterations ({time.time() - t0:.1f}s)', flush=True)
 
 
 def main():
@@ -333,7 +356,8 @@ def main():
     structure_fixtures(a.ref, mg, ta, a.out)
   if a.only in (None, 'step'):
     for name, (build, kw, n) in STEP_CASES.items():
-      step_fixture(a.ref, mg, name, build, kw, n, a.out)
+      for alias in (False, True):
+        step_fixture(a.ref, mg, name, build, kw, n, a.out, alias)
 
 
 if __name__ == '__main__':

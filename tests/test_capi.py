@@ -1,0 +1,84 @@
+"""The C-ABI library: it loads, exports every symbol include/mgpbd.h
+declares, and its host-only entry points validate arguments.  No GPU."""
+
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from controllable_pbd_3d_gb300 import _native as N
+
+
+def declared():
+  hdr = open(os.path.join(ROOT, 'include', 'mgpbd.h')).read()
+  return sorted(set(re.findall(r'\b(mgpbd_[a-z_0-9]+)\s*\(', hdr)))
+
+
+def test_library_loads_and_exports_every_declared_symbol():
+  L = N.lib()
+  names = declared()
+  assert len(names) >= 40
+  for n in names:
+    assert hasattr(L, n), n
+  out = subprocess.run(['nm', '-D', '--defined-only', N.lib_path()], capture_output=True,
+                       text=True).stdout
+  exported = {ln.split()[-1] for ln in out.splitlines() if ' T mgpbd_' in ln}
+  assert set(names) == exported
+
+
+def test_ctypes_signatures_cover_the_header():
+  assert set(N._SIGS) == set(declared())
+
+
+def test_params_struct_layout():
+  p = N.default_params()
+  # every field is 4 bytes; gravity counts 3
+  assert C.sizeof(N.Params) == 4 * (len(N.Params._fields_) + 2)
+  assert abs(p.mu - 1e6) < 1 and p.maxiter == 20 and p.maxiter_cg == 100
+  assert abs(p.omega_jacobi - 2.0 / 3.0) < 1e-7 and p.use_line_search == 1
+  assert p.mode == N.MGPBD_MODE_PARITY and p.cg_alias == 0
+
+
+def test_error_codes_and_strings():
+  L = N.lib()
+  assert L.mgpbd_strerror(0) == b'ok'
+  assert L.mgpbd_strerror(-1) == b'invalid argument'
+  assert L.mgpbd_create(None, None) == -1
+  p = N.default_params()
+  h = C.c_void_p()
+  # dt must be positive
+  assert L.mgpbd_create(C.byref(p), C.byref(h)) == -1
+  assert b'dt' in L.mgpbd_last_error()
+  # calls on a null handle
+  assert L.mgpbd_init(None) == -1
+  assert L.mgpbd_step(None, 0) == -1
+
+
+def test_host_entry_points_validate():
+  L = N.lib()
+  nnz = C.c_int64()
+  assert L.mgpbd_host_pattern(None, 1, C.byref(nnz), None, None) == -1
+  t = np.array([0, 1, 2, 3], np.int32)
+  agg = np.zeros(1, np.int32)
+  n = C.c_int32()
+  assert L.mgpbd_host_aggregate(t.ctypes.data, 1, 0, agg.ctypes.data, C.byref(n)) == -1
+  assert L.mgpbd_host_aggregate(t.ctypes.data, 1, 8, agg.ctypes.data, C.byref(n)) == 0
+  assert n.value == 1
+
+
+def test_step_before_init_is_a_state_error():
+  pytest.importorskip('torch')
+  L = N.lib()
+  p = N.default_params()
+  p.dt = 1.0 / 300
+  h = C.c_void_p()
+  assert L.mgpbd_create(C.byref(p), C.byref(h)) == 0
+  try:
+    assert L.mgpbd_step(h, 0) == -4
+    assert L.mgpbd_init(h) == -4  # no mesh bound
+  finally:
+    L.mgpbd_destroy(h)

@@ -1,0 +1,169 @@
+"""CUDA path (through the C ABI) against the reference's golden vectors and
+the oracle.
+
+Tolerances (float32 arithmetic on both sides; the CUDA path uses its own
+3x3 SVD and a different summation order than the reference):
+  per-stage values   max|gpu - ref| <= 1e-4 * max|ref|   (1e-5 for C)
+  positions          max|gpu - ref| <= 1e-5 * max|ref| after the fixture's
+                     substeps (the target of the MGPBD step)
+Integer structure (pattern, aggregates, coarse pattern, contribution map) is
+compared bit for bit.
+"""
+
+import numpy as np
+import pytest
+
+from conftest import golden, solver_kwargs, step_fixture_names
+
+pytestmark = pytest.mark.gpu
+
+NAMES = step_fixture_names()
+
+
+def rel(a, b):
+  a = np.asarray(a, np.float64)
+  b = np.asarray(b, np.float64)
+  return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
+
+
+def np_(t):
+  return t.detach().cpu().numpy()
+
+
+def make_solver(torch, z, **extra):
+  from controllable_pbd_3d_gb300.mgpbd_gpu import MGPBDSolverGPU
+  x = torch.tensor(z['x0'], device='cuda')
+  kw = solver_kwargs(z)
+  kw.update(extra)
+  s = MGPBDSolverGPU(x, torch.tensor(z['x_ref'], device='cuda'),
+                     torch.tensor(z['invm'], device='cuda'),
+                     torch.tensor(z['t_i'], device='cuda'), None, z['gravity'].tolist(),
+                     float(z['dt']), cg_alias=bool(z['cg_alias']), **kw)
+  s.init()
+  return s, x
+
+
+@pytest.mark.parametrize('name', NAMES)
+def test_init_structure_and_rest_shape(cuda, name):
+  z = golden(name)
+  s, _ = make_solver(cuda, z)
+  g = s._gpu_solver
+  np.testing.assert_array_equal(np_(g._gpu_As[0].indices), z['indices'])
+  np.testing.assert_array_equal(np_(g._gpu_As[0].indptr), z['indptr'])
+  np.testing.assert_array_equal(np_(g._gpu_As[1].indices), z['coarse_indices'])
+  np.testing.assert_array_equal(np_(g._gpu_As[1].indptr), z['coarse_indptr'])
+  np.testing.assert_array_equal(np_(g._agg[0]), z['agg_ids'])
+  assert rel(np_(s.Dm_inv), z['Dm_inv']) < 1e-5
+  assert rel(np_(s.alpha_tilde), z['alpha_tilde']) < 1e-5
+  assert rel(np_(s.rest_vol), z['rest_vol']) < 1e-5
+  assert rel(np_(g._gpu_As[0].data), z['A0_data']) < 1e-4
+
+
+@pytest.mark.parametrize('name', NAMES)
+def test_first_newton_iteration_stages(cuda, name):
+  """Each stage of cons/mgpbd_gpu.py:405-440 on identical inputs."""
+  z = golden(name)
+  s, x = make_solver(cuda, z)
+  g = s._gpu_solver
+  s.make_prediction()
+  assert rel(np_(x), z['it0_x_pred']) < 1e-6
+  s.lambdaf.zero_()
+  s._compute_C_and_gradC()
+  assert rel(np_(s.constraints), z['it0_constraints']) < 1e-5
+  assert rel(np_(s.gradC), z['it0_gradC']) < 1e-4
+  s._fill_A_and_update_gpu()
+  assert rel(np_(g._gpu_As[0].data), z['it0_A_data']) < 1e-4
+  assert rel(np_(g._gpu_As[1].data), z['it0_coarse_data']) < 1e-4
+  assert rel(np_(g._gpu_As[0].diag_inv), z['it0_diag_inv0']) < 1e-4
+  assert rel(np_(g._gpu_As[1].diag_inv), z['it0_diag_inv1']) < 1e-4
+  s._residual_norm_gpu()
+  assert rel(np_(s._b_gpu), z['it0_b']) < 1e-5
+  zz = g.vcycle_apply(cuda.tensor(z['it0_b'], device='cuda'))
+  assert rel(np_(zz), z['it0_vcycle_z']) < 1e-4
+  it = g.solve(s._b_gpu, s._dlam_gpu)
+  assert it == int(z['it0_cg_iters'])
+  assert rel(np_(s._dlam_gpu), z['it0_dlam']) < 1e-3
+  s._scatter_dlam_gpu()
+  assert rel(np_(s.dpos), z['it0_dpos']) < 1e-3
+  assert rel(np_(s.lambdaf), z['it0_lambda_post']) < 1e-3
+  assert s._line_search() == float(z['it0_omega'])
+
+
+@pytest.mark.parametrize('name', NAMES)
+def test_level_spmv_and_jacobi(cuda, name):
+  """GPUSparseMatrix.spmv / jacobi_smooth (cons/sparse_gpu.py:123-144) on
+  the reference's own first-iteration matrices."""
+  z = golden(name)
+  s, _ = make_solver(cuda, z)
+  g = s._gpu_solver
+  s.make_prediction()
+  s.lambdaf.zero_()
+  s._compute_C_and_gradC()
+  s._fill_A_and_update_gpu()
+  for lvl, A in enumerate(g._gpu_As):
+    xv = cuda.tensor(z[f'it0_spmv_x{lvl}'], device='cuda')
+    y = cuda.empty_like(xv)
+    A.spmv(xv, y)
+    assert rel(np_(y), z[f'it0_spmv_y{lvl}']) < 1e-4
+    bv = cuda.tensor(z[f'it0_jac_b{lvl}'], device='cuda')
+    A.jacobi_smooth(bv, xv, y, s.omega_jacobi)
+    assert rel(np_(y), z[f'it0_jac_y{lvl}']) < 1e-4
+
+
+@pytest.mark.parametrize('name', NAMES)
+def test_substep_trajectory(cuda, name):
+  """Whole substeps (cons/mgpbd_gpu.py:200-204): positions within 1e-5 of
+  the reference's."""
+  z = golden(name)
+  s, x = make_solver(cuda, z)
+  traj = z['x_traj']
+  for k in range(len(traj)):
+    s.step(k)
+    scale = float(np.abs(traj[k]).max())
+    err = float(np.abs(np_(x) - traj[k]).max())
+    assert err <= 1e-5 * scale, (k, err)
+  log = z['newton_log']
+  last = s.newton_log()
+  assert len(last) == int(np.sum(log[:, 0] == log[-1, 0]))
+
+
+@pytest.mark.parametrize('mode', ['parity', 'fast'])
+def test_cube10_against_float64_oracle(cuda, mode):
+  """A 10^3 cube (5000 tets) against the float64 oracle, both run with
+  the same options to tight tolerances."""
+  from controllable_pbd_3d_gb300 import meshgen
+  from oracle.mgpbd_oracle import MGPBDOracle
+  n = 10
+  xr, t = meshgen.hex_grid_tets(n, n, n)
+  x0, _ = meshgen.hex_grid_tets(n, n, n, jitter=0.02, seed=3)
+  invm = np.ones(len(xr), np.float32)
+  invm[meshgen.grid_face_vertices(n, n, n, 1)] = 0
+  kw = dict(mu=1e5, damp=0.993, maxiter=6, rtol=1e-6, atol=1e-9, maxiter_cg=200, tol_cg=1e-9,
+            rel_tol_cg=1e-7)
+  extra = dict(smoother='safe', coarse_solver='jacobi') if mode == 'fast' else {}
+  o = MGPBDOracle(x0, xr, invm, t, [0, -9.8, 0], 1 / 300, dtype=np.float64,
+                  smoother=extra.get('smoother', 'jacobi'), **kw)
+  o.init()
+  xt = cuda.tensor(x0, device='cuda')
+  from controllable_pbd_3d_gb300.mgpbd_gpu import MGPBDSolverGPU
+  s = MGPBDSolverGPU(xt, cuda.tensor(xr, device='cuda'), cuda.tensor(invm, device='cuda'),
+                     cuda.tensor(t, device='cuda'), None, [0, -9.8, 0], 1 / 300, mode=mode, **kw,
+                     **extra)
+  s.init()
+  for k in range(2):
+    o.step(k)
+    s.step(k)
+  err = float(np.abs(np_(xt) - o.x).max())
+  assert err <= 1e-5 * float(np.abs(o.x).max()), err
+
+
+def test_fast_mode_matches_parity_mode(cuda):
+  """The captured device-driven CG computes what the host-driven one does."""
+  z = golden('step_cube6_mu3e4.npz')
+  s1, x1 = make_solver(cuda, z)
+  s2, x2 = make_solver(cuda, z, mode='fast')
+  for k in range(2):
+    s1.step(k)
+    s2.step(k)
+  assert float(np.abs(np_(x1) - np_(x2)).max()) <= 1e-6
+  assert s1.stats()['cg_iters_total'] == s2.stats()['cg_iters_total']
