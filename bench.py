@@ -56,7 +56,13 @@ def workload(n, seed=0):
 
 SOLVER_KW = dict(damp=1.0, maxiter=20, atol=1e-4, rtol=1e-2, maxiter_cg=200, tol_cg=1e-12,
                  rel_tol_cg=1e-6, n_smooth=2, kinematic_pins=True)
-FAST_KW = dict(mode='fast', smoother='safe', coarse_solver='jacobi')
+# the optimised step: device-driven CG (one CUDA graph per solve), matrix-free
+# operator, degree-8 Chebyshev preconditioner
+FAST_KW = dict(mode='fast', precond='cheb', cheb_degree=8, cheb_lo=0.01)
+# the plain float32 AMG-PCG: the reference's two-level tet-aggregation V-cycle
+# on CSR matrices with host-checked loops; the smoother weight is capped at
+# 4/(3 lambda_max) because omega = 2/3 diverges at this stiffness
+PLAIN_KW = dict(mode='parity', smoother='safe', precond='vcycle')
 DT = 1.0 / 60.0 / 5.0
 
 
@@ -168,39 +174,71 @@ def time_steps(torch, s, k, first):
   return e0.elapsed_time(e1) / 1e3, st
 
 
-def kernel_roofline(torch, s, hbm_peak, peak_kind, reps=40):
-  """Level-0 weighted Jacobi sweep (the dominant launch: 4 per CG
-  iteration) timed with CUDA events on the current stream."""
-  from controllable_pbd_3d_gb300 import _native as N
+def _event_time(torch, fn, reps):
+  """Average device time of fn's launches: `reps` calls captured into one
+  CUDA graph (so host launch overhead does not leave gaps), replayed once
+  between CUDA events on the stream the kernels run on."""
+  for _ in range(3):
+    fn()
+  torch.cuda.synchronize()
+  g = torch.cuda.CUDAGraph()
+  side = torch.cuda.Stream()
+  with torch.cuda.stream(side):
+    with torch.cuda.graph(g, stream=side):
+      for _ in range(reps):
+        fn()
+  torch.cuda.synchronize()
+  stream = torch.cuda.current_stream()
+  e0 = torch.cuda.Event(enable_timing=True)
+  e1 = torch.cuda.Event(enable_timing=True)
+  g.replay()
+  torch.cuda.synchronize()
+  e0.record(stream)
+  g.replay()
+  e1.record(stream)
+  torch.cuda.synchronize()
+  return e0.elapsed_time(e1) / 1e3 / reps
+
+
+def roofline_matrix_free(torch, s, hbm_peak, peak_kind, reps=50):
+  """Matrix-free A x (vertex phase + tet phase), the operator behind every
+  CG iteration of the optimised step, timed with CUDA events on the current
+  stream.  Algorithmic bytes per application: vertex phase reads the
+  vertex-major gradients (16 B per tet slot), row offsets and inverse
+  masses, gathers x once per tet and writes u (16 B per vertex); tet phase
+  reads tet indices (16 B), gradients (48 B), alpha, x, gathers u once per
+  vertex and writes y."""
+  nt, nv = s.n_tets, s.n_verts
+  x = torch.randn(nt, device='cuda')
+  s.apply_A(x, matrix_free=1)
+  dt = _event_time(torch, lambda: s.apply_A(x, matrix_free=2), reps)
+  bytes_ = (16 * 4 * nt + 4 * (nv + 1) + 4 * nv + 4 * nt + 16 * nv) + \
+           (16 * nt + 48 * nt + 16 * nv + 4 * nt + 4 * nt + 4 * nt)
+  achieved = bytes_ / dt / 1e9
+  return {'kernel': 'k_jv<kSrcX> + k_jt_plain (matrix-free A x, 2 launches)', 'bound': 'hbm',
+          'achieved': round(achieved, 1), 'peak': hbm_peak, 'unit': 'GB/s',
+          'frac': round(achieved / hbm_peak, 4), 'peak_kind': peak_kind,
+          'algorithmic_bytes_per_launch': bytes_, 'launch_us': round(dt * 1e6, 2),
+          'working_set_note': 'the operator data (~46 MB at 320k tets) fits in the 129 MB L2, '
+                              'so repeated applications can exceed the HBM roofline',
+          'traffic': None}
+
+
+def roofline_csr(torch, s, hbm_peak, peak_kind, reps=40):
+  """Level-0 weighted Jacobi sweep of the CSR V-cycle (the dominant launch
+  of the plain AMG-PCG: 4 per CG iteration), vectorised row kernel."""
   A = s._gpu_solver._gpu_As[0]
   n, nnz = A.n_rows, A.nnz
   b = torch.randn(n, device='cuda')
   x = torch.randn(n, device='cuda')
   y = torch.empty_like(x)
-  L = N.lib()
-  stream = torch.cuda.current_stream()
-
-  def launch():
-    N.check(L.mgpbd_csr_jacobi(n, A.indptr.data_ptr(), A.indices.data_ptr(), A.data.data_ptr(),
-                               A.diag_inv.data_ptr(), b.data_ptr(), x.data_ptr(), y.data_ptr(),
-                               0.5, C.c_void_p(stream.cuda_stream)), 'mgpbd_csr_jacobi')
-  for _ in range(5):
-    launch()
-  e0 = torch.cuda.Event(enable_timing=True)
-  e1 = torch.cuda.Event(enable_timing=True)
-  torch.cuda.synchronize()
-  e0.record(stream)
-  for _ in range(reps):
-    launch()
-  e1.record(stream)
-  torch.cuda.synchronize()
-  dt = e0.elapsed_time(e1) / 1e3 / reps
+  dt = _event_time(torch, lambda: s.level_sweep(0, 1, x, b, y, 0.5), reps)
   # algorithmic bytes: values + column ids + row pointers + x gathered once,
   # b, 1/diag read, x_new written
   bytes_ = 8 * nnz + 4 * (n + 1) + 4 * n * 4
   achieved = bytes_ / dt / 1e9
-  return {'kernel': 'k_csr_rows<32,kJacobi> (level-0 weighted Jacobi sweep)', 'bound': 'hbm',
-          'achieved': round(achieved, 1), 'peak': hbm_peak, 'unit': 'GB/s',
+  return {'kernel': 'k_csr_rows_vec<8,4,kJacobi> (level-0 weighted Jacobi sweep, CSR)',
+          'bound': 'hbm', 'achieved': round(achieved, 1), 'peak': hbm_peak, 'unit': 'GB/s',
           'frac': round(achieved / hbm_peak, 4), 'peak_kind': peak_kind,
           'algorithmic_bytes_per_launch': bytes_, 'launch_us': round(dt * 1e6, 2),
           'traffic': None}
@@ -265,21 +303,46 @@ def run_ours(args):
   e2e = {'value': round(ws * args.steps / t_e2e, 3), 'unit': UNIT,
          'h2d_bytes_per_step': 2 * x.numel() * 4, 'd2h_bytes_per_step': 2 * x.numel() * 4}
 
-  roof = kernel_roofline(torch, s, hbm, kind)
+  roof = roofline_matrix_free(torch, s, hbm, kind)
   st0 = st[-1]
+  n_verts, n_tets = s.n_verts, s.n_tets
+  del s
+  torch.cuda.empty_cache()
+
+  # the plain float32 AMG-PCG on the same workload (fewer steps: it is slow)
+  plain = None
+  if not args.no_plain:
+    kwp = dict(SOLVER_KW)
+    kwp.update(PLAIN_KW)
+    sp_, xp, _ = make_solver(torch, args.size, kwp)
+    sp_.step(0)
+    k_plain = max(1, min(args.steps, args.plain_steps))
+    tp, stp = time_steps(torch, sp_, k_plain, 1)
+    roof_csr = roofline_csr(torch, sp_, hbm, kind)
+    plain = {'value': round(k_plain / tp, 4), 'unit': UNIT, 'steps': k_plain,
+             'newton_iters_per_step': sum(x['newton_iters'] for x in stp) / k_plain,
+             'cg_iters_per_step': sum(x['cg_iters_total'] for x in stp) / k_plain,
+             'config': 'parity-mode CSR V-cycle (2-level tet aggregation, 50 coarse Jacobi '
+                       'sweeps, smoother weight min(2/3, 4/(3 lambda_max))), host-checked loops',
+             'roofline': roof_csr}
+    del sp_
+    torch.cuda.empty_cache()
   out = {
       'metric': METRIC, 'value': round(value, 3), 'unit': UNIT, 'n_gpus': ws,
       'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(t_max * 1e3 / args.steps, 3),
       'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
       'data': 'synthetic (seeded hex-grid cube; reference meshes unavailable)',
-      'config': {'workload': f'{args.size}^3 hex cube, 5 tets/hex', 'n_verts': s.n_verts,
-                 'n_tets': s.n_tets, 'nnz_level0': st0['nnz'][0], 'levels': st0['rows'],
+      'config': {'workload': f'{args.size}^3 hex cube, 5 tets/hex', 'n_verts': n_verts,
+                 'n_tets': n_tets, 'nnz_level0': st0['nnz'][0], 'levels': st0['rows'],
                  'compliance': compliance, 'dt': DT, 'rel_res_cg': 1e-6, 'mode': 'fast',
                  'l2': 'level-0 matrix 207 MB > L2, no flush', 'parallelism': f'replicas{ws}'},
       'newton_iters_per_step': newton / args.steps, 'cg_iters_per_step': cg / args.steps,
       'cg_iters_per_s': round(ws * cg / t_max, 1), 'gpu_launches': int(launches),
       'clocks': clk.summary(), 'e2e': e2e, 'roofline': roof,
   }
+  if plain is not None:
+    out['plain_fp32_amg_pcg'] = plain
+    out['speedup_vs_plain'] = round(value / ws / plain['value'], 2)
   if rank == 0 and not args.no_cpu_baseline:
     t_it, log = cpu_baseline_sample(args.size)
     per_sub = max(newton / args.steps, 1e-9)
@@ -331,6 +394,8 @@ def main():
   ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
   ap.add_argument('--size', type=int, default=40)
   ap.add_argument('--no-cpu-baseline', action='store_true')
+  ap.add_argument('--no-plain', action='store_true')
+  ap.add_argument('--plain-steps', type=int, default=2)
   args = ap.parse_args()
   if args.impl == 'reference':
     run_reference(args)

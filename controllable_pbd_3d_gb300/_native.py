@@ -49,7 +49,7 @@ class Params(C.Structure):
       ('omega_jacobi', f32), ('setup_interval', i32), ('use_line_search', i32), ('mode', i32),
       ('rel_tol_cg', f32), ('coarse_solver', i32), ('smoother', i32), ('max_levels', i32),
       ('max_coarse', i32), ('kinematic_pins', i32), ('coarse_sweeps', i32), ('cg_alias', i32),
-      ('compliance', f32),
+      ('compliance', f32), ('precond', i32), ('cheb_degree', i32), ('cheb_lo', f32),
   ]
 
 
@@ -102,6 +102,8 @@ _SIGS = {
     'mgpbd_scatter': (C.c_int, [vp, vp]),
     'mgpbd_line_search': (C.c_int, [vp, P_f64]),
     'mgpbd_apply_dpos': (C.c_int, [vp, f64]),
+    'mgpbd_apply_matrix': (C.c_int, [vp, i32, vp, vp]),
+    'mgpbd_level_sweep': (C.c_int, [vp, i32, i32, vp, vp, vp, f32]),
     'mgpbd_csr_spmv': (C.c_int, [i32, vp, vp, vp, vp, vp, vp]),
     'mgpbd_csr_jacobi': (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp, f32, vp]),
     'mgpbd_csr_diag_inv': (C.c_int, [i32, vp, vp, vp, vp, vp]),

@@ -78,6 +78,9 @@ void mgpbd_default_params(mgpbd_params* p) {
   p->coarse_sweeps = 0;
   p->cg_alias = 0;
   p->compliance = 0.0f;
+  p->precond = MGPBD_PRECOND_VCYCLE;
+  p->cheb_degree = 8;
+  p->cheb_lo = 0.01f;
 }
 
 const char* mgpbd_strerror(int code) {
@@ -256,6 +259,18 @@ int mgpbd_line_search(mgpbd_handle h, double* omega) {
 int mgpbd_apply_dpos(mgpbd_handle h, double omega) {
   if (!h) return MGPBD_EINVAL;
   return guarded([&] { h->impl.apply_dpos(omega); });
+}
+
+int mgpbd_apply_matrix(mgpbd_handle h, int32_t matrix_free, const float* x, float* y) {
+  if (!h || !x || !y) return MGPBD_EINVAL;
+  if (matrix_free < 0 || matrix_free > 2) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.apply_matrix(matrix_free, x, y); });
+}
+
+int mgpbd_level_sweep(mgpbd_handle h, int32_t level, int32_t op, const float* x, const float* b,
+                      float* y, float omega) {
+  if (!h || !x || !y || (op == 1 && !b)) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.level_sweep(level, op, x, b, y, omega); });
 }
 
 int mgpbd_synchronize(mgpbd_handle h) {

@@ -1,0 +1,529 @@
+// Matrix-free A = J W J^T + alpha~ and the Chebyshev-preconditioned CG of
+// FAST mode (see jform.cuh).  Reductions finish in the last block of the
+// kernel that produces them (ticket counter + fixed-order sum), so one CG
+// iteration of degree k is 2k + 2 kernels with no scalar-only launches.
+#include "jform.cuh"
+
+#include <cmath>
+
+#include "common.h"
+
+namespace mgpbd {
+
+namespace {
+
+constexpr int kT = 256;      // threads per block
+constexpr int kVG = 4;       // lanes per vertex in the vertex phase
+
+enum Src { kSrcX = 0, kSrcZbP = 1, kSrcScaled = 2 };
+enum Epi { kEpiPlain = 0, kEpiAp = 1, kEpiCheb = 2, kEpiPow = 3 };
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// block-wide float64 sum, result valid in thread 0 (fixed pattern)
+__device__ __forceinline__ double block_sum_d(double v) {
+  __shared__ double sh[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v = warp_sum_d(v);
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  v = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+  if (wid == 0) v = warp_sum_d(v);
+  __syncthreads();
+  return v;
+}
+
+// Publish this block's partial; returns true in the block that finished
+// last (all partials visible to it).  Never waits on other blocks.
+__device__ __forceinline__ bool publish_last(double v, double* partials, uint32_t* ticket) {
+  __shared__ bool last;
+  v = block_sum_d(v);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = v;
+    __threadfence();
+    const uint32_t t = atomicAdd(ticket, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  return last;
+}
+
+// fixed-order sum of the partials, valid in thread 0 of the last block
+__device__ __forceinline__ double gather_partials(const double* partials, int n) {
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += __ldcg(partials + i);
+  return block_sum_d(acc);
+}
+
+__device__ __forceinline__ float dot3(float4 g, float4 u) { return g.x * u.x + g.y * u.y + g.z * u.z; }
+
+// ---------------------------------------------------------------------------
+__global__ void k_jprep(const int32_t* __restrict__ inc_ent, const float* __restrict__ gradC,
+                        const int4* __restrict__ t_i, const float* __restrict__ invm,
+                        const float* __restrict__ alpha, int32_t nt, float4* __restrict__ gV,
+                        float* __restrict__ dinv) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < 4LL * nt; k += stride) {
+    const int32_t e = inc_ent[k];
+    const float* g = gradC + 3LL * e;
+    gV[k] = make_float4(g[0], g[1], g[2], __int_as_float(e >> 2));
+  }
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += stride) {
+    const int4 q = t_i[t];
+    const float* g = gradC + 12 * t;
+    const float w[4] = {invm[q.x], invm[q.y], invm[q.z], invm[q.w]};
+    float d = 0.0f;
+#pragma unroll
+    for (int l = 0; l < 4; ++l)
+      d += w[l] * (g[3 * l] * g[3 * l] + g[3 * l + 1] * g[3 * l + 1] + g[3 * l + 2] * g[3 * l + 2]);
+    d += alpha[t];
+    dinv[t] = fabsf(d) > 1e-30f ? 1.0f / d : 0.0f;
+  }
+}
+
+// vertex phase: u_v = w_v sum x_t g_{t,l}, x_t from Src
+template <int SRC>
+__global__ void __launch_bounds__(kT)
+    k_jv(int32_t nv, const int32_t* __restrict__ inc_ptr, const float4* __restrict__ gV,
+         const float* __restrict__ invm, const float* __restrict__ x, const float* __restrict__ p,
+         const CgState* __restrict__ st, const JState* __restrict__ js, float4* __restrict__ u,
+         float scale_unused) {
+  if (st && st->done) return;
+  float beta = 0.0f, scl = 1.0f;
+  if (SRC == kSrcZbP) beta = (float)st->beta;
+  if (SRC == kSrcScaled) scl = (float)js->theta;  // holds 1/|v| during the power steps
+  const int lane = threadIdx.x % kVG;
+  constexpr int kPerWarp = 32 / kVG;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t stride = ((int64_t)gridDim.x * blockDim.x >> 5) * kPerWarp;
+  for (int64_t base = warp * kPerWarp; base < nv; base += stride) {
+    const int64_t v = base + (threadIdx.x & 31) / kVG;
+    const bool valid = v < nv;
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    const float w = valid ? invm[v] : 0.0f;
+    if (valid && w != 0.0f) {
+      const int32_t k0 = inc_ptr[v], k1 = inc_ptr[v + 1];
+      for (int32_t k = k0 + lane; k < k1; k += kVG) {
+        const float4 e = __ldg(gV + k);
+        const int32_t t = __float_as_int(e.w);
+        float xt;
+        if (SRC == kSrcZbP) xt = x[t] + beta * p[t];
+        else if (SRC == kSrcScaled) xt = x[t] * scl;
+        else xt = x[t];
+        ax += xt * e.x;
+        ay += xt * e.y;
+        az += xt * e.z;
+      }
+    }
+#pragma unroll
+    for (int o = kVG / 2; o > 0; o >>= 1) {
+      ax += __shfl_xor_sync(0xffffffffu, ax, o, kVG);
+      ay += __shfl_xor_sync(0xffffffffu, ay, o, kVG);
+      az += __shfl_xor_sync(0xffffffffu, az, o, kVG);
+    }
+    if (valid && lane == 0) u[v] = make_float4(w * ax, w * ay, w * az, 0.0f);
+  }
+}
+
+struct TArgs {
+  const int4* t_i;
+  const float4* gradC;
+  const float4* u;
+  const float* alpha;
+  const float* dinv;
+  int32_t nt;
+};
+
+__device__ __forceinline__ float jt_core(const TArgs& a, int64_t t) {
+  const int4 q = a.t_i[t];
+  const float4 g0 = __ldg(a.gradC + 3 * t), g1 = __ldg(a.gradC + 3 * t + 1),
+               g2 = __ldg(a.gradC + 3 * t + 2);
+  const float4 u0 = a.u[q.x], u1 = a.u[q.y], u2 = a.u[q.z], u3 = a.u[q.w];
+  // g_{t,0} = (g0.x, g0.y, g0.z), g_{t,1} = (g0.w, g1.x, g1.y), ...
+  return (g0.x * u0.x + g0.y * u0.y + g0.z * u0.z) + (g0.w * u1.x + g1.x * u1.y + g1.y * u1.z) +
+         (g1.z * u2.x + g1.w * u2.y + g2.x * u2.z) + (g2.y * u3.x + g2.z * u3.y + g2.w * u3.z);
+}
+
+// y = A x (tests)
+__global__ void k_jt_plain(TArgs a, const float* __restrict__ x, float* __restrict__ y) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < a.nt;
+       t += (int64_t)gridDim.x * blockDim.x)
+    y[t] = jt_core(a, t) + a.alpha[t] * x[t];
+}
+
+// p = z + beta p; Ap; p.Ap -> alpha (last block)
+__global__ void __launch_bounds__(kT)
+    k_jt_ap(TArgs a, const float* __restrict__ z, float* __restrict__ p, float* __restrict__ ap,
+            double* __restrict__ partials, CgState* st, JState* js) {
+  if (st->done) return;
+  const float beta = (float)st->beta;
+  double acc = 0.0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < a.nt;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const float pt = z[t] + beta * p[t];
+    const float y = jt_core(a, t) + a.alpha[t] * pt;
+    p[t] = pt;
+    ap[t] = y;
+    acc += (double)pt * (double)y;
+  }
+  if (publish_last(acc, partials, &js->ticket[0])) {
+    const double pap = gather_partials(partials, gridDim.x);
+    if (threadIdx.x == 0) {
+      js->ticket[0] = 0;
+      st->pap = pap;
+      if (!isfinite(pap)) st->status |= MGPBD_STATUS_NAN;
+      if (!(fabs(pap) >= 1e-30) || !isfinite(pap)) {
+        st->done = 1;
+      } else {
+        if (pap <= 0.0) st->status |= MGPBD_STATUS_PAP_NONPOS;
+        st->alpha = st->rz / pap;
+      }
+    }
+  }
+}
+
+// x += alpha p ; r -= alpha Ap ; first Chebyshev step z = d = D^-1 r / theta
+__global__ void __launch_bounds__(kT)
+    k_ju(int32_t nt, const float* __restrict__ p, const float* __restrict__ ap,
+         const float* __restrict__ dinv, double* __restrict__ xd, double* __restrict__ r,
+         float* __restrict__ z, float* __restrict__ d, double* __restrict__ partials,
+         CgState* st, JState* js) {
+  if (st->done) return;
+  const double al = st->alpha;
+  const float it = js->inv_theta;
+  const bool jac = js->degree == 1;
+  double rr = 0.0, rz = 0.0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    xd[t] += al * (double)p[t];
+    const double rt = r[t] - al * (double)ap[t];
+    r[t] = rt;
+    const float zt = dinv[t] * (float)rt * it;
+    z[t] = zt;
+    d[t] = zt;
+    rr += rt * rt;
+    rz += rt * (double)zt;
+  }
+  // two reductions: r.r (partials[0..G)) and, for degree 1, r.z ([G..2G))
+  double* p2 = partials + gridDim.x;
+  {
+    double v2 = block_sum_d(rz);
+    if (threadIdx.x == 0) p2[blockIdx.x] = v2;
+  }
+  if (publish_last(rr, partials, &js->ticket[1])) {
+    const double rrs = gather_partials(partials, gridDim.x);
+    const double rzs = jac ? gather_partials(p2, gridDim.x) : 0.0;
+    if (threadIdx.x == 0) {
+      js->ticket[1] = 0;
+      st->rr = rrs;
+      if (!isfinite(rrs)) {
+        st->status |= MGPBD_STATUS_NAN;
+        st->done = 1;
+      } else if (rrs < st->tol2) {
+        st->iters += 1;
+        st->done = 1;
+      } else if (jac) {
+        st->rz_new = rzs;
+        if (fabs(st->rz) < 1e-30) {
+          st->iters += 1;
+          st->done = 1;
+        } else {
+          st->beta = rzs / st->rz;
+          st->rz = rzs;
+          st->iters += 1;
+          if (st->iters >= st->maxiter) {
+            st->done = 1;
+            st->status |= MGPBD_STATUS_CG_MAXITER;
+          }
+        }
+      }
+    }
+  }
+}
+
+// Chebyshev step i >= 1: rr = D^-1 (r - A z); d = c1 d + c2 rr; z += d.
+// The last step also reduces r.z: init -> rz; loop -> beta, iteration count.
+template <bool LAST, bool INIT>
+__global__ void __launch_bounds__(kT)
+    k_jt_cheb(TArgs a, int step, const double* __restrict__ r, float* __restrict__ z,
+              float* __restrict__ d, double* __restrict__ partials, CgState* st, JState* js) {
+  if (st->done) return;
+  const float c1 = js->c1[step], c2 = js->c2[step];
+  double acc = 0.0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < a.nt;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const float zt = z[t];
+    const float y = jt_core(a, t) + a.alpha[t] * zt;
+    const float rt = (float)r[t];
+    const float rrv = a.dinv[t] * (rt - y);
+    const float dt = c1 * d[t] + c2 * rrv;
+    d[t] = dt;
+    const float zn = zt + dt;
+    z[t] = zn;
+    if (LAST) acc += r[t] * (double)zn;
+  }
+  if (!LAST) return;
+  if (publish_last(acc, partials, &js->ticket[2])) {
+    const double rz = gather_partials(partials, gridDim.x);
+    if (threadIdx.x == 0) {
+      js->ticket[2] = 0;
+      if (INIT) {
+        st->rz = rz;
+        if (!isfinite(rz)) {
+          st->status |= MGPBD_STATUS_NAN;
+          st->done = 1;
+        }
+      } else {
+        st->rz_new = rz;
+        if (fabs(st->rz) < 1e-30) {
+          st->iters += 1;
+          st->done = 1;
+        } else {
+          st->beta = rz / st->rz;
+          st->rz = rz;
+          st->iters += 1;
+          if (st->iters >= st->maxiter) {
+            st->done = 1;
+            st->status |= MGPBD_STATUS_CG_MAXITER;
+          }
+        }
+      }
+    }
+  }
+}
+
+// CG init: x = 0, r = b, p = 0, z = d = D^-1 b / theta; b.b -> tolerance
+__global__ void __launch_bounds__(kT)
+    k_ju0(int32_t nt, const float* __restrict__ b, const float* __restrict__ dinv,
+          double* __restrict__ xd, double* __restrict__ r, float* __restrict__ z,
+          float* __restrict__ d, float* __restrict__ p, double* __restrict__ partials,
+          CgState* st, JState* js, double tol_abs, double tol_rel, int maxiter) {
+  const float it = js->inv_theta;
+  const bool jac = js->degree == 1;
+  double bb = 0.0, rz = 0.0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const float bt = b[t];
+    xd[t] = 0.0;
+    r[t] = bt;
+    p[t] = 0.0f;
+    const float zt = dinv[t] * bt * it;
+    z[t] = zt;
+    d[t] = zt;
+    bb += (double)bt * bt;
+    rz += (double)bt * zt;
+  }
+  double* p2 = partials + gridDim.x;
+  {
+    double v2 = block_sum_d(rz);
+    if (threadIdx.x == 0) p2[blockIdx.x] = v2;
+  }
+  if (publish_last(bb, partials, &js->ticket[3])) {
+    const double bbs = gather_partials(partials, gridDim.x);
+    const double rzs = gather_partials(p2, gridDim.x);
+    if (threadIdx.x == 0) {
+      js->ticket[3] = 0;
+      st->rr0 = bbs;
+      const double t2 = tol_abs * tol_abs, r2 = tol_rel * tol_rel * bbs;
+      st->tol2 = r2 > t2 ? r2 : t2;
+      st->iters = 0;
+      st->maxiter = maxiter;
+      st->done = maxiter <= 0;
+      st->status = isfinite(bbs) ? 0 : MGPBD_STATUS_NAN;
+      st->beta = 0.0;
+      st->alpha = st->pap = st->rr = st->rz_new = 0.0;
+      st->body_runs = 0;
+      st->rz = jac ? rzs : 0.0;
+    }
+  }
+}
+
+__global__ void k_jfinish(const double* __restrict__ xd, float* __restrict__ x, int32_t nt) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt;
+       t += (int64_t)gridDim.x * blockDim.x)
+    x[t] = (float)xd[t];
+}
+
+// power iteration step on D^-1 A: w = D^-1 A (v * s), |w|^2 -> s = 1/|w|
+__global__ void __launch_bounds__(kT)
+    k_jt_pow(TArgs a, const float* __restrict__ v, float* __restrict__ w,
+             double* __restrict__ partials, JState* js) {
+  const float s = (float)js->theta;
+  double acc = 0.0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < a.nt;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const float y = a.dinv[t] * (jt_core(a, t) + a.alpha[t] * v[t] * s);
+    w[t] = y;
+    acc += (double)y * y;
+  }
+  if (publish_last(acc, partials, &js->ticket[0])) {
+    const double n2 = gather_partials(partials, gridDim.x);
+    if (threadIdx.x == 0) {
+      js->ticket[0] = 0;
+      const double nrm = sqrt(n2);
+      js->lmax = nrm;  // |D^-1 A v| for |v| = 1
+      js->theta = nrm > 0.0 && isfinite(nrm) ? 1.0 / nrm : 1.0;
+    }
+  }
+}
+
+// |v| of the starting vector -> theta slot holds 1/|v|
+__global__ void k_jnorm(const float* __restrict__ v, int32_t nt, double* __restrict__ partials,
+                        JState* js) {
+  double acc = 0.0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt;
+       t += (int64_t)gridDim.x * blockDim.x)
+    acc += (double)v[t] * v[t];
+  if (publish_last(acc, partials, &js->ticket[0])) {
+    const double n2 = gather_partials(partials, gridDim.x);
+    if (threadIdx.x == 0) {
+      js->ticket[0] = 0;
+      js->theta = n2 > 0.0 ? 1.0 / sqrt(n2) : 1.0;
+    }
+  }
+}
+
+__global__ void k_jcoef(JState* js, int degree, float lo_ratio) {
+  if (threadIdx.x != 0) return;
+  double hi = js->lmax * 1.05;
+  if (!(hi > 0.0) || !isfinite(hi)) hi = 2.0;
+  const double lo = hi * lo_ratio;
+  const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
+  double rho = 1.0 / sigma;
+  js->c1[0] = 0.0f;
+  js->c2[0] = 0.0f;
+  for (int i = 1; i < degree && i < kMaxCheb; ++i) {
+    const double rn = 1.0 / (2.0 * sigma - rho);
+    js->c1[i] = (float)(rn * rho);
+    js->c2[i] = (float)(2.0 * rn / delta);
+    rho = rn;
+  }
+  js->theta = theta;
+  js->inv_theta = (float)(1.0 / theta);
+  js->degree = degree;
+}
+
+__global__ void k_seed(float* v, int32_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t h = static_cast<uint32_t>(i) * 2654435761u;
+    h ^= h >> 15;
+    v[i] = 0.5f + (h & 0xffff) * (1.0f / 65536.0f);
+  }
+}
+
+// tet-phase grids: up to 8 blocks of 256 per SM
+inline int tgrid(int64_t n) {
+  int64_t g = (n + kT - 1) / kT;
+  return static_cast<int>(g < 1 ? 1 : (g > kMaxReduceBlocks ? kMaxReduceBlocks : g));
+}
+
+inline int vgrid(int32_t nv) {
+  int64_t g = (static_cast<int64_t>(nv) * kVG + kT - 1) / kT;
+  return static_cast<int>(g < 1 ? 1 : (g > kMaxReduceBlocks ? kMaxReduceBlocks : g));
+}
+
+TArgs targs(const JView& j) {
+  TArgs a;
+  a.t_i = reinterpret_cast<const int4*>(j.t_i);
+  a.gradC = reinterpret_cast<const float4*>(j.gradC);
+  a.u = j.u;
+  a.alpha = j.alpha;
+  a.dinv = j.dinv;
+  a.nt = j.nt;
+  return a;
+}
+
+}  // namespace
+
+void launch_jform_prepare(const JView& j, const int32_t* inc_ent, float4* gV, float* dinv,
+                          cudaStream_t s) {
+  int g = tgrid(4LL * j.nt);
+  k_jprep<<<g, kT, 0, s>>>(inc_ent, j.gradC, reinterpret_cast<const int4*>(j.t_i), j.invm, j.alpha,
+                           j.nt, gV, dinv);
+  MGPBD_CHECK_LAUNCH();
+}
+
+void launch_jform_apply(const JView& j, const float* x, float* y, cudaStream_t s) {
+  k_jv<kSrcX><<<vgrid(j.nv), kT, 0, s>>>(j.nv, j.inc_ptr, j.gV, j.invm, x, nullptr, nullptr,
+                                          nullptr, j.u, 0.f);
+  MGPBD_CHECK_LAUNCH();
+  k_jt_plain<<<tgrid(j.nt), kT, 0, s>>>(targs(j), x, y);
+  MGPBD_CHECK_LAUNCH();
+}
+
+void launch_jform_cheb_setup(const JView& j, float* v, float* w, double* partials, JState* js,
+                             CgState* st, int iters, int degree, float lo_ratio, cudaStream_t s) {
+  (void)st;
+  const int G = tgrid(j.nt);
+  k_jnorm<<<G, kT, 0, s>>>(v, j.nt, partials, js);
+  MGPBD_CHECK_LAUNCH();
+  for (int it = 0; it < iters; ++it) {
+    float* src = (it % 2 == 0) ? v : w;
+    float* dst = (it % 2 == 0) ? w : v;
+    k_jv<kSrcScaled><<<vgrid(j.nv), kT, 0, s>>>(j.nv, j.inc_ptr, j.gV, j.invm, src, nullptr, nullptr,
+                                                js, j.u, 0.f);
+    MGPBD_CHECK_LAUNCH();
+    k_jt_pow<<<G, kT, 0, s>>>(targs(j), src, dst, partials, js);
+    MGPBD_CHECK_LAUNCH();
+  }
+  k_jcoef<<<1, 32, 0, s>>>(js, degree, lo_ratio);
+  MGPBD_CHECK_LAUNCH();
+}
+
+void launch_jcg_init(const JView& j, const JVecs& v, JState* js, CgState* st, double tol_abs,
+                     double tol_rel, int maxiter, cudaStream_t s) {
+  const int G = tgrid(j.nt);
+  k_ju0<<<G, kT, 0, s>>>(j.nt, v.b, j.dinv, v.xd, v.r, v.z, v.d, v.p, v.partials, st, js, tol_abs,
+                         tol_rel, maxiter);
+  MGPBD_CHECK_LAUNCH();
+  // remaining Chebyshev steps of z = M^-1 r (degree read on the host side
+  // from the same value given to launch_jform_cheb_setup)
+}
+
+void launch_jcg_cheb_steps(const JView& j, const JVecs& v, JState* js, CgState* st, int degree,
+                           bool init, cudaStream_t s) {
+  const int G = tgrid(j.nt);
+  for (int i = 1; i < degree; ++i) {
+    k_jv<kSrcX><<<vgrid(j.nv), kT, 0, s>>>(j.nv, j.inc_ptr, j.gV, j.invm, v.z, nullptr, st, js, j.u,
+                                            0.f);
+    MGPBD_CHECK_LAUNCH();
+    const bool last = i == degree - 1;
+    if (last && init)
+      k_jt_cheb<true, true><<<G, kT, 0, s>>>(targs(j), i, v.r, v.z, v.d, v.partials, st, js);
+    else if (last)
+      k_jt_cheb<true, false><<<G, kT, 0, s>>>(targs(j), i, v.r, v.z, v.d, v.partials, st, js);
+    else
+      k_jt_cheb<false, false><<<G, kT, 0, s>>>(targs(j), i, v.r, v.z, v.d, v.partials, st, js);
+    MGPBD_CHECK_LAUNCH();
+  }
+}
+
+void launch_jcg_body(const JView& j, const JVecs& v, JState* js, CgState* st, int degree,
+                     cudaStream_t s) {
+  const int G = tgrid(j.nt);
+  k_jv<kSrcZbP><<<vgrid(j.nv), kT, 0, s>>>(j.nv, j.inc_ptr, j.gV, j.invm, v.z, v.p, st, js, j.u, 0.f);
+  MGPBD_CHECK_LAUNCH();
+  k_jt_ap<<<G, kT, 0, s>>>(targs(j), v.z, v.p, v.ap, v.partials, st, js);
+  MGPBD_CHECK_LAUNCH();
+  k_ju<<<G, kT, 0, s>>>(j.nt, v.p, v.ap, j.dinv, v.xd, v.r, v.z, v.d, v.partials, st, js);
+  MGPBD_CHECK_LAUNCH();
+  launch_jcg_cheb_steps(j, v, js, st, degree, false, s);
+}
+
+void launch_jcg_finish(const JVecs& v, int32_t nt, const CgState* st, cudaStream_t s) {
+  (void)st;
+  k_jfinish<<<tgrid(nt), kT, 0, s>>>(v.xd, v.x, nt);
+  MGPBD_CHECK_LAUNCH();
+}
+
+void launch_seed(float* v, int32_t n, cudaStream_t s) {
+  k_seed<<<tgrid(n), kT, 0, s>>>(v, n);
+  MGPBD_CHECK_LAUNCH();
+}
+
+}  // namespace mgpbd

@@ -1,0 +1,88 @@
+// Matrix-free application of the MGPBD system matrix A = J W J^T + alpha~
+// (the matrix _fill_A_kernel assembles, cons/mgpbd_gpu.py:273-309) and the
+// Chebyshev-preconditioned CG built on it (FAST mode).
+//
+//   A x = J W J^T x + alpha~ x
+//   vertex phase:  u_v = w_v * sum_{(t,l): t_i[4t+l] = v} x_t g_{t,l}
+//   tet phase:     (A x)_t = sum_l g_{t,l} . u_{t_i[4t+l]} + alpha~_t x_t
+//
+// Per application this streams the gradients twice (tet-major gradC and a
+// vertex-major copy gV with the tet id in .w, 48 + 64 B per tet) instead of
+// the 8 B per nonzero of the CSR matrix (~81 nonzeros per row): ~45 MB
+// instead of ~214 MB at 320k tets, small enough to stay in the 129 MB L2
+// across the thousands of applications of one solve.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kernels.cuh"
+
+namespace mgpbd {
+
+constexpr int kMaxCheb = 32;
+
+// Device scalars of the Chebyshev-preconditioned CG; lives next to CgState.
+struct JState {
+  double theta;           // (lmax + lmin) / 2 of D^-1 A
+  double lmax;            // power-iteration estimate of lambda_max(D^-1 A)
+  float c1[kMaxCheb];     // rho_i * rho_{i-1}
+  float c2[kMaxCheb];     // 2 rho_i / delta
+  float inv_theta;
+  int32_t degree;
+  uint32_t ticket[4];     // last-block counters of the fused reductions
+};
+
+struct JView {
+  int32_t nt = 0, nv = 0;
+  const int32_t* t_i = nullptr;      // (nt, 4)
+  const float* gradC = nullptr;      // (nt, 4, 3)
+  const float4* gV = nullptr;        // (4 nt) vertex-major (g, tet id)
+  const int32_t* inc_ptr = nullptr;  // (nv + 1)
+  const float* invm = nullptr;       // (nv)
+  const float* alpha = nullptr;      // (nt)
+  const float* dinv = nullptr;       // (nt) 1 / diag(A)
+  float4* u = nullptr;               // (nv) vertex scratch
+};
+
+// gV[k] = (gradC[inc_ent[k]], tet id) and 1/diag(A) per tet
+void launch_jform_prepare(const JView& j, const int32_t* inc_ent, float4* gV, float* dinv,
+                          cudaStream_t s);
+// y = A x (plain), for tests and the power iteration
+void launch_jform_apply(const JView& j, const float* x, float* y, cudaStream_t s);
+// lambda_max(D^-1 A) by `iters` power steps on the persistent vector v (nt)
+// and the Chebyshev coefficients for `degree` on [lmax * lo_ratio, lmax]
+void launch_jform_cheb_setup(const JView& j, float* v, float* w, double* partials,
+                             JState* js, CgState* st, int iters, int degree, float lo_ratio,
+                             cudaStream_t s);
+
+// CG with the degree-k Chebyshev preconditioner (k >= 1; k = 1 is scaled
+// Jacobi), scalars on the device.  init: x = 0, r = b, z = M^-1 r, p = z.
+struct JVecs {
+  const float* b = nullptr;
+  float* x = nullptr;
+  double* xd = nullptr;  // float64 copy of x (accumulated)
+  double* r = nullptr;   // float64 residual
+  float* z = nullptr;
+  float* d = nullptr;
+  float* p = nullptr;
+  float* ap = nullptr;
+  double* partials = nullptr;
+};
+void launch_jcg_init(const JView& j, const JVecs& v, JState* js, CgState* st, double tol_abs,
+                     double tol_rel, int maxiter, cudaStream_t s);
+// Chebyshev steps 1..degree-1 of z = M^-1 r (the last one reduces r.z:
+// init -> rz, otherwise beta and the iteration count)
+void launch_jcg_cheb_steps(const JView& j, const JVecs& v, JState* js, CgState* st, int degree,
+                           bool init, cudaStream_t s);
+// one CG iteration: p = z + beta p, Ap, alpha, x/r update and convergence
+// test, z = M^-1 r, beta (all kernels are no-ops once st->done)
+void launch_jcg_body(const JView& j, const JVecs& v, JState* js, CgState* st, int degree,
+                     cudaStream_t s);
+// deterministic start vector of the power iteration
+void launch_seed(float* v, int32_t n, cudaStream_t s);
+// x (float32 output) = xd
+void launch_jcg_finish(const JVecs& v, int32_t nt, const CgState* st, cudaStream_t s);
+
+}  // namespace mgpbd

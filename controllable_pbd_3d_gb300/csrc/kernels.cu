@@ -424,11 +424,97 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// Vectorised variant for the library's own (padded) CSR arrays: each of the
+// G lanes of a row loads U float4 values and U int4 column ids per pass from
+// the 16-byte aligned window that starts at indptr[row] rounded down to a
+// multiple of 4, and masks the elements outside [indptr[row], indptr[row+1]).
+// The arrays carry >= 4 padding elements, so the last window stays inside
+// the allocation.  All U loads of a pass are issued before the first use,
+// which keeps 2*U*16 bytes per lane in flight.
+template <int G, int U, int OP>
+__global__ void __launch_bounds__(kThreads)
+    k_csr_rows_vec(int32_t n, const int32_t* __restrict__ indptr,
+                   const int32_t* __restrict__ indices, const float* __restrict__ data,
+                   const float* __restrict__ x, const float* __restrict__ b,
+                   const float* __restrict__ dinv, float* __restrict__ y, float w,
+                   const float* __restrict__ wp, double* __restrict__ partials,
+                   const CgState* __restrict__ st) {
+  if (st && st->done) return;
+  if (wp) w = *wp;
+  const int lane = threadIdx.x % G;
+  constexpr int kRowsPerWarp = 32 / G;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t stride = ((int64_t)gridDim.x * blockDim.x >> 5) * kRowsPerWarp;
+  double dacc = 0.0;
+  for (int64_t base = warp * kRowsPerWarp; base < n; base += stride) {
+    const int64_t row = base + (threadIdx.x & 31) / G;
+    const bool valid = row < n;
+    float sum = 0.0f;
+    if (valid) {
+      const int32_t k0 = indptr[row], k1 = indptr[row + 1];
+      for (int32_t kb = k0 & ~3; kb < k1; kb += 4 * G * U) {
+        float4 dv[U];
+        int4 iv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int32_t kk = kb + 4 * (lane + G * u);
+          if (kk < k1) {
+            dv[u] = __ldg(reinterpret_cast<const float4*>(data + kk));
+            iv[u] = __ldg(reinterpret_cast<const int4*>(indices + kk));
+          } else {
+            dv[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+            iv[u] = make_int4(0, 0, 0, 0);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int32_t kk = kb + 4 * (lane + G * u);
+          if (kk + 0 >= k0 && kk + 0 < k1) sum += dv[u].x * __ldg(x + iv[u].x);
+          if (kk + 1 >= k0 && kk + 1 < k1) sum += dv[u].y * __ldg(x + iv[u].y);
+          if (kk + 2 >= k0 && kk + 2 < k1) sum += dv[u].z * __ldg(x + iv[u].z);
+          if (kk + 3 >= k0 && kk + 3 < k1) sum += dv[u].w * __ldg(x + iv[u].w);
+        }
+      }
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, G);
+    if (valid && lane == 0) {
+      if (OP == kSpmv) {
+        y[row] = sum;
+      } else if (OP == kSpmvDot) {
+        y[row] = sum;
+        dacc += (double)x[row] * (double)sum;
+      } else if (OP == kResidual) {
+        y[row] = b[row] - sum;
+      } else {
+        y[row] = x[row] + w * dinv[row] * (b[row] - sum);
+      }
+    }
+  }
+  if (OP == kSpmvDot) {
+    dacc = block_sum(dacc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = dacc;
+  }
+}
+
 template <int OP>
 void rows_dispatch(const CsrView& a, const float* x, const float* b, float* y, float w,
                    double* partials, const CgState* st, cudaStream_t s, const float* wp = nullptr) {
   if (a.n <= 0) return;
   double avg = a.n ? (double)a.nnz / a.n : 0.0;
+  if (a.padded && OP != kJacobiZero) {
+    // one pass of G lanes x U float4 covers 4*G*U elements of a row
+    int G = avg >= 40 ? 8 : 4;
+    int grid = OP == kSpmvDot ? reduce_blocks(a.n) : grid_for(a.n, kThreads / G);
+    if (G == 8)
+      k_csr_rows_vec<8, 4, OP><<<grid, kThreads, 0, s>>>(a.n, a.indptr, a.indices, a.data, x, b,
+                                                          a.diag_inv, y, w, wp, partials, st);
+    else
+      k_csr_rows_vec<4, 4, OP><<<grid, kThreads, 0, s>>>(a.n, a.indptr, a.indices, a.data, x, b,
+                                                          a.diag_inv, y, w, wp, partials, st);
+    MGPBD_CHECK_LAUNCH();
+    return;
+  }
   int G = avg >= 48 ? 32 : (avg >= 20 ? 16 : (avg >= 8 ? 8 : 4));
   if (OP == kJacobiZero) G = 1;
   int rows_per_block = kThreads / G;

@@ -65,7 +65,12 @@ struct CsrView {
   const int32_t* indices = nullptr;
   const float* data = nullptr;
   const float* diag_inv = nullptr;
+  // indices/data are 16-byte aligned and padded by >= 4 elements, so the
+  // vectorised row kernel may be used
+  bool padded = false;
 };
+// padding (elements) the library allocates after every CSR value/index array
+constexpr int64_t kCsrPad = 8;
 // y = A x
 void launch_spmv(const CsrView& a, const float* x, float* y, cudaStream_t s);
 // y = A x and partials of x.y (float64)  -- for CG's p.Ap

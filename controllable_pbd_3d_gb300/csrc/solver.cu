@@ -20,6 +20,21 @@ void upload(DevBuf<T>& d, const std::vector<T>& h, cudaStream_t s) {
     MGPBD_CUDA(cudaMemcpyAsync(d.p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, s));
 }
 
+// CSR value/index arrays get kCsrPad zeroed elements after the last entry so
+// the vectorised row kernel's last 16-byte window stays inside the buffer.
+template <class T>
+void alloc_padded(DevBuf<T>& d, int64_t n, cudaStream_t s) {
+  d.alloc(n + kCsrPad);
+  MGPBD_CUDA(cudaMemsetAsync(d.p, 0, sizeof(T) * (n + kCsrPad), s));
+}
+
+template <class T>
+void upload_padded(DevBuf<T>& d, const std::vector<T>& h, cudaStream_t s) {
+  alloc_padded(d, static_cast<int64_t>(h.size()), s);
+  if (!h.empty())
+    MGPBD_CUDA(cudaMemcpyAsync(d.p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, s));
+}
+
 // Power-iteration estimate of lambda_max(D^-1 A); the weight written to
 // *omega is min(omega_cap, 4 / (3 * 1.1 * lambda)).
 __global__ void k_pw_init(float* v, int32_t n) {
@@ -91,12 +106,22 @@ Solver::Solver(const mgpbd_params& p) : p_(p) {
   require(p.n_smooth >= 0 && p.maxiter >= 0 && p.maxiter_cg >= 0, MGPBD_EINVAL,
           "iteration counts must be non-negative");
   require(p.mode == MGPBD_MODE_PARITY || p.mode == MGPBD_MODE_FAST, MGPBD_EINVAL, "unknown mode");
+  require(p.precond == MGPBD_PRECOND_VCYCLE || p.precond == MGPBD_PRECOND_CHEB, MGPBD_EINVAL,
+          "unknown preconditioner");
+  if (p.precond == MGPBD_PRECOND_CHEB) {
+    require(p.mode == MGPBD_MODE_FAST, MGPBD_EINVAL, "the Chebyshev preconditioner needs FAST mode");
+    require(p.cheb_degree >= 1 && p.cheb_degree < kMaxCheb, MGPBD_EINVAL,
+            "cheb_degree must be in [1, 31]");
+    require(p.cheb_lo > 0.0f && p.cheb_lo < 1.0f, MGPBD_EINVAL, "cheb_lo must be in (0, 1)");
+    require(!p.cg_alias, MGPBD_EINVAL, "cg_alias applies to the V-cycle preconditioner only");
+  }
   // no CUDA call here: a handle can be created (and its host-side
   // validation exercised) on a machine without a GPU
 }
 
 Solver::~Solver() {
   if (cg_exec_) cudaGraphExecDestroy(cg_exec_);
+  if (jcg_exec_) cudaGraphExecDestroy(jcg_exec_);
   if (h_buf_) cudaFreeHost(h_buf_);
   if (h_state_) cudaFreeHost(h_state_);
 }
@@ -121,6 +146,10 @@ void Solver::set_mesh(const float* x_ref, const float* invm, const int32_t* t_i,
   if (cg_exec_) {
     cudaGraphExecDestroy(cg_exec_);
     cg_exec_ = nullptr;
+  }
+  if (jcg_exec_) {
+    cudaGraphExecDestroy(jcg_exec_);
+    jcg_exec_ = nullptr;
   }
 }
 
@@ -183,8 +212,8 @@ void Solver::init() {
   L0.n = nt_;
   L0.nnz = L0.host.nnz();
   upload(L0.indptr, L0.host.indptr, s);
-  upload(L0.indices, L0.host.indices, s);
-  L0.data.alloc(L0.nnz);
+  upload_padded(L0.indices, L0.host.indices, s);
+  alloc_padded(L0.data, L0.nnz, s);
   L0.diag_inv.alloc(nt_);
 
   std::vector<int32_t> ip, ie;
@@ -248,11 +277,11 @@ void Solver::build_hierarchy(const std::vector<int32_t>& t_host, const std::vect
     C.n = n_agg;
     C.nnz = g.coarse.nnz();
     upload(C.indptr, g.coarse.indptr, s);
-    upload(C.indices, g.coarse.indices, s);
+    upload_padded(C.indices, g.coarse.indices, s);
     upload(C.diag_pos, g.diag_pos, s);
     upload(C.contrib_off, g.contrib_off, s);
     upload(C.contrib_idx, g.contrib_idx, s);
-    C.data.alloc(C.nnz);
+    alloc_padded(C.data, C.nnz, s);
     C.diag_inv.alloc(C.n);
     C.host = std::move(g.coarse);
     fine_vals.swap(cv);
@@ -281,11 +310,11 @@ void Solver::build_hierarchy(const std::vector<int32_t>& t_host, const std::vect
     C.n = n_agg;
     C.nnz = g.coarse.nnz();
     upload(C.indptr, g.coarse.indptr, s);
-    upload(C.indices, g.coarse.indices, s);
+    upload_padded(C.indices, g.coarse.indices, s);
     upload(C.diag_pos, g.diag_pos, s);
     upload(C.contrib_off, g.contrib_off, s);
     upload(C.contrib_idx, g.contrib_idx, s);
-    C.data.alloc(C.nnz);
+    alloc_padded(C.data, C.nnz, s);
     C.diag_inv.alloc(C.n);
     C.host = std::move(g.coarse);
     ++extra;
@@ -326,6 +355,167 @@ void Solver::alloc_work() {
     chol_.alloc(static_cast<int64_t>(n) * n);
     chol_info_.alloc(1);
   }
+  // matrix-free operator data (used by the Chebyshev path and by
+  // mgpbd_apply_matrix in every mode)
+  gV_.alloc(4LL * nt_);
+  u_.alloc(nv_);
+  jdinv_.alloc(nt_);
+  MGPBD_CUDA(cudaMemsetAsync(u_.p, 0, sizeof(float4) * nv_, s));
+  if (cheb()) {
+    jz_.alloc(nt_);
+    jd_.alloc(nt_);
+    jp_.alloc(nt_);
+    jap_.alloc(nt_);
+    pw_v_.alloc(nt_);
+    pw_w_.alloc(nt_);
+    jxd_.alloc(nt_);
+    jr_.alloc(nt_);
+    jst_.alloc(1);
+    MGPBD_CUDA(cudaMemsetAsync(jst_.p, 0, sizeof(JState), s));
+    launch_seed(pw_v_.p, nt_, s);
+  }
+}
+
+// y = A x on level 0: matrix-free from the current gradients, or the CSR
+// values of the last fill
+void Solver::apply_matrix(int matrix_free, const float* x, float* y) {
+  require_init();
+  if (matrix_free) {
+    JView j = jview();
+    if (matrix_free == 1) launch_jform_prepare(j, inc_ent_.p, gV_.p, jdinv_.p, stream_);
+    launch_jform_apply(j, x, y, stream_);
+  } else {
+    launch_spmv(levels_[0].view(), x, y, stream_);
+  }
+}
+
+// one row-kernel pass over the library's CSR of `level`: op 0 y = A x,
+// op 1 y = x + omega D^-1 (b - A x)
+void Solver::level_sweep(int32_t level, int32_t op, const float* x, const float* b, float* y,
+                         float omega) {
+  require_init();
+  require(level >= 0 && level < n_levels(), MGPBD_EINVAL, "level out of range");
+  require(op == 0 || op == 1, MGPBD_EINVAL, "op must be 0 (spmv) or 1 (jacobi)");
+  CsrView A = levels_[level].view();
+  if (op == 0) launch_spmv(A, x, y, stream_);
+  else launch_jacobi(A, b, x, y, omega, stream_);
+}
+
+JView Solver::jview() {
+  JView j;
+  j.nt = nt_;
+  j.nv = nv_;
+  j.t_i = t_i_;
+  j.gradC = gradC_.p;
+  j.gV = gV_.p;
+  j.inc_ptr = inc_ptr_.p;
+  j.invm = invm_;
+  j.alpha = alpha_.p;
+  j.dinv = jdinv_.p;
+  j.u = u_.p;
+  return j;
+}
+
+JVecs Solver::jvecs(const float* b, float* x) {
+  JVecs v;
+  v.b = b;
+  v.x = x;
+  v.xd = jxd_.p;
+  v.r = jr_.p;
+  v.z = jz_.p;
+  v.d = jd_.p;
+  v.p = jp_.p;
+  v.ap = jap_.p;
+  v.partials = partials_.p;
+  return v;
+}
+
+// Per Newton iteration: vertex-major gradients, 1/diag(A), lambda_max of
+// D^-1 A (six power steps, warm-started from the previous vector) and the
+// Chebyshev coefficients.
+void Solver::jform_setup() {
+  JView j = jview();
+  launch_jform_prepare(j, inc_ent_.p, gV_.p, jdinv_.p, stream_);
+  launch_jform_cheb_setup(j, pw_v_.p, pw_w_.p, partials_.p, jst_.p, cg_state_.p, 6,
+                          p_.cheb_degree, p_.cheb_lo, stream_);
+}
+
+// CG with the Chebyshev preconditioner as one CUDA graph: init, a device-side
+// while loop over iterations (bounded by maxiter_cg on the device), and the
+// float32 copy of the float64 solution.
+int32_t Solver::pcg_cheb(const float* b, float* x) {
+  cudaStream_t outer = stream_;
+  if (!jcg_exec_ || jcg_b_ != b || jcg_x_ != x) {
+    if (jcg_exec_) {
+      cudaGraphExecDestroy(jcg_exec_);
+      jcg_exec_ = nullptr;
+    }
+    cudaStream_t cs, bs;
+    MGPBD_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    MGPBD_CUDA(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking));
+    cudaGraph_t graph = nullptr;
+    try {
+      JView j = jview();
+      JVecs v = jvecs(b, x);
+      long long c0 = g_launches.load();
+      MGPBD_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+      launch_jcg_init(j, v, jst_.p, cg_state_.p, p_.tol_cg, p_.rel_tol_cg, p_.maxiter_cg, cs);
+      launch_jcg_cheb_steps(j, v, jst_.p, cg_state_.p, p_.cheb_degree, true, cs);
+      long long c1 = g_launches.load();
+      cudaStreamCaptureStatus cst;
+      const cudaGraphNode_t* deps = nullptr;
+      size_t ndeps = 0;
+      MGPBD_CUDA(cudaStreamGetCaptureInfo(cs, &cst, nullptr, &graph, &deps, nullptr, &ndeps));
+      cudaGraphConditionalHandle handle;
+      MGPBD_CUDA(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
+      cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+      cp.conditional.handle = handle;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      cudaGraphNode_t cond;
+      MGPBD_CUDA(cudaGraphAddNode(&cond, graph, deps, nullptr, ndeps, &cp));
+      cudaGraph_t body = cp.conditional.phGraph_out[0];
+      MGPBD_CUDA(cudaStreamUpdateCaptureDependencies(cs, &cond, nullptr, 1, cudaStreamSetCaptureDependencies));
+      MGPBD_CUDA(cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+      launch_jcg_body(j, v, jst_.p, cg_state_.p, p_.cheb_degree, bs);
+      k_set_cond<<<1, 1, 0, bs>>>(handle, cg_state_.p);
+      MGPBD_CHECK_LAUNCH();
+      long long c2 = g_launches.load();
+      MGPBD_CUDA(cudaStreamEndCapture(bs, &body));
+      launch_jcg_finish(v, nt_, cg_state_.p, cs);
+      long long c3 = g_launches.load();
+      g_launches.fetch_sub(c3 - c0);
+      jgraph_init_launches_ = (c1 - c0) + (c3 - c2);
+      jgraph_body_launches_ = c2 - c1;
+      MGPBD_CUDA(cudaStreamEndCapture(cs, &graph));
+      MGPBD_CUDA(cudaGraphInstantiate(&jcg_exec_, graph, 0));
+      cudaGraphDestroy(graph);
+    } catch (...) {
+      cudaStreamCaptureStatus cst;
+      if (cudaStreamIsCapturing(bs, &cst) == cudaSuccess && cst != cudaStreamCaptureStatusNone) {
+        cudaGraph_t g2;
+        cudaStreamEndCapture(bs, &g2);
+      }
+      if (cudaStreamIsCapturing(cs, &cst) == cudaSuccess && cst != cudaStreamCaptureStatusNone) {
+        cudaGraph_t g2 = nullptr;
+        cudaStreamEndCapture(cs, &g2);
+        if (g2) cudaGraphDestroy(g2);
+      }
+      cudaGetLastError();
+      cudaStreamDestroy(cs);
+      cudaStreamDestroy(bs);
+      throw;
+    }
+    cudaStreamDestroy(cs);
+    cudaStreamDestroy(bs);
+    jcg_b_ = b;
+    jcg_x_ = x;
+  }
+  MGPBD_CUDA(cudaGraphLaunch(jcg_exec_, outer));
+  sync_read(h_state_, cg_state_.p, sizeof(CgState));
+  g_launches.fetch_add(jgraph_init_launches_ + jgraph_body_launches_ * h_state_->body_runs);
+  status_ |= static_cast<uint32_t>(h_state_->status);
+  return h_state_->iters;
 }
 
 // ---------------------------------------------------------------------------
@@ -354,6 +544,11 @@ void Solver::compute_constraints() {
 // _fill_A_and_update_gpu (cons/mgpbd_gpu.py:320-324)
 void Solver::fill_matrices() {
   require_init();
+  if (cheb()) {
+    // matrix-free: no CSR values; the gradients are the operator
+    jform_setup();
+    return;
+  }
   cudaStream_t s = stream_;
   Level& L0 = levels_[0];
   launch_fill_A(L0.indptr.p, L0.indices.p, t_i_, invm_, gradC_.p, alpha_.p, nt_, L0.data.p,
@@ -468,6 +663,7 @@ void Solver::precondition(const CgState* guard) {
 
 void Solver::vcycle_into(const float* r, float* z) {
   require_init();
+  require(!cheb(), MGPBD_ENOTSUP, "no V-cycle: the solver uses the Chebyshev preconditioner");
   vcycle(0, r, nullptr);
   MGPBD_CUDA(cudaMemcpyAsync(z, levels_[0].xa.p, sizeof(float) * nt_, cudaMemcpyDeviceToDevice,
                              stream_));
@@ -493,6 +689,7 @@ void Solver::cg_body(const float* b, float* x) {
 // GPUMultigridSolver.solve (cons/mgpcg_gpu.py:261-329)
 int32_t Solver::pcg(const float* b, float* x) {
   require_init();
+  if (cheb()) return pcg_cheb(b, x);
   if (p_.mode == MGPBD_MODE_FAST && b == rhs_.p && x == dlam_.p) return pcg_graph(b, x);
   cudaStream_t s = stream_;
   int64_t n = nt_;

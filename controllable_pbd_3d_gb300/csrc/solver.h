@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "common.h"
+#include "jform.cuh"
 #include "kernels.cuh"
 #include "structure.h"
 
@@ -37,6 +38,7 @@ struct Level {
     v.indices = indices.p;
     v.data = data.p;
     v.diag_inv = diag_inv.p;
+    v.padded = true;
     return v;
   }
 };
@@ -65,6 +67,11 @@ class Solver {
   void scatter(const float* dlam);
   double line_search();
   void apply_dpos(double omega);
+  // matrix_free: 0 CSR values, 1 gradients (prepared first), 2 gradients
+  // as prepared by the last call
+  void apply_matrix(int matrix_free, const float* x, float* y);
+  void level_sweep(int32_t level, int32_t op, const float* x, const float* b, float* y,
+                   float omega);
 
   const mgpbd_stats& stats() const { return stats_; }
   // rows of (iteration, residual, cg_iters, omega, host seconds) of the last
@@ -91,6 +98,12 @@ class Solver {
   // z = V-cycle(r) for the CG residual r (level-0 result left in xa)
   void precondition(const CgState* guard);
   int32_t pcg_graph(const float* b, float* x);
+  // FAST mode with the Chebyshev preconditioner (matrix-free A)
+  bool cheb() const { return p_.precond == MGPBD_PRECOND_CHEB; }
+  JView jview();
+  JVecs jvecs(const float* b, float* x);
+  void jform_setup();
+  int32_t pcg_cheb(const float* b, float* x);
   void sync_read(void* host, const void* dev, size_t bytes);
   double finalize_read(const double* partials, int blocks);
 
@@ -124,6 +137,17 @@ class Solver {
   float* cg_graph_x_ = nullptr;
   long long graph_init_launches_ = 0;
   long long graph_body_launches_ = 0;
+
+  // matrix-free (J-form) data of the Chebyshev path
+  DevBuf<float4> gV_, u_;
+  DevBuf<float> jdinv_, jz_, jd_, jp_, jap_, pw_v_, pw_w_;
+  DevBuf<double> jxd_, jr_;
+  DevBuf<JState> jst_;
+  cudaGraphExec_t jcg_exec_ = nullptr;
+  const float* jcg_b_ = nullptr;
+  float* jcg_x_ = nullptr;
+  long long jgraph_init_launches_ = 0;
+  long long jgraph_body_launches_ = 0;
 
   mgpbd_stats stats_{};
   uint32_t status_ = 0;

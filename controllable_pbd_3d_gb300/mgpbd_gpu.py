@@ -82,7 +82,11 @@ class MGPBDSolverGPU:
     max_levels     extra levels by matrix-graph aggregation (0: reference);
     kinematic_pins vertices with invm == 0 skip the prediction;
     cg_alias       reproduce the reference PCG whose V-cycle overwrites the
-                   CG residual (cons/mgpcg_gpu.py:239-240 vs :275).
+                   CG residual (cons/mgpcg_gpu.py:239-240 vs :275);
+    compliance     > 0: alpha~ = compliance / dt^2 for every tet;
+    precond        'vcycle' (reference) or 'cheb' (FAST only: Chebyshev
+                   polynomial of degree cheb_degree on [lmax*cheb_lo, lmax],
+                   matrix-free operator, no CSR assembly).
   """
 
   def __init__(self, v_p, v_p_ref, v_invm, t_i, t_m, gravity, dt, mu=1e6, damp=1.0, maxiter=20,
@@ -91,7 +95,7 @@ class MGPBDSolverGPU:
                aggregation='tet', benchmark=None, *, mode='parity', rel_tol_cg=0.0,
                coarse_solver='jacobi', smoother='jacobi', max_levels=0, max_coarse=400,
                kinematic_pins=False, coarse_sweeps=0, cg_alias=False, compliance=0.0,
-               check_finite=True):
+               precond='vcycle', cheb_degree=8, cheb_lo=0.01, check_finite=True):
     if aggregation != 'tet':
       raise NotImplementedError(
           "aggregation='pyamg' needs PyAMG's smoothed-aggregation setup, which this "
@@ -153,6 +157,9 @@ class MGPBDSolverGPU:
     p.coarse_sweeps = int(coarse_sweeps)
     p.cg_alias = int(bool(cg_alias))
     p.compliance = float(compliance)
+    p.precond = {'vcycle': 0, 'cheb': 1}[precond]
+    p.cheb_degree = int(cheb_degree)
+    p.cheb_lo = float(cheb_lo)
     self.params = p
     h = C.c_void_p()
     N.check(self._lib.mgpbd_create(C.byref(p), C.byref(h)), 'mgpbd_create')
@@ -306,6 +313,26 @@ class MGPBDSolverGPU:
 
   def synchronize(self):
     N.check(self._lib.mgpbd_synchronize(self._h), 'mgpbd_synchronize')
+
+  def apply_A(self, x, matrix_free=True):
+    """y = A x for the current system (matrix-free from the gradients, or
+    with the assembled CSR values)."""
+    self._stream()
+    y = torch.empty_like(x)
+    mode = int(matrix_free) if not isinstance(matrix_free, bool) else int(matrix_free)
+    N.check(self._lib.mgpbd_apply_matrix(self._h, mode, x.data_ptr(), y.data_ptr()),
+            'mgpbd_apply_matrix')
+    return y
+
+  def level_sweep(self, level, op, x, b=None, y=None, omega=2.0 / 3.0):
+    """One pass of the internal CSR row kernel on a multigrid level."""
+    self._stream()
+    if y is None:
+      y = torch.empty_like(x)
+    N.check(self._lib.mgpbd_level_sweep(self._h, int(level), int(op), x.data_ptr(),
+                                        b.data_ptr() if b is not None else None, y.data_ptr(),
+                                        float(omega)), 'mgpbd_level_sweep')
+    return y
 
 
 def _now():

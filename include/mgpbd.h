@@ -99,7 +99,18 @@ typedef struct mgpbd_params {
   /* > 0: alpha~ = compliance / dt^2 for every tet (the XPBD convention of
    * cons/length.py:30) instead of 1 / (mu dt^2 V_t) (cons/mgpbd_gpu.py:151) */
   float compliance;
+  /* CG preconditioner: MGPBD_PRECOND_VCYCLE (the reference's aggregation
+   * V-cycle on CSR matrices) or MGPBD_PRECOND_CHEB (FAST mode only: a
+   * degree-`cheb_degree` Chebyshev polynomial in D^-1 A on the interval
+   * [lambda_max * cheb_lo, lambda_max], with A applied matrix-free from the
+   * constraint gradients; no CSR assembly per Newton iteration) */
+  int32_t precond;
+  int32_t cheb_degree;
+  float cheb_lo;
 } mgpbd_params;
+
+#define MGPBD_PRECOND_VCYCLE 0
+#define MGPBD_PRECOND_CHEB 1
 
 typedef struct mgpbd_stats {
   int32_t newton_iters;     /* Newton iterations run in the last solve        */
@@ -216,6 +227,18 @@ int mgpbd_scatter(mgpbd_handle h, const float* dlam);
 int mgpbd_line_search(mgpbd_handle h, double* omega);
 /* _apply_dpos (cons/mgpbd_gpu.py:345-349) */
 int mgpbd_apply_dpos(mgpbd_handle h, double omega);
+
+/* y = A x for the level-0 system of the last fill (device vectors, nt):
+ * matrix_free = 1 applies J W J^T + alpha~ from the current gradients
+ * (the operator _fill_A_kernel assembles, cons/mgpbd_gpu.py:273-309);
+ * matrix_free = 2 does the same reusing the vertex-major gradients of the
+ * previous call; matrix_free = 0 multiplies by the assembled CSR values. */
+int mgpbd_apply_matrix(mgpbd_handle h, int32_t matrix_free, const float* x, float* y);
+/* One pass of the library's vectorised CSR row kernel on multigrid level
+ * `level`: op 0 y = A x (GPUSparseMatrix.spmv, cons/sparse_gpu.py:123-132),
+ * op 1 y = x + omega D^-1 (b - A x) (jacobi_smooth, :134-144). */
+int mgpbd_level_sweep(mgpbd_handle h, int32_t level, int32_t op, const float* x,
+                      const float* b, float* y, float omega);
 
 /* ---- standalone sparse kernels on caller CSR (device arrays) ------------ */
 /* GPUSparseMatrix.spmv (cons/sparse_gpu.py:123-132): y = A x */

@@ -157,6 +157,99 @@ def test_cube10_against_float64_oracle(cuda, mode):
   assert err <= 1e-5 * float(np.abs(o.x).max()), err
 
 
+@pytest.mark.parametrize('name', NAMES[:2])
+def test_matrix_free_apply_equals_csr(cuda, name):
+  """A x from the gradients (no assembly) equals the assembled CSR product
+  and the reference's own matrix."""
+  z = golden(name)
+  s, _ = make_solver(cuda, z)
+  s.make_prediction()
+  s.lambdaf.zero_()
+  s._compute_C_and_gradC()
+  s._fill_A_and_update_gpu()
+  xv = cuda.tensor(z['it0_spmv_x0'], device='cuda')
+  y_mf = np_(s.apply_A(xv, matrix_free=True))
+  y_csr = np_(s.apply_A(xv, matrix_free=False))
+  assert rel(y_mf, y_csr) < 1e-5
+  assert rel(y_mf, z['it0_spmv_y0']) < 1e-4
+  # the vectorised internal row kernel on both levels
+  for lvl in range(2):
+    x = cuda.tensor(z[f'it0_spmv_x{lvl}'], device='cuda')
+    assert rel(np_(s.level_sweep(lvl, 0, x)), z[f'it0_spmv_y{lvl}']) < 1e-4
+    b = cuda.tensor(z[f'it0_jac_b{lvl}'], device='cuda')
+    y = s.level_sweep(lvl, 1, x, b, omega=s.omega_jacobi)
+    assert rel(np_(y), z[f'it0_jac_y{lvl}']) < 1e-4
+
+
+@pytest.mark.parametrize('degree', [1, 4, 8])
+def test_chebyshev_pcg_solves_the_system(cuda, degree):
+  """The matrix-free Chebyshev-preconditioned CG reaches the requested
+  relative residual of the true system (checked in float64 on the host
+  with the reference-order CSR matrix)."""
+  from controllable_pbd_3d_gb300 import meshgen
+  import scipy.sparse as sp
+  n = 8
+  xr, t = meshgen.hex_grid_tets(n, n, n)
+  x0, _ = meshgen.hex_grid_tets(n, n, n, jitter=0.02, seed=4)
+  invm = np.ones(len(xr), np.float32)
+  invm[meshgen.grid_face_vertices(n, n, n, 1)] = 0
+  from controllable_pbd_3d_gb300.mgpbd_gpu import MGPBDSolverGPU
+  xt = cuda.tensor(x0, device='cuda')
+  s = MGPBDSolverGPU(xt, cuda.tensor(xr, device='cuda'), cuda.tensor(invm, device='cuda'),
+                     cuda.tensor(t, device='cuda'), None, [0, -9.8, 0], 1 / 300, mu=1e5,
+                     mode='fast', precond='cheb', cheb_degree=degree, maxiter_cg=3000,
+                     tol_cg=1e-12, rel_tol_cg=1e-6)
+  s.init()
+  s.make_prediction()
+  s.lambdaf.zero_()
+  s._compute_C_and_gradC()
+  s._residual_norm_gpu()
+  s._fill_A_and_update_gpu()
+  it = s._gpu_solver.solve(s._b_gpu, s._dlam_gpu)
+  assert 0 < it < 3000
+  # true residual with the float32 CSR values in float64 arithmetic
+  g = s._gpu_solver._gpu_As[0]
+  s2 = MGPBDSolverGPU(cuda.tensor(np_(xt), device='cuda'), cuda.tensor(xr, device='cuda'),
+                      cuda.tensor(invm, device='cuda'), cuda.tensor(t, device='cuda'), None,
+                      [0, -9.8, 0], 1 / 300, mu=1e5)
+  s2.init()
+  s2._compute_C_and_gradC()
+  s2._fill_A_and_update_gpu()
+  A = s2._gpu_solver._gpu_As[0].to_scipy().astype(np.float64)
+  b = np_(s._b_gpu).astype(np.float64)
+  xsol = np_(s._dlam_gpu).astype(np.float64)
+  rres = np.linalg.norm(b - A @ xsol) / np.linalg.norm(b)
+  assert rres < 1e-4, rres
+  del g
+
+
+def test_fast_cheb_matches_float64_oracle(cuda):
+  """FAST mode with the matrix-free Chebyshev PCG converges to the same
+  positions as the float64 oracle (both solved tightly)."""
+  from controllable_pbd_3d_gb300 import meshgen
+  from oracle.mgpbd_oracle import MGPBDOracle
+  n = 8
+  xr, t = meshgen.hex_grid_tets(n, n, n)
+  x0, _ = meshgen.hex_grid_tets(n, n, n, jitter=0.02, seed=3)
+  invm = np.ones(len(xr), np.float32)
+  invm[meshgen.grid_face_vertices(n, n, n, 1)] = 0
+  kw = dict(mu=1e5, damp=0.993, maxiter=5, rtol=1e-6, atol=1e-9, maxiter_cg=3000, tol_cg=1e-12,
+            rel_tol_cg=1e-7)
+  o = MGPBDOracle(x0, xr, invm, t, [0, -9.8, 0], 1 / 300, dtype=np.float64, **kw)
+  o.init()
+  from controllable_pbd_3d_gb300.mgpbd_gpu import MGPBDSolverGPU
+  xt = cuda.tensor(x0, device='cuda')
+  s = MGPBDSolverGPU(xt, cuda.tensor(xr, device='cuda'), cuda.tensor(invm, device='cuda'),
+                     cuda.tensor(t, device='cuda'), None, [0, -9.8, 0], 1 / 300, mode='fast',
+                     precond='cheb', **kw)
+  s.init()
+  for k in range(2):
+    o.step(k)
+    s.step(k)
+  err = float(np.abs(np_(xt) - o.x).max())
+  assert err <= 1e-5 * float(np.abs(o.x).max()), err
+
+
 def test_fast_mode_matches_parity_mode(cuda):
   """The captured device-driven CG computes what the host-driven one does."""
   z = golden('step_cube6_mu3e4.npz')
