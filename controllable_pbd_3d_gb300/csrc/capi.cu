@@ -81,6 +81,7 @@ void mgpbd_default_params(mgpbd_params* p) {
   p->precond = MGPBD_PRECOND_VCYCLE;
   p->cheb_degree = 8;
   p->cheb_lo = 0.01f;
+  p->use_graph = 1;
 }
 
 const char* mgpbd_strerror(int code) {

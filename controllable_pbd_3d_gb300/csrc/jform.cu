@@ -15,7 +15,8 @@ namespace {
 constexpr int kT = 256;      // threads per block
 constexpr int kVG = 4;       // lanes per vertex in the vertex phase
 
-enum Src { kSrcX = 0, kSrcZbP = 1, kSrcScaled = 2 };
+// x_t read by the vertex phase: x, z + beta p, or x * sqrt(1/diag) (Lanczos)
+enum Src { kSrcX = 0, kSrcZbP = 1, kSrcSqrtD = 2 };
 enum Epi { kEpiPlain = 0, kEpiAp = 1, kEpiCheb = 2, kEpiPow = 3 };
 
 __device__ __forceinline__ double warp_sum_d(double v) {
@@ -93,9 +94,8 @@ __global__ void __launch_bounds__(kT)
          const CgState* __restrict__ st, const JState* __restrict__ js, float4* __restrict__ u,
          float scale_unused) {
   if (st && st->done) return;
-  float beta = 0.0f, scl = 1.0f;
+  float beta = 0.0f;
   if (SRC == kSrcZbP) beta = (float)st->beta;
-  if (SRC == kSrcScaled) scl = (float)js->theta;  // holds 1/|v| during the power steps
   const int lane = threadIdx.x % kVG;
   constexpr int kPerWarp = 32 / kVG;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(kT)
         const int32_t t = __float_as_int(e.w);
         float xt;
         if (SRC == kSrcZbP) xt = x[t] + beta * p[t];
-        else if (SRC == kSrcScaled) xt = x[t] * scl;
+        else if (SRC == kSrcSqrtD) xt = x[t] * sqrtf(p[t]);
         else xt = x[t];
         ax += xt * e.x;
         ay += xt * e.y;
@@ -194,8 +194,8 @@ __global__ void __launch_bounds__(kT)
          CgState* st, JState* js) {
   if (st->done) return;
   const double al = st->alpha;
-  const float it = js->inv_theta;
-  const bool jac = js->degree == 1;
+  const float it = js->cf.inv_theta;
+  const bool jac = js->cf.degree == 1;
   double rr = 0.0, rz = 0.0;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt;
        t += (int64_t)gridDim.x * blockDim.x) {
@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(kT)
     k_jt_cheb(TArgs a, int step, const double* __restrict__ r, float* __restrict__ z,
               float* __restrict__ d, double* __restrict__ partials, CgState* st, JState* js) {
   if (st->done) return;
-  const float c1 = js->c1[step], c2 = js->c2[step];
+  const float c1 = js->cf.c1[step], c2 = js->cf.c2[step];
   double acc = 0.0;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < a.nt;
        t += (int64_t)gridDim.x * blockDim.x) {
@@ -302,8 +302,8 @@ __global__ void __launch_bounds__(kT)
           double* __restrict__ xd, double* __restrict__ r, float* __restrict__ z,
           float* __restrict__ d, float* __restrict__ p, double* __restrict__ partials,
           CgState* st, JState* js, double tol_abs, double tol_rel, int maxiter) {
-  const float it = js->inv_theta;
-  const bool jac = js->degree == 1;
+  const float it = js->cf.inv_theta;
+  const bool jac = js->cf.degree == 1;
   double bb = 0.0, rz = 0.0;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt;
        t += (int64_t)gridDim.x * blockDim.x) {
@@ -348,63 +348,91 @@ __global__ void k_jfinish(const double* __restrict__ xd, float* __restrict__ x, 
     x[t] = (float)xd[t];
 }
 
-// power iteration step on D^-1 A: w = D^-1 A (v * s), |w|^2 -> s = 1/|w|
+// Lanczos on S = D^-1/2 A D^-1/2 (Golub & Van Loan, sec. 10.1): step j
+// computes w = S q_j - b_{j-1} q_{j-1} and a_j = q_j . w ...
 __global__ void __launch_bounds__(kT)
-    k_jt_pow(TArgs a, const float* __restrict__ v, float* __restrict__ w,
-             double* __restrict__ partials, JState* js) {
-  const float s = (float)js->theta;
+    k_lz_apply(TArgs a, int j, const float* __restrict__ q, const float* __restrict__ qprev,
+               float* __restrict__ w, double* __restrict__ partials, JState* js) {
+  const float bprev = j > 0 ? (float)js->lz_b[j - 1] : 0.0f;
   double acc = 0.0;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < a.nt;
        t += (int64_t)gridDim.x * blockDim.x) {
-    const float y = a.dinv[t] * (jt_core(a, t) + a.alpha[t] * v[t] * s);
+    const float sd = sqrtf(a.dinv[t]);
+    const float y = sd * (jt_core(a, t) + a.alpha[t] * q[t] * sd) - bprev * qprev[t];
+    w[t] = y;
+    acc += (double)q[t] * y;
+  }
+  if (publish_last(acc, partials, &js->ticket[0])) {
+    const double s = gather_partials(partials, gridDim.x);
+    if (threadIdx.x == 0) {
+      js->ticket[0] = 0;
+      js->lz_a[j] = s;
+    }
+  }
+}
+
+// ... then w -= a_j q_j and b_j = |w|
+__global__ void __launch_bounds__(kT)
+    k_lz_orth(int32_t nt, int j, const float* __restrict__ q, float* __restrict__ w,
+              double* __restrict__ partials, JState* js) {
+  const float aj = (float)js->lz_a[j];
+  double acc = 0.0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const float y = w[t] - aj * q[t];
     w[t] = y;
     acc += (double)y * y;
   }
-  if (publish_last(acc, partials, &js->ticket[0])) {
-    const double n2 = gather_partials(partials, gridDim.x);
+  if (publish_last(acc, partials, &js->ticket[1])) {
+    const double s = gather_partials(partials, gridDim.x);
     if (threadIdx.x == 0) {
-      js->ticket[0] = 0;
-      const double nrm = sqrt(n2);
-      js->lmax = nrm;  // |D^-1 A v| for |v| = 1
-      js->theta = nrm > 0.0 && isfinite(nrm) ? 1.0 / nrm : 1.0;
+      js->ticket[1] = 0;
+      js->lz_b[j] = sqrt(s);
     }
   }
 }
 
-// |v| of the starting vector -> theta slot holds 1/|v|
-__global__ void k_jnorm(const float* __restrict__ v, int32_t nt, double* __restrict__ partials,
-                        JState* js) {
+// q_{j+1} = w / b_j, q_j -> qprev
+__global__ void k_lz_next(int32_t nt, int j, float* __restrict__ q, float* __restrict__ qprev,
+                          const float* __restrict__ w, const JState* js) {
+  const double b = js->lz_b[j];
+  const float inv = b > 0.0 ? (float)(1.0 / b) : 0.0f;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    qprev[t] = q[t];
+    q[t] = w[t] * inv;
+  }
+}
+
+// start vector: fixed pseudo-random entries, normalised
+__global__ void __launch_bounds__(kT)
+    k_lz_seed(int32_t nt, float* __restrict__ q, double* __restrict__ partials, JState* js) {
   double acc = 0.0;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt;
-       t += (int64_t)gridDim.x * blockDim.x)
-    acc += (double)v[t] * v[t];
+       t += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t h = static_cast<uint32_t>(t) * 2654435761u;
+    h ^= h >> 15;
+    const float v = 0.5f + (h & 0xffff) * (1.0f / 65536.0f);
+    q[t] = v;
+    acc += (double)v * v;
+  }
   if (publish_last(acc, partials, &js->ticket[0])) {
-    const double n2 = gather_partials(partials, gridDim.x);
+    const double s = gather_partials(partials, gridDim.x);
     if (threadIdx.x == 0) {
       js->ticket[0] = 0;
-      js->theta = n2 > 0.0 ? 1.0 / sqrt(n2) : 1.0;
+      js->scale = s > 0.0 ? 1.0 / sqrt(s) : 1.0;
     }
   }
 }
 
-__global__ void k_jcoef(JState* js, int degree, float lo_ratio) {
-  if (threadIdx.x != 0) return;
-  double hi = js->lmax * 1.05;
-  if (!(hi > 0.0) || !isfinite(hi)) hi = 2.0;
-  const double lo = hi * lo_ratio;
-  const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
-  double rho = 1.0 / sigma;
-  js->c1[0] = 0.0f;
-  js->c2[0] = 0.0f;
-  for (int i = 1; i < degree && i < kMaxCheb; ++i) {
-    const double rn = 1.0 / (2.0 * sigma - rho);
-    js->c1[i] = (float)(rn * rho);
-    js->c2[i] = (float)(2.0 * rn / delta);
-    rho = rn;
+__global__ void k_lz_scale(int32_t nt, float* __restrict__ q, float* __restrict__ qprev,
+                           const JState* js) {
+  const float sc = (float)js->scale;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    q[t] *= sc;
+    qprev[t] = 0.0f;
   }
-  js->theta = theta;
-  js->inv_theta = (float)(1.0 / theta);
-  js->degree = degree;
 }
 
 __global__ void k_seed(float* v, int32_t n) {
@@ -456,23 +484,81 @@ void launch_jform_apply(const JView& j, const float* x, float* y, cudaStream_t s
   MGPBD_CHECK_LAUNCH();
 }
 
-void launch_jform_cheb_setup(const JView& j, float* v, float* w, double* partials, JState* js,
-                             CgState* st, int iters, int degree, float lo_ratio, cudaStream_t s) {
-  (void)st;
+void launch_jform_lanczos(const JView& j, float* q, float* qprev, float* w, double* partials,
+                          JState* js, int steps, cudaStream_t s) {
+  require(steps >= 1 && steps <= kMaxLanczos, MGPBD_EINVAL, "Lanczos steps out of range");
   const int G = tgrid(j.nt);
-  k_jnorm<<<G, kT, 0, s>>>(v, j.nt, partials, js);
+  k_lz_seed<<<G, kT, 0, s>>>(j.nt, q, partials, js);
   MGPBD_CHECK_LAUNCH();
-  for (int it = 0; it < iters; ++it) {
-    float* src = (it % 2 == 0) ? v : w;
-    float* dst = (it % 2 == 0) ? w : v;
-    k_jv<kSrcScaled><<<vgrid(j.nv), kT, 0, s>>>(j.nv, j.inc_ptr, j.gV, j.invm, src, nullptr, nullptr,
-                                                js, j.u, 0.f);
+  k_lz_scale<<<G, kT, 0, s>>>(j.nt, q, qprev, js);
+  MGPBD_CHECK_LAUNCH();
+  for (int it = 0; it < steps; ++it) {
+    k_jv<kSrcSqrtD><<<vgrid(j.nv), kT, 0, s>>>(j.nv, j.inc_ptr, j.gV, j.invm, q, j.dinv, nullptr,
+                                               js, j.u, 0.f);
     MGPBD_CHECK_LAUNCH();
-    k_jt_pow<<<G, kT, 0, s>>>(targs(j), src, dst, partials, js);
+    k_lz_apply<<<G, kT, 0, s>>>(targs(j), it, q, qprev, w, partials, js);
     MGPBD_CHECK_LAUNCH();
+    k_lz_orth<<<G, kT, 0, s>>>(j.nt, it, q, w, partials, js);
+    MGPBD_CHECK_LAUNCH();
+    if (it + 1 < steps) {
+      k_lz_next<<<G, kT, 0, s>>>(j.nt, it, q, qprev, w, js);
+      MGPBD_CHECK_LAUNCH();
+    }
   }
-  k_jcoef<<<1, 32, 0, s>>>(js, degree, lo_ratio);
-  MGPBD_CHECK_LAUNCH();
+}
+
+// Largest eigenvalue of the symmetric tridiagonal T (diagonal a, off-
+// diagonal b) by Sturm-sequence bisection on its Gershgorin interval.
+double lanczos_lmax(const double* a, const double* b, int k) {
+  double lo = 1e300, hi = -1e300;
+  for (int i = 0; i < k; ++i) {
+    double r = (i > 0 ? std::fabs(b[i - 1]) : 0.0) + (i + 1 < k ? std::fabs(b[i]) : 0.0);
+    lo = std::fmin(lo, a[i] - r);
+    hi = std::fmax(hi, a[i] + r);
+  }
+  if (!(hi >= lo) || !std::isfinite(hi) || !std::isfinite(lo)) return NAN;
+  // count of eigenvalues < x
+  auto below = [&](double x) {
+    int c = 0;
+    double d = 1.0;
+    for (int i = 0; i < k; ++i) {
+      double bb = i > 0 ? b[i - 1] * b[i - 1] : 0.0;
+      d = (a[i] - x) - (i > 0 ? bb / d : 0.0);
+      if (d == 0.0) d = -1e-300;
+      if (d < 0.0) ++c;
+    }
+    return c;
+  };
+  for (int it = 0; it < 200 && hi - lo > 1e-12 * std::fmax(1.0, std::fabs(hi)); ++it) {
+    double mid = 0.5 * (lo + hi);
+    if (below(mid) >= k) hi = mid;  // all eigenvalues below mid
+    else lo = mid;
+  }
+  return hi;
+}
+
+// Chebyshev acceleration coefficients on [hi * lo_ratio, hi] (Saad,
+// "Iterative Methods for Sparse Linear Systems", 2nd ed., Alg. 12.1):
+// sigma = theta / delta, rho_0 = 1 / sigma, rho_i = 1 / (2 sigma - rho_{i-1}),
+// d_i = rho_i rho_{i-1} d_{i-1} + (2 rho_i / delta) r_i.
+ChebCoef chebyshev_coefficients(double lmax, int degree, double lo_ratio) {
+  ChebCoef c{};
+  double hi = lmax;
+  if (!(hi > 0.0) || !std::isfinite(hi)) hi = 2.0;
+  const double lo = hi * lo_ratio;
+  const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
+  double rho = 1.0 / sigma;
+  for (int i = 1; i < degree && i < kMaxCheb; ++i) {
+    const double rn = 1.0 / (2.0 * sigma - rho);
+    c.c1[i] = static_cast<float>(rn * rho);
+    c.c2[i] = static_cast<float>(2.0 * rn / delta);
+    rho = rn;
+  }
+  c.theta = theta;
+  c.lmax = lmax;
+  c.inv_theta = static_cast<float>(1.0 / theta);
+  c.degree = degree;
+  return c;
 }
 
 void launch_jcg_init(const JView& j, const JVecs& v, JState* js, CgState* st, double tol_abs,

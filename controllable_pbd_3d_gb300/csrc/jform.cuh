@@ -22,16 +22,25 @@
 namespace mgpbd {
 
 constexpr int kMaxCheb = 32;
+constexpr int kMaxLanczos = 32;
 
-// Device scalars of the Chebyshev-preconditioned CG; lives next to CgState.
-struct JState {
-  double theta;           // (lmax + lmin) / 2 of D^-1 A
-  double lmax;            // power-iteration estimate of lambda_max(D^-1 A)
+// Chebyshev coefficients (written by the host after each Lanczos estimate)
+struct ChebCoef {
+  double theta;           // (hi + lo) / 2 of the interval on D^-1 A
+  double lmax;            // Lanczos estimate of lambda_max(D^-1 A)
   float c1[kMaxCheb];     // rho_i * rho_{i-1}
   float c2[kMaxCheb];     // 2 rho_i / delta
   float inv_theta;
   int32_t degree;
-  uint32_t ticket[4];     // last-block counters of the fused reductions
+};
+
+// Device scalars of the Chebyshev-preconditioned CG; lives next to CgState.
+struct JState {
+  ChebCoef cf;
+  double lz_a[kMaxLanczos];  // Lanczos diagonal
+  double lz_b[kMaxLanczos];  // Lanczos off-diagonal
+  double scale;              // scratch scalar (1/|q| of the start vector)
+  uint32_t ticket[4];        // last-block counters of the fused reductions
 };
 
 struct JView {
@@ -51,11 +60,15 @@ void launch_jform_prepare(const JView& j, const int32_t* inc_ent, float4* gV, fl
                           cudaStream_t s);
 // y = A x (plain), for tests and the power iteration
 void launch_jform_apply(const JView& j, const float* x, float* y, cudaStream_t s);
-// lambda_max(D^-1 A) by `iters` power steps on the persistent vector v (nt)
-// and the Chebyshev coefficients for `degree` on [lmax * lo_ratio, lmax]
-void launch_jform_cheb_setup(const JView& j, float* v, float* w, double* partials,
-                             JState* js, CgState* st, int iters, int degree, float lo_ratio,
-                             cudaStream_t s);
+// `steps` Lanczos steps on S = D^-1/2 A D^-1/2 from a fixed start vector;
+// the tridiagonal coefficients land in js->lz_a / js->lz_b (q, qprev, w:
+// nt floats of scratch)
+void launch_jform_lanczos(const JView& j, float* q, float* qprev, float* w, double* partials,
+                          JState* js, int steps, cudaStream_t s);
+// host side: largest eigenvalue of the Lanczos tridiagonal (bisection) and
+// the Chebyshev coefficients of `degree` on [hi * lo_ratio, hi]
+double lanczos_lmax(const double* a, const double* b, int k);
+ChebCoef chebyshev_coefficients(double lmax, int degree, double lo_ratio);
 
 // CG with the degree-k Chebyshev preconditioner (k >= 1; k = 1 is scaled
 // Jacobi), scalars on the device.  init: x = 0, r = b, z = M^-1 r, p = z.

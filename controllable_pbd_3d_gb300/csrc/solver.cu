@@ -124,6 +124,7 @@ Solver::~Solver() {
   if (jcg_exec_) cudaGraphExecDestroy(jcg_exec_);
   if (h_buf_) cudaFreeHost(h_buf_);
   if (h_state_) cudaFreeHost(h_state_);
+  if (h_cf_) cudaFreeHost(h_cf_);
 }
 
 void Solver::require_init() const {
@@ -171,6 +172,7 @@ void Solver::init() {
   cudaStream_t s = stream_;
   if (!h_buf_) MGPBD_CUDA(cudaMallocHost(&h_buf_, sizeof(double) * 64));
   if (!h_state_) MGPBD_CUDA(cudaMallocHost(&h_state_, sizeof(CgState)));
+  if (!h_cf_) MGPBD_CUDA(cudaMallocHost(&h_cf_, sizeof(ChebCoef)));
   x_old_.alloc(3LL * nv_);
   x_pred_.alloc(3LL * nv_);
   dpos_.alloc(3LL * nv_);
@@ -431,13 +433,22 @@ JVecs Solver::jvecs(const float* b, float* x) {
 }
 
 // Per Newton iteration: vertex-major gradients, 1/diag(A), lambda_max of
-// D^-1 A (six power steps, warm-started from the previous vector) and the
-// Chebyshev coefficients.
+// D^-1 A by 24 Lanczos steps (upper end taken 2% above the Ritz value; a
+// Chebyshev interval that misses the top of the spectrum makes the
+// preconditioner indefinite) and the Chebyshev coefficients.
 void Solver::jform_setup() {
+  constexpr int kSteps = 24;
   JView j = jview();
   launch_jform_prepare(j, inc_ent_.p, gV_.p, jdinv_.p, stream_);
-  launch_jform_cheb_setup(j, pw_v_.p, pw_w_.p, partials_.p, jst_.p, cg_state_.p, 6,
-                          p_.cheb_degree, p_.cheb_lo, stream_);
+  launch_jform_lanczos(j, pw_v_.p, jd_.p, pw_w_.p, partials_.p, jst_.p, kSteps, stream_);
+  static_assert(2 * kMaxLanczos <= 64, "h_buf_ holds the Lanczos coefficients");
+  MGPBD_CUDA(cudaMemcpyAsync(h_buf_, jst_.p->lz_a, sizeof(double) * kMaxLanczos,
+                             cudaMemcpyDeviceToHost, stream_));
+  sync_read(h_buf_ + kMaxLanczos, jst_.p->lz_b, sizeof(double) * kMaxLanczos);
+  double lmax = lanczos_lmax(h_buf_, h_buf_ + kMaxLanczos, kSteps);
+  if (!std::isfinite(lmax) || !(lmax > 0.0)) status_ |= MGPBD_STATUS_NAN;
+  *h_cf_ = chebyshev_coefficients(1.02 * lmax, p_.cheb_degree, p_.cheb_lo);
+  MGPBD_CUDA(cudaMemcpyAsync(&jst_.p->cf, h_cf_, sizeof(ChebCoef), cudaMemcpyHostToDevice, stream_));
 }
 
 // CG with the Chebyshev preconditioner as one CUDA graph: init, a device-side
@@ -445,6 +456,22 @@ void Solver::jform_setup() {
 // float32 copy of the float64 solution.
 int32_t Solver::pcg_cheb(const float* b, float* x) {
   cudaStream_t outer = stream_;
+  if (!p_.use_graph) {
+    // same kernels from the host; every kernel is a no-op once done is set
+    JView j = jview();
+    JVecs v = jvecs(b, x);
+    launch_jcg_init(j, v, jst_.p, cg_state_.p, p_.tol_cg, p_.rel_tol_cg, p_.maxiter_cg, outer);
+    launch_jcg_cheb_steps(j, v, jst_.p, cg_state_.p, p_.cheb_degree, true, outer);
+    for (int32_t k = 0; k < p_.maxiter_cg; k += 8) {
+      for (int c = 0; c < 8; ++c) launch_jcg_body(j, v, jst_.p, cg_state_.p, p_.cheb_degree, outer);
+      sync_read(h_state_, cg_state_.p, sizeof(CgState));
+      if (h_state_->done) break;
+    }
+    launch_jcg_finish(v, nt_, cg_state_.p, outer);
+    sync_read(h_state_, cg_state_.p, sizeof(CgState));
+    status_ |= static_cast<uint32_t>(h_state_->status);
+    return h_state_->iters;
+  }
   if (!jcg_exec_ || jcg_b_ != b || jcg_x_ != x) {
     if (jcg_exec_) {
       cudaGraphExecDestroy(jcg_exec_);
@@ -690,7 +717,8 @@ void Solver::cg_body(const float* b, float* x) {
 int32_t Solver::pcg(const float* b, float* x) {
   require_init();
   if (cheb()) return pcg_cheb(b, x);
-  if (p_.mode == MGPBD_MODE_FAST && b == rhs_.p && x == dlam_.p) return pcg_graph(b, x);
+  if (p_.mode == MGPBD_MODE_FAST && p_.use_graph && b == rhs_.p && x == dlam_.p)
+    return pcg_graph(b, x);
   cudaStream_t s = stream_;
   int64_t n = nt_;
   int blocks = reduce_blocks(n);

@@ -130,6 +130,7 @@ class Solver {
   DevBuf<float> pw_a_, pw_b_;  // power-iteration vectors
   double* h_buf_ = nullptr;    // pinned host scratch
   CgState* h_state_ = nullptr;
+  ChebCoef* h_cf_ = nullptr;   // pinned staging of the Chebyshev coefficients
 
   // captured CG loop (FAST mode)
   cudaGraphExec_t cg_exec_ = nullptr;

@@ -95,7 +95,8 @@ class MGPBDSolverGPU:
                aggregation='tet', benchmark=None, *, mode='parity', rel_tol_cg=0.0,
                coarse_solver='jacobi', smoother='jacobi', max_levels=0, max_coarse=400,
                kinematic_pins=False, coarse_sweeps=0, cg_alias=False, compliance=0.0,
-               precond='vcycle', cheb_degree=8, cheb_lo=0.01, check_finite=True):
+               precond='vcycle', cheb_degree=8, cheb_lo=0.01, use_graph=True,
+               check_finite=True):
     if aggregation != 'tet':
       raise NotImplementedError(
           "aggregation='pyamg' needs PyAMG's smoothed-aggregation setup, which this "
@@ -160,6 +161,7 @@ class MGPBDSolverGPU:
     p.precond = {'vcycle': 0, 'cheb': 1}[precond]
     p.cheb_degree = int(cheb_degree)
     p.cheb_lo = float(cheb_lo)
+    p.use_graph = int(bool(use_graph))
     self.params = p
     h = C.c_void_p()
     N.check(self._lib.mgpbd_create(C.byref(p), C.byref(h)), 'mgpbd_create')

@@ -107,6 +107,11 @@ typedef struct mgpbd_params {
   int32_t precond;
   int32_t cheb_degree;
   float cheb_lo;
+  /* FAST mode: 1 (default) runs each CG solve as one CUDA graph with a
+   * device-side while loop; 0 launches the same kernels from a host loop
+   * that checks the device state every 8 iterations (for profilers that
+   * cannot look inside conditional graphs). */
+  int32_t use_graph;
 } mgpbd_params;
 
 #define MGPBD_PRECOND_VCYCLE 0

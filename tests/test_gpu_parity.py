@@ -250,6 +250,23 @@ def test_fast_cheb_matches_float64_oracle(cuda):
   assert err <= 1e-5 * float(np.abs(o.x).max()), err
 
 
+@pytest.mark.parametrize('precond', ['cheb', 'vcycle'])
+def test_graph_and_host_loops_agree(cuda, precond):
+  """The captured device-driven CG and the host-driven launch of the same
+  kernels give bit-identical positions."""
+  z = golden('step_cube6_mu3e4.npz')
+  kw = dict(mode='fast', precond=precond, rel_tol_cg=1e-6, maxiter_cg=2000)
+  if precond == 'vcycle':
+    kw['smoother'] = 'safe'
+  s1, x1 = make_solver(cuda, z, use_graph=True, **kw)
+  s2, x2 = make_solver(cuda, z, use_graph=False, **kw)
+  for k in range(2):
+    s1.step(k)
+    s2.step(k)
+  np.testing.assert_array_equal(np_(x1), np_(x2))
+  assert s1.stats()['cg_iters_total'] == s2.stats()['cg_iters_total']
+
+
 def test_fast_mode_matches_parity_mode(cuda):
   """The captured device-driven CG computes what the host-driven one does."""
   z = golden('step_cube6_mu3e4.npz')
