@@ -1,0 +1,11 @@
+"""GB300 (sm_103a) implementation of the MGPBD global XPBD step of
+JamesYang-7/Controllable_PBD_3D, behind the reference's Python interface.
+
+The compute runs in libmgpbd.so (hand-written CUDA + C++); this package
+is the ctypes binding and the Python mirrors of the reference classes.
+"""
+
+from .mgpbd_gpu import MGPBDSolverGPU  # noqa: F401
+from .solver_benchmark import SolverBenchmark  # noqa: F401
+
+__all__ = ['MGPBDSolverGPU', 'SolverBenchmark']

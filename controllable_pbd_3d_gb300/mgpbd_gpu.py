@@ -272,7 +272,10 @@ class MGPBDSolverGPU:
     rc = self._lib.mgpbd_solve(self._h, int(frame))
     if self.benchmark is not None:
       for ite, r, cg, om, t in self.newton_log():
-        self.benchmark.record_iteration(int(ite), r, cg_iters=int(cg), omega=om, t=t)
+        try:
+          self.benchmark.record_iteration(int(ite), r, cg_iters=int(cg), omega=om, t=t)
+        except TypeError:  # a recorder without the timestamp argument
+          self.benchmark.record_iteration(int(ite), r, cg_iters=int(cg), omega=om)
       self.benchmark.end_frame()
     self._check(rc, 'mgpbd_solve')
 
