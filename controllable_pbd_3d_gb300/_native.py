@@ -109,6 +109,7 @@ _SIGS = {
     'mgpbd_csr_jacobi': (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp, f32, vp]),
     'mgpbd_csr_diag_inv': (C.c_int, [i32, vp, vp, vp, vp, vp]),
     'mgpbd_dot': (C.c_int, [i32, vp, vp, P_f64, vp]),
+    'mgpbd_dot_noalloc': (C.c_int, [i32, vp, vp, P_f64, vp]),
     'mgpbd_axpy': (C.c_int, [i32, f32, vp, vp, vp]),
     'mgpbd_xpay': (C.c_int, [i32, f32, vp, vp, vp]),
     'mgpbd_scale': (C.c_int, [i32, f32, vp, vp]),

@@ -259,6 +259,21 @@ int mgpbd_csr_diag_inv(int32_t n_rows, const int32_t* indptr, const int32_t* ind
                        const float* data, float* diag_inv, void* stream);
 /* gpu_dot (cons/sparse_gpu.py:18-23); float64 accumulation, fixed order */
 int mgpbd_dot(int32_t n, const float* a, const float* b, double* out, void* stream);
+/* Same result as mgpbd_dot (within float64 rounding), for callers that may
+ * not allocate GPU memory: no counterpart in the reference.  Hosts that own
+ * the device memory budget (an engine or tool embedding this library, a
+ * real-time loop with a fixed memory plan) can forbid cudaMalloc/cudaFree,
+ * which may wait for the whole device and bypass the host's allocator.
+ * This entry point allocates nothing: its scratch is a 512 KiB device
+ * array inside libmgpbd.so (one float64 per 1024 elements plus the
+ * result), held by every GPU that loads the library until the process
+ * exits.  n is limited to 67,108,864 elements (MGPBD_ERANGE beyond).  The
+ * first call on each device looks up the array's address (with that
+ * device current); make that first call before any stream capture.  All
+ * calls share the one array: calls that overlap on the GPU (other streams,
+ * other host threads) race and must be serialised by the caller.  `out` is
+ * host memory; the call returns after the result is copied back. */
+int mgpbd_dot_noalloc(int32_t n, const float* a, const float* b, double* out, void* stream);
 /* gpu_axpy (:26-30) y += alpha x ; gpu_xpay (:33-37) y = x + alpha y */
 int mgpbd_axpy(int32_t n, float alpha, const float* x, float* y, void* stream);
 int mgpbd_xpay(int32_t n, float alpha, const float* x, float* y, void* stream);
