@@ -391,6 +391,30 @@ def run_ours(args):
     dist.destroy_process_group()
 
 
+def run_profile_solve(args):
+  """One linear solve (substep 0, Newton iteration 0) of the workload with
+  the kernels launched from the host (no CUDA graph), for profilers: a few
+  thousand launches instead of the ~250k of a timed step."""
+  import torch
+  kw = dict(SOLVER_KW)
+  kw.update(FAST_KW if args.profile_precond == 'cheb' else PLAIN_KW)
+  kw['use_graph'] = False
+  kw['maxiter_cg'] = args.profile_maxiter
+  s, x, _ = make_solver(torch, args.size, kw)
+  s.make_prediction()
+  s.lambdaf.zero_()
+  s._compute_C_and_gradC()
+  s._residual_norm_gpu()
+  s._fill_A_and_update_gpu()
+  torch.cuda.synchronize()
+  t0 = time.perf_counter()
+  it = s._gpu_solver.solve(s._b_gpu, s._dlam_gpu)
+  torch.cuda.synchronize()
+  print(json.dumps({'profile_solve': args.profile_precond, 'size': args.size, 'cg_iters': it,
+                    'seconds': round(time.perf_counter() - t0, 4),
+                    'status': s.stats()['status']}), flush=True)
+
+
 def run_reference(args):
   """The reference algorithm on the host cores: the OpenMP CPU port of the
   plain step (the reference itself needs Taichi, which is not available).
@@ -440,8 +464,13 @@ def main():
   # same kernels launched from a host loop instead of one CUDA graph per
   # CG solve (ncu cannot profile kernels inside conditional graphs)
   ap.add_argument('--no-graph', action='store_true')
+  ap.add_argument('--profile-solve', action='store_true')
+  ap.add_argument('--profile-precond', default='cheb', choices=['cheb', 'vcycle'])
+  ap.add_argument('--profile-maxiter', type=int, default=6000)
   args = ap.parse_args()
-  if args.impl == 'reference':
+  if args.profile_solve:
+    run_profile_solve(args)
+  elif args.impl == 'reference':
     run_reference(args)
   else:
     run_ours(args)

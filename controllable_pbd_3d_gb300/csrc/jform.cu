@@ -4,7 +4,10 @@
 // iteration of degree k is 2k + 2 kernels with no scalar-only launches.
 #include "jform.cuh"
 
+#include <algorithm>
 #include <cmath>
+#include <mutex>
+#include <unordered_map>
 
 #include "common.h"
 
@@ -107,16 +110,45 @@ __global__ void __launch_bounds__(kT)
     const float w = valid ? invm[v] : 0.0f;
     if (valid && w != 0.0f) {
       const int32_t k0 = inc_ptr[v], k1 = inc_ptr[v + 1];
-      for (int32_t k = k0 + lane; k < k1; k += kVG) {
-        const float4 e = __ldg(gV + k);
-        const int32_t t = __float_as_int(e.w);
+      // up to kUnroll entries per lane in one pass (24 incident tets per
+      // vertex): all entry loads first, then all dependent x gathers, so a
+      // lane keeps several requests in flight instead of one
+      constexpr int kUnroll = 6;
+      float4 e[kUnroll];
+#pragma unroll
+      for (int u2 = 0; u2 < kUnroll; ++u2) {
+        const int32_t k = k0 + lane + kVG * u2;
+        e[u2] = k < k1 ? __ldg(gV + k) : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+      }
+      float xs[kUnroll];
+#pragma unroll
+      for (int u2 = 0; u2 < kUnroll; ++u2) {
+        const int32_t t = __float_as_int(e[u2].w);
+        float xt = 0.0f;
+        if (t >= 0) {
+          if (SRC == kSrcZbP) xt = x[t] + beta * p[t];
+          else if (SRC == kSrcSqrtD) xt = x[t] * sqrtf(p[t]);
+          else xt = x[t];
+        }
+        xs[u2] = xt;
+      }
+#pragma unroll
+      for (int u2 = 0; u2 < kUnroll; ++u2) {
+        ax += xs[u2] * e[u2].x;
+        ay += xs[u2] * e[u2].y;
+        az += xs[u2] * e[u2].z;
+      }
+      // vertices with more than kVG * kUnroll incident tets
+      for (int32_t k = k0 + lane + kVG * kUnroll; k < k1; k += kVG) {
+        const float4 ee = __ldg(gV + k);
+        const int32_t t = __float_as_int(ee.w);
         float xt;
         if (SRC == kSrcZbP) xt = x[t] + beta * p[t];
         else if (SRC == kSrcSqrtD) xt = x[t] * sqrtf(p[t]);
         else xt = x[t];
-        ax += xt * e.x;
-        ay += xt * e.y;
-        az += xt * e.z;
+        ax += xt * ee.x;
+        ay += xt * ee.y;
+        az += xt * ee.z;
       }
     }
 #pragma unroll
@@ -444,14 +476,42 @@ __global__ void k_seed(float* v, int32_t n) {
   }
 }
 
-// tet-phase grids: up to 8 blocks of 256 per SM
-inline int tgrid(int64_t n) {
-  int64_t g = (n + kT - 1) / kT;
-  return static_cast<int>(g < 1 ? 1 : (g > kMaxReduceBlocks ? kMaxReduceBlocks : g));
+// Blocks of kT threads of `fn` that fit on the device at once (one wave),
+// from the occupancy calculator, cached per kernel.  Grids never exceed one
+// wave: the kernels stride over their work, so a partial second wave (and
+// its tail) never occurs.
+int resident_blocks(const void* fn) {
+  static std::mutex mu;
+  static std::unordered_map<const void*, int> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = cache.find(fn);
+  if (it != cache.end()) return it->second;
+  int dev = 0, sms = 0, per_sm = 0;
+  MGPBD_CUDA(cudaGetDevice(&dev));
+  MGPBD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  MGPBD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kT, 0));
+  int r = std::max(1, std::min(sms * std::max(per_sm, 1), kMaxReduceBlocks));
+  cache[fn] = r;
+  return r;
 }
 
-inline int vgrid(int32_t nv) {
+template <class K>
+inline int tgrid_for(K* fn, int64_t n) {
+  int64_t g = (n + kT - 1) / kT;
+  int cap = resident_blocks(reinterpret_cast<const void*>(fn));
+  return static_cast<int>(g < 1 ? 1 : (g > cap ? cap : g));
+}
+
+template <class K>
+inline int vgrid_for(K* fn, int32_t nv) {
   int64_t g = (static_cast<int64_t>(nv) * kVG + kT - 1) / kT;
+  int cap = resident_blocks(reinterpret_cast<const void*>(fn));
+  return static_cast<int>(g < 1 ? 1 : (g > cap ? cap : g));
+}
+
+// tet-phase grid for kernels whose occupancy is not looked up
+inline int tgrid(int64_t n) {
+  int64_t g = (n + kT - 1) / kT;
   return static_cast<int>(g < 1 ? 1 : (g > kMaxReduceBlocks ? kMaxReduceBlocks : g));
 }
 
@@ -477,23 +537,23 @@ void launch_jform_prepare(const JView& j, const int32_t* inc_ent, float4* gV, fl
 }
 
 void launch_jform_apply(const JView& j, const float* x, float* y, cudaStream_t s) {
-  k_jv<kSrcX><<<vgrid(j.nv), kT, 0, s>>>(j.nv, j.inc_ptr, j.gV, j.invm, x, nullptr, nullptr,
-                                          nullptr, j.u, 0.f);
+  k_jv<kSrcX><<<vgrid_for(k_jv<kSrcX>, j.nv), kT, 0, s>>>(j.nv, j.inc_ptr, j.gV, j.invm, x,
+                                                            nullptr, nullptr, nullptr, j.u, 0.f);
   MGPBD_CHECK_LAUNCH();
-  k_jt_plain<<<tgrid(j.nt), kT, 0, s>>>(targs(j), x, y);
+  k_jt_plain<<<tgrid_for(k_jt_plain, j.nt), kT, 0, s>>>(targs(j), x, y);
   MGPBD_CHECK_LAUNCH();
 }
 
 void launch_jform_lanczos(const JView& j, float* q, float* qprev, float* w, double* partials,
                           JState* js, int steps, cudaStream_t s) {
   require(steps >= 1 && steps <= kMaxLanczos, MGPBD_EINVAL, "Lanczos steps out of range");
-  const int G = tgrid(j.nt);
+  const int G = tgrid_for(k_lz_apply, j.nt);
   k_lz_seed<<<G, kT, 0, s>>>(j.nt, q, partials, js);
   MGPBD_CHECK_LAUNCH();
   k_lz_scale<<<G, kT, 0, s>>>(j.nt, q, qprev, js);
   MGPBD_CHECK_LAUNCH();
   for (int it = 0; it < steps; ++it) {
-    k_jv<kSrcSqrtD><<<vgrid(j.nv), kT, 0, s>>>(j.nv, j.inc_ptr, j.gV, j.invm, q, j.dinv, nullptr,
+    k_jv<kSrcSqrtD><<<vgrid_for(k_jv<kSrcSqrtD>, j.nv), kT, 0, s>>>(j.nv, j.inc_ptr, j.gV, j.invm, q, j.dinv, nullptr,
                                                js, j.u, 0.f);
     MGPBD_CHECK_LAUNCH();
     k_lz_apply<<<G, kT, 0, s>>>(targs(j), it, q, qprev, w, partials, js);
@@ -563,7 +623,7 @@ ChebCoef chebyshev_coefficients(double lmax, int degree, double lo_ratio) {
 
 void launch_jcg_init(const JView& j, const JVecs& v, JState* js, CgState* st, double tol_abs,
                      double tol_rel, int maxiter, cudaStream_t s) {
-  const int G = tgrid(j.nt);
+  const int G = tgrid_for(k_ju0, j.nt);
   k_ju0<<<G, kT, 0, s>>>(j.nt, v.b, j.dinv, v.xd, v.r, v.z, v.d, v.p, v.partials, st, js, tol_abs,
                          tol_rel, maxiter);
   MGPBD_CHECK_LAUNCH();
@@ -573,9 +633,9 @@ void launch_jcg_init(const JView& j, const JVecs& v, JState* js, CgState* st, do
 
 void launch_jcg_cheb_steps(const JView& j, const JVecs& v, JState* js, CgState* st, int degree,
                            bool init, cudaStream_t s) {
-  const int G = tgrid(j.nt);
+  const int G = tgrid_for(k_jt_cheb<true, false>, j.nt);
   for (int i = 1; i < degree; ++i) {
-    k_jv<kSrcX><<<vgrid(j.nv), kT, 0, s>>>(j.nv, j.inc_ptr, j.gV, j.invm, v.z, nullptr, st, js, j.u,
+    k_jv<kSrcX><<<vgrid_for(k_jv<kSrcX>, j.nv), kT, 0, s>>>(j.nv, j.inc_ptr, j.gV, j.invm, v.z, nullptr, st, js, j.u,
                                             0.f);
     MGPBD_CHECK_LAUNCH();
     const bool last = i == degree - 1;
@@ -591,12 +651,12 @@ void launch_jcg_cheb_steps(const JView& j, const JVecs& v, JState* js, CgState* 
 
 void launch_jcg_body(const JView& j, const JVecs& v, JState* js, CgState* st, int degree,
                      cudaStream_t s) {
-  const int G = tgrid(j.nt);
-  k_jv<kSrcZbP><<<vgrid(j.nv), kT, 0, s>>>(j.nv, j.inc_ptr, j.gV, j.invm, v.z, v.p, st, js, j.u, 0.f);
+  k_jv<kSrcZbP><<<vgrid_for(k_jv<kSrcZbP>, j.nv), kT, 0, s>>>(j.nv, j.inc_ptr, j.gV, j.invm, v.z,
+                                                              v.p, st, js, j.u, 0.f);
   MGPBD_CHECK_LAUNCH();
-  k_jt_ap<<<G, kT, 0, s>>>(targs(j), v.z, v.p, v.ap, v.partials, st, js);
+  k_jt_ap<<<tgrid_for(k_jt_ap, j.nt), kT, 0, s>>>(targs(j), v.z, v.p, v.ap, v.partials, st, js);
   MGPBD_CHECK_LAUNCH();
-  k_ju<<<G, kT, 0, s>>>(j.nt, v.p, v.ap, j.dinv, v.xd, v.r, v.z, v.d, v.partials, st, js);
+  k_ju<<<tgrid_for(k_ju, j.nt), kT, 0, s>>>(j.nt, v.p, v.ap, j.dinv, v.xd, v.r, v.z, v.d, v.partials, st, js);
   MGPBD_CHECK_LAUNCH();
   launch_jcg_cheb_steps(j, v, js, st, degree, false, s);
 }
