@@ -50,7 +50,7 @@ class Params(C.Structure):
       ('rel_tol_cg', f32), ('coarse_solver', i32), ('smoother', i32), ('max_levels', i32),
       ('max_coarse', i32), ('kinematic_pins', i32), ('coarse_sweeps', i32), ('cg_alias', i32),
       ('compliance', f32), ('precond', i32), ('cheb_degree', i32), ('cheb_lo', f32),
-      ('use_graph', i32),
+      ('use_graph', i32), ('persistent', i32), ('primal', i32),
   ]
 
 
@@ -58,7 +58,7 @@ class Stats(C.Structure):
   _fields_ = [
       ('newton_iters', i32), ('cg_iters_total', i32), ('cg_iters_last', i32), ('n_levels', i32),
       ('residual0', f64), ('residual', f64), ('omega_last', f64), ('status', C.c_uint32),
-      ('nnz', i64 * 8), ('rows', i64 * 8),
+      ('nnz', i64 * 8), ('rows', i64 * 8), ('cg_path', i32), ('cg_grid', i32),
   ]
 
 

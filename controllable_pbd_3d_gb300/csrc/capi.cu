@@ -82,6 +82,8 @@ void mgpbd_default_params(mgpbd_params* p) {
   p->cheb_degree = 8;
   p->cheb_lo = 0.01f;
   p->use_graph = 1;
+  p->persistent = 1;
+  p->primal = 0;
 }
 
 const char* mgpbd_strerror(int code) {

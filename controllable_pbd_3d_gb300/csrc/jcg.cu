@@ -1,0 +1,638 @@
+// The Chebyshev-preconditioned CG of FAST mode as ONE cooperative
+// persistent kernel per solve.
+//
+// Every phase of an iteration (vertex phase, tet phase, vector update) runs
+// on all blocks of one resident grid, separated by a grid barrier, instead
+// of one kernel launch per phase: a launch costs each SM ~3 us of ramp-up
+// and drain around ~4 us of work here, and a degree-k iteration has 2k + 1
+// phases.  Scalars (alpha, beta, the stopping test) never leave the chip:
+// each block writes its partial of a dot product, and after the barrier
+// warp 0 of every block sums all partials in the same fixed order, so all
+// blocks hold bit-identical scalars and take the same branch.
+//
+// Staging: when the mesh is small enough (up to ~400k tets on 152 SMs),
+// each block owns a contiguous range of vertices (balanced by incident
+// entries plus a per-vertex weight) and of tets (32-aligned), and copies
+// their constant operator data into shared memory once per solve: the
+// vertex-major entries (gradient, tet id), the incidence offsets and
+// weights, and the tet indices.  A phase then issues only the gathers of the vector it applies
+// A to (x_t in the vertex phase, u_v in the tet phase) plus the coalesced
+// per-tet loads, instead of two or three dependent L2 round trips.
+// Larger meshes run the same phases reading everything from L2, with tets
+// and vertices strided over the grid.
+//
+// Arithmetic is float32 per element (GB300's float64 rate is a small
+// fraction of its float32 rate).  Dot products sum in float32 within a warp
+// and in float64 across warps and blocks; the solution is accumulated with
+// Kahan compensation (Kahan 1965) so ~10^3 updates do not lose its low bits.
+//
+// Barrier waits are bounded: a block that waits longer than the given limit
+// marks the solve failed (status bit, error flag) and returns, and every
+// other block leaves at its next wait; the host reports the failure.
+#include <algorithm>
+#include <cmath>
+
+#include "common.h"
+#include "jform.cuh"
+#include "jform_dev.cuh"
+#include "persist.cuh"
+
+namespace mgpbd {
+
+namespace {
+
+using namespace jdev;
+using namespace pdev;
+
+// One block of kPT threads per SM: up to 112 registers a thread, so each
+// thread can issue the gathers of several tets (vertices) before it uses
+// them, and 152 arrivals per grid barrier.
+constexpr int kPT = 576;
+constexpr int kTB = 4;   // tets a thread handles per round of a tet phase
+constexpr int kVS = 4;   // lanes per vertex in the staged vertex phase
+constexpr int kVE = 6;   // entries a lane gathers per vertex and round
+constexpr int kVB = 4;   // vertices a lane group handles per round
+constexpr int kVertexCost = 64;  // per-vertex weight of the work split
+
+struct PArgs {
+  TArgs ta;  // t_i, gradC, u, alpha~, 1/diag, nt
+  int32_t nv;
+  const int32_t* inc_ptr;
+  const float4* gV;
+  const float* invm;
+  float4* u;
+  const float* b;
+  float* x;
+  float* xc;
+  float* r;
+  float* z;
+  float* d;
+  float* p;
+  float* ap;
+  double* partials;  // 3 slots of gridDim.x
+  GridSync* gs;
+  CgState* st;
+  const JState* js;
+  const int32_t* part_v;  // staged: block vertex ranges (grid + 1)
+  const int32_t* part_t;  // staged: block tet ranges (grid + 1)
+  int32_t emax, tmax, vmax;
+  double tol_abs, tol_rel;
+  int32_t maxiter, degree;
+  unsigned long long spin_ns;
+};
+
+// This block's share of the work: tets from tbeg to tend in steps of tstep
+// (staged: the block's own range; otherwise strided over the whole grid),
+// and, when staged, its vertex range and the shared-memory copies.
+struct Own {
+  int64_t tbeg, tend, tstep;
+  int32_t tb0;
+  int32_t vb0, nvb;
+  const float4* e;     // entries of the block's vertices
+  const int4* q;       // indices of the block's tets
+  const int32_t* off;  // nvb + 1 entry offsets
+  const float* w;      // nvb vertex weights
+};
+
+__device__ __forceinline__ bool grid_sync(const PArgs& a, unsigned long long& gen) {
+  return pdev::grid_sync(a.gs, &a.st->status, a.spin_ns, gen);
+}
+
+// sum_l g_{t,l} . u_{q_l} for tet t with indices q
+__device__ __forceinline__ float tdot(const TArgs& a, int64_t t, int4 q) {
+  const float4 g0 = __ldg(a.gradC + 3 * t), g1 = __ldg(a.gradC + 3 * t + 1),
+               g2 = __ldg(a.gradC + 3 * t + 2);
+  const float4 u0 = a.u[q.x], u1 = a.u[q.y], u2 = a.u[q.z], u3 = a.u[q.w];
+  return (g0.x * u0.x + g0.y * u0.y + g0.z * u0.z) + (g0.w * u1.x + g1.x * u1.y + g1.y * u1.z) +
+         (g1.z * u2.x + g1.w * u2.y + g2.x * u2.z) + (g2.y * u3.x + g2.z * u3.y + g2.w * u3.z);
+}
+
+template <bool STAGED>
+__device__ __forceinline__ int4 tet_q(const PArgs& a, const Own& o, int64_t t) {
+  if (STAGED) return o.q[t - o.tb0];
+  return a.ta.t_i[t];
+}
+
+// Vertex phase: u_v = w_v sum x_t g_{t,l} with x_t = z_t (+ beta p_t).
+template <int SRC, bool STAGED>
+__device__ __forceinline__ void vphase(const PArgs& a, const Own& o, float beta) {
+  if (!STAGED) {
+    const int lane = threadIdx.x % kVG;
+    constexpr int kPerWarp = 32 / kVG;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t stride = ((int64_t)gridDim.x * blockDim.x >> 5) * kPerWarp;
+    for (int64_t base = warp * kPerWarp; base < a.nv; base += stride) {
+      const int64_t v = base + (threadIdx.x & 31) / kVG;
+      const bool valid = v < a.nv;
+      float w;
+      const float3 s = jv_group<SRC>(v, valid, lane, a.inc_ptr, a.gV, a.invm, a.z, a.p, beta, &w);
+      if (valid && lane == 0) a.u[v] = make_float4(w * s.x, w * s.y, w * s.z, 0.0f);
+    }
+    return;
+  }
+  // staged: kVS lanes per vertex, kVB vertices per lane group and round;
+  // the entries (shared memory, one pad slot after each vertex's run so
+  // consecutive vertices start 4 banks apart) give the tet ids, and all
+  // gathers of a round are issued before any is consumed
+  const int lane = threadIdx.x % kVS;
+  const int grp = threadIdx.x / kVS;
+  const int ngrp = blockDim.x / kVS;
+  for (int base = 0; base < o.nvb; base += kVB * ngrp) {
+    int k0[kVB], k1[kVB];
+    float wv[kVB];
+#pragma unroll
+    for (int i = 0; i < kVB; ++i) {
+      const int lv = base + grp + i * ngrp;
+      k0[i] = k1[i] = 0;
+      wv[i] = 0.0f;
+      if (lv < o.nvb) {
+        wv[i] = o.w[lv];
+        if (wv[i] != 0.0f) {
+          k0[i] = o.off[lv];
+          k1[i] = o.off[lv + 1] - 1;
+        }
+      }
+    }
+    float xs[kVB][kVE];
+#pragma unroll
+    for (int i = 0; i < kVB; ++i) {
+#pragma unroll
+      for (int c = 0; c < kVE; ++c) {
+        const int k = k0[i] + lane + kVS * c;
+        float xt = 0.0f;
+        if (k < k1[i]) {
+          const int32_t t = __float_as_int(o.e[k].w);
+          xt = SRC == kSrcZbP ? a.z[t] + beta * a.p[t] : a.z[t];
+        }
+        xs[i][c] = xt;
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < kVB; ++i) {
+      float ax = 0.f, ay = 0.f, az = 0.f;
+#pragma unroll
+      for (int c = 0; c < kVE; ++c) {
+        const int k = k0[i] + lane + kVS * c;
+        if (k < k1[i]) {
+          const float4 g = o.e[k];
+          ax += xs[i][c] * g.x;
+          ay += xs[i][c] * g.y;
+          az += xs[i][c] * g.z;
+        }
+      }
+      // vertices with more than kVS * kVE incident tets
+      for (int k = k0[i] + lane + kVS * kVE; k < k1[i]; k += kVS) {
+        const float4 g = o.e[k];
+        const int32_t t = __float_as_int(g.w);
+        const float xt = SRC == kSrcZbP ? a.z[t] + beta * a.p[t] : a.z[t];
+        ax += xt * g.x;
+        ay += xt * g.y;
+        az += xt * g.z;
+      }
+#pragma unroll
+      for (int sh = kVS / 2; sh > 0; sh >>= 1) {
+        ax += __shfl_xor_sync(0xffffffffu, ax, sh, kVS);
+        ay += __shfl_xor_sync(0xffffffffu, ay, sh, kVS);
+        az += __shfl_xor_sync(0xffffffffu, az, sh, kVS);
+      }
+      const int lv = base + grp + i * ngrp;
+      if (lane == 0 && lv < o.nvb)
+        a.u[o.vb0 + lv] = make_float4(wv[i] * ax, wv[i] * ay, wv[i] * az, 0.0f);
+    }
+  }
+}
+
+// Chebyshev step: rr = D^-1 (r - A z); d = c1 d + c2 rr; z += d.  LAST also
+// writes this block's partial of r.z.
+template <bool LAST, bool STAGED>
+__device__ __forceinline__ void tphase_cheb(const PArgs& a, const Own& o, float c1, float c2,
+                                            double* slot) {
+  float acc = 0.0f;
+  for (int64_t tb = o.tbeg; tb < o.tend; tb += kTB * o.tstep) {
+    float y[kTB];
+#pragma unroll
+    for (int i = 0; i < kTB; ++i) {
+      const int64_t t = tb + i * o.tstep;
+      y[i] = t < o.tend ? tdot(a.ta, t, tet_q<STAGED>(a, o, t)) : 0.0f;
+    }
+#pragma unroll
+    for (int i = 0; i < kTB; ++i) {
+      const int64_t t = tb + i * o.tstep;
+      if (t < o.tend) {
+        const float zt = a.z[t];
+        const float yt = y[i] + __ldg(a.ta.alpha + t) * zt;
+        const float rt = a.r[t];
+        const float rrv = __ldg(a.ta.dinv + t) * (rt - yt);
+        const float dt = c1 * a.d[t] + c2 * rrv;
+        a.d[t] = dt;
+        const float zn = zt + dt;
+        a.z[t] = zn;
+        if (LAST) acc += rt * zn;
+      }
+    }
+  }
+  if (LAST) put_partial(acc, slot);
+}
+
+// p = z + beta p; ap = A p; this block's partial of p.Ap
+template <bool STAGED>
+__device__ __forceinline__ void tphase_ap(const PArgs& a, const Own& o, float bf, double* slot) {
+  float acc = 0.0f;
+  for (int64_t tb = o.tbeg; tb < o.tend; tb += kTB * o.tstep) {
+    float y[kTB];
+#pragma unroll
+    for (int i = 0; i < kTB; ++i) {
+      const int64_t t = tb + i * o.tstep;
+      y[i] = t < o.tend ? tdot(a.ta, t, tet_q<STAGED>(a, o, t)) : 0.0f;
+    }
+#pragma unroll
+    for (int i = 0; i < kTB; ++i) {
+      const int64_t t = tb + i * o.tstep;
+      if (t < o.tend) {
+        const float pt = a.z[t] + bf * a.p[t];
+        const float yt = y[i] + __ldg(a.ta.alpha + t) * pt;
+        a.p[t] = pt;
+        a.ap[t] = yt;
+        acc += pt * yt;
+      }
+    }
+  }
+  put_partial(acc, slot);
+}
+
+template <bool STAGED>
+__global__ void __launch_bounds__(kPT, 1) k_jcg(PArgs a) {
+  extern __shared__ __align__(16) unsigned char s_dyn[];
+  __shared__ float s_c1[kMaxCheb], s_c2[kMaxCheb];
+  __shared__ float s_scal;  // alpha or beta, broadcast from thread 0
+  __shared__ int s_stop;
+  // CG scalars, read and written by thread 0 only (shared memory keeps them
+  // out of every thread's registers)
+  __shared__ double bbs, tol2, rz, rr, pap, alpha, beta;
+  __shared__ int32_t iters;
+  __shared__ uint32_t status;
+  if (threadIdx.x < kMaxCheb) {
+    s_c1[threadIdx.x] = a.js->cf.c1[threadIdx.x];
+    s_c2[threadIdx.x] = a.js->cf.c2[threadIdx.x];
+  }
+  if (threadIdx.x == 0) {
+    bbs = tol2 = rz = rr = pap = alpha = beta = 0.0;
+    iters = 0;
+    status = 0;
+  }
+  const float it = a.js->cf.inv_theta;
+  const int m = a.degree;
+  const int G = gridDim.x;
+  double* P0 = a.partials;
+  double* P1 = a.partials + G;
+  double* P2 = a.partials + 2 * G;
+  unsigned long long gen = 0;
+
+  Own o;
+  if (STAGED) {
+    const int32_t tb0 = a.part_t[blockIdx.x], tb1 = a.part_t[blockIdx.x + 1];
+    const int32_t vb0 = a.part_v[blockIdx.x], vb1 = a.part_v[blockIdx.x + 1];
+    const int32_t e0 = a.inc_ptr[vb0], ne = a.inc_ptr[vb1] - e0;
+    o.tbeg = tb0 + threadIdx.x;
+    o.tend = tb1;
+    o.tstep = blockDim.x;
+    o.tb0 = tb0;
+    o.vb0 = vb0;
+    o.nvb = vb1 - vb0;
+    float4* se = reinterpret_cast<float4*>(s_dyn);
+    int4* sq = reinterpret_cast<int4*>(se + a.emax + a.vmax);
+    int32_t* soff = reinterpret_cast<int32_t*>(sq + a.tmax);
+    float* sw = reinterpret_cast<float*>(soff + a.vmax + 1);
+    // vertex lv's entries go to [off + lv, off + lv + n): one pad slot per vertex
+    const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5, ln = threadIdx.x & 31;
+    for (int lv = wid; lv < o.nvb; lv += nw) {
+      const int32_t k0 = a.inc_ptr[vb0 + lv], n = a.inc_ptr[vb0 + lv + 1] - k0;
+      const int32_t dst = k0 - e0 + lv;
+      for (int j = ln; j < n; j += 32) se[dst + j] = __ldg(a.gV + k0 + j);
+    }
+    for (int k = threadIdx.x; k < tb1 - tb0; k += blockDim.x) sq[k] = a.ta.t_i[tb0 + k];
+    for (int k = threadIdx.x; k <= o.nvb; k += blockDim.x) soff[k] = a.inc_ptr[vb0 + k] - e0 + k;
+    for (int k = threadIdx.x; k < o.nvb; k += blockDim.x) sw[k] = a.invm[vb0 + k];
+    (void)ne;
+    o.e = se;
+    o.q = sq;
+    o.off = soff;
+    o.w = sw;
+  } else {
+    o.tbeg = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    o.tend = a.ta.nt;
+    o.tstep = (int64_t)G * blockDim.x;
+    o.tb0 = 0;
+    o.vb0 = 0;
+    o.nvb = 0;
+    o.e = nullptr;
+    o.q = nullptr;
+    o.off = nullptr;
+    o.w = nullptr;
+  }
+  __syncthreads();
+
+  // x = 0, r = b, p = 0, z = d = D^-1 b / theta; partials of b.b and b.z
+  {
+    float bb = 0.0f, bz = 0.0f;
+    for (int64_t t = o.tbeg; t < o.tend; t += o.tstep) {
+      const float bt = a.b[t];
+      a.x[t] = 0.0f;
+      a.xc[t] = 0.0f;
+      a.r[t] = bt;
+      a.p[t] = 0.0f;
+      const float zt = __ldg(a.ta.dinv + t) * bt * it;
+      a.z[t] = zt;
+      a.d[t] = zt;
+      bb += bt * bt;
+      bz += bt * zt;
+    }
+    put_partial(bb, P0);
+    put_partial(bz, P1);
+  }
+  if (!grid_sync(a, gen)) return;
+  if (threadIdx.x < 32) {
+    const double sb = warp_sum_partials(P0, G);
+    const double sz = warp_sum_partials(P1, G);
+    if (threadIdx.x == 0) {
+      bbs = sb;
+      rz = sz;
+      const double t2 = a.tol_abs * a.tol_abs, r2 = a.tol_rel * a.tol_rel * bbs;
+      tol2 = r2 > t2 ? r2 : t2;
+      int stop = a.maxiter <= 0;
+      if (!isfinite(bbs)) {
+        status |= MGPBD_STATUS_NAN;
+        stop = 1;
+      }
+      s_stop = stop;
+    }
+  }
+  __syncthreads();
+  bool done = s_stop != 0;
+
+  // remaining Chebyshev steps of z = M^-1 r
+  if (!done && m > 1) {
+    for (int i = 1; i < m; ++i) {
+      vphase<kSrcX, STAGED>(a, o, 0.0f);
+      if (!grid_sync(a, gen)) return;
+      if (i == m - 1) tphase_cheb<true, STAGED>(a, o, s_c1[i], s_c2[i], P2);
+      else tphase_cheb<false, STAGED>(a, o, s_c1[i], s_c2[i], P2);
+      if (!grid_sync(a, gen)) return;
+    }
+    if (threadIdx.x < 32) {
+      const double sz = warp_sum_partials(P2, G);
+      if (threadIdx.x == 0) {
+        rz = sz;
+        int stop = 0;
+        if (!isfinite(rz)) {
+          status |= MGPBD_STATUS_NAN;
+          stop = 1;
+        }
+        s_stop = stop;
+      }
+    }
+    __syncthreads();
+    done = s_stop != 0;
+  }
+
+  float bf = 0.0f;  // beta
+  while (!done) {
+    // u = W J^T (z + beta p)
+    vphase<kSrcZbP, STAGED>(a, o, bf);
+    if (!grid_sync(a, gen)) return;
+    // p = z + beta p; ap = A p; partials of p.Ap
+    tphase_ap<STAGED>(a, o, bf, P0);
+    if (!grid_sync(a, gen)) return;
+    if (threadIdx.x < 32) {
+      const double sp = warp_sum_partials(P0, G);
+      if (threadIdx.x == 0) {
+        pap = sp;
+        int stop = 0;
+        if (!isfinite(pap)) status |= MGPBD_STATUS_NAN;
+        if (!(fabs(pap) >= 1e-30) || !isfinite(pap)) {
+          stop = 1;
+        } else {
+          if (pap <= 0.0) status |= MGPBD_STATUS_PAP_NONPOS;
+          alpha = rz / pap;
+          s_scal = (float)alpha;
+        }
+        s_stop = stop;
+      }
+    }
+    __syncthreads();
+    if (s_stop) break;
+    // x += alpha p (compensated); r -= alpha Ap; z = d = D^-1 r / theta;
+    // partials of r.r and r.z
+    {
+      const float al = s_scal;
+      float acc_rr = 0.0f, acc_rz = 0.0f;
+      for (int64_t t = o.tbeg; t < o.tend; t += o.tstep) {
+        const float pt = a.p[t], apt = a.ap[t];
+        const float s = a.x[t];
+        const float y = al * pt - a.xc[t];
+        const float sn = s + y;
+        a.xc[t] = (sn - s) - y;
+        a.x[t] = sn;
+        const float rt = a.r[t] - al * apt;
+        a.r[t] = rt;
+        const float zt = __ldg(a.ta.dinv + t) * rt * it;
+        a.z[t] = zt;
+        a.d[t] = zt;
+        acc_rr += rt * rt;
+        acc_rz += rt * zt;
+      }
+      put_partial(acc_rr, P1);
+      if (m == 1) put_partial(acc_rz, P2);
+    }
+    if (!grid_sync(a, gen)) return;
+    if (threadIdx.x < 32) {
+      const double sr = warp_sum_partials(P1, G);
+      if (threadIdx.x == 0) {
+        rr = sr;
+        int stop = 0;
+        if (!isfinite(rr)) {
+          status |= MGPBD_STATUS_NAN;
+          stop = 1;
+        } else if (rr < tol2) {
+          iters += 1;
+          stop = 1;
+        }
+        s_stop = stop;
+      }
+    }
+    __syncthreads();
+    if (s_stop) break;
+    if (m > 1) {
+      for (int i = 1; i < m; ++i) {
+        vphase<kSrcX, STAGED>(a, o, 0.0f);
+        if (!grid_sync(a, gen)) return;
+        if (i == m - 1) tphase_cheb<true, STAGED>(a, o, s_c1[i], s_c2[i], P2);
+        else tphase_cheb<false, STAGED>(a, o, s_c1[i], s_c2[i], P2);
+        if (!grid_sync(a, gen)) return;
+      }
+    }
+    if (threadIdx.x < 32) {
+      const double sz = warp_sum_partials(P2, G);
+      if (threadIdx.x == 0) {
+        iters += 1;
+        int stop = 0;
+        if (fabs(rz) < 1e-30) {
+          stop = 1;
+        } else {
+          beta = sz / rz;
+          rz = sz;
+          s_scal = (float)beta;
+          if (iters >= a.maxiter) {
+            status |= MGPBD_STATUS_CG_MAXITER;
+            stop = 1;
+          }
+        }
+        s_stop = stop;
+      }
+    }
+    __syncthreads();
+    if (s_stop) break;
+    bf = s_scal;
+  }
+
+  // the compensated sum, rounded once
+  for (int64_t t = o.tbeg; t < o.tend; t += o.tstep) a.x[t] = a.x[t] - a.xc[t];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    CgState* st = a.st;
+    st->rz = rz;
+    st->pap = pap;
+    st->alpha = alpha;
+    st->beta = beta;
+    st->rr = rr;
+    st->rr0 = bbs;
+    st->tol2 = tol2;
+    st->iters = iters;
+    st->done = 1;
+    st->maxiter = a.maxiter;
+    st->body_runs = 1;
+    atomicOr(reinterpret_cast<unsigned int*>(&st->status), status);
+  }
+}
+
+int64_t staged_smem_bytes(int32_t emax, int32_t tmax, int32_t vmax) {
+  const int64_t b = 16LL * (emax + vmax) + 16LL * tmax + 4LL * (vmax + 1) + 4LL * vmax;
+  return (b + 15) / 16 * 16;
+}
+
+}  // namespace
+
+JcgPlan jcg_plan(const std::vector<int32_t>& inc_ptr, int32_t nv, int32_t nt) {
+  require(static_cast<int64_t>(inc_ptr.size()) == static_cast<int64_t>(nv) + 1, MGPBD_EINVAL,
+          "incidence offsets must hold nv + 1 entries");
+  int dev = 0, coop = 0, sms = 0, optin = 0;
+  MGPBD_CUDA(cudaGetDevice(&dev));
+  MGPBD_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+  require(coop != 0, MGPBD_ENOTSUP, "device does not support cooperative launch");
+  MGPBD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  MGPBD_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  const int64_t ne = inc_ptr[nv];
+  {
+    JcgPlan p;
+    const int G = sms;
+    p.vb.resize(G + 1);
+    p.tb.resize(G + 1);
+    // vertices: equal shares of (incident entries + kVertexCost per vertex),
+    // so neither gathers nor vertex rounds pile up in one block; tets: equal
+    // 32-aligned shares
+    const int64_t total = ne + static_cast<int64_t>(kVertexCost) * nv;
+    int32_t v = 0;
+    for (int b = 0; b <= G; ++b) {
+      if (b == G) {
+        p.vb[b] = nv;
+      } else {
+        const int64_t target = total * b / G;
+        while (v < nv && inc_ptr[v] + static_cast<int64_t>(kVertexCost) * v < target) ++v;
+        p.vb[b] = v;
+      }
+      const int64_t tt = (static_cast<int64_t>(nt) * b / G + 31) / 32 * 32;
+      p.tb[b] = b == G ? nt : static_cast<int32_t>(std::min<int64_t>(tt, nt));
+    }
+    for (int b = 0; b < G; ++b) {
+      p.vmax = std::max(p.vmax, p.vb[b + 1] - p.vb[b]);
+      p.tmax = std::max(p.tmax, p.tb[b + 1] - p.tb[b]);
+      p.emax = std::max(p.emax, inc_ptr[p.vb[b + 1]] - inc_ptr[p.vb[b]]);
+    }
+    const int64_t smem = staged_smem_bytes(p.emax, p.tmax, p.vmax);
+    if (smem <= optin) {
+      MGPBD_CUDA(cudaFuncSetAttribute(k_jcg<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(smem)));
+      int occ = 0;
+      MGPBD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_jcg<true>, kPT,
+                                                               static_cast<size_t>(smem)));
+      if (occ >= 1) {
+        p.staged = true;
+        p.grid = G;
+        p.smem = static_cast<int>(smem);
+        return p;
+      }
+    }
+  }
+  // too large to stage: every phase reads from L2, work strided over the grid
+  JcgPlan p;
+  int occ = 0;
+  MGPBD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_jcg<false>, kPT, 0));
+  require(occ >= 1, MGPBD_ENOTSUP, "persistent CG kernel does not fit on an SM");
+  p.staged = false;
+  p.grid = sms * occ;
+  p.smem = 0;
+  return p;
+}
+
+void launch_jcg_persistent(const JView& j, const JcgVecs& v, const JcgPlan& plan,
+                           const int32_t* part_dev, const JState* js, CgState* st, double tol_abs,
+                           double tol_rel, int maxiter, int degree, double spin_limit_s,
+                           cudaStream_t s) {
+  require(degree >= 1 && degree <= kMaxCheb, MGPBD_EINVAL, "Chebyshev degree out of range");
+  require(plan.grid > 0, MGPBD_ESTATE, "persistent CG plan not built");
+  require(3LL * plan.grid <= v.partials_capacity, MGPBD_ERANGE, "partials buffer too small");
+  require(!plan.staged || part_dev != nullptr, MGPBD_ESTATE, "staged plan without partition");
+  PArgs a;
+  a.ta.t_i = reinterpret_cast<const int4*>(j.t_i);
+  a.ta.gradC = reinterpret_cast<const float4*>(j.gradC);
+  a.ta.u = j.u;
+  a.ta.alpha = j.alpha;
+  a.ta.dinv = j.dinv;
+  a.ta.nt = j.nt;
+  a.nv = j.nv;
+  a.inc_ptr = j.inc_ptr;
+  a.gV = j.gV;
+  a.invm = j.invm;
+  a.u = j.u;
+  a.b = v.b;
+  a.x = v.x;
+  a.xc = v.xc;
+  a.r = v.r;
+  a.z = v.z;
+  a.d = v.d;
+  a.p = v.p;
+  a.ap = v.ap;
+  a.partials = v.partials;
+  a.gs = v.gs;
+  a.st = st;
+  a.js = js;
+  a.part_v = plan.staged ? part_dev : nullptr;
+  a.part_t = plan.staged ? part_dev + plan.grid + 1 : nullptr;
+  a.emax = plan.emax;
+  a.tmax = plan.tmax;
+  a.vmax = plan.vmax;
+  a.tol_abs = tol_abs;
+  a.tol_rel = tol_rel;
+  a.maxiter = maxiter;
+  a.degree = degree;
+  a.spin_ns = static_cast<unsigned long long>(spin_limit_s * 1e9);
+  MGPBD_CUDA(cudaMemsetAsync(v.gs, 0, sizeof(GridSync), s));
+  MGPBD_CUDA(cudaMemsetAsync(st, 0, sizeof(CgState), s));
+  void* args[] = {&a};
+  const void* fn = plan.staged ? reinterpret_cast<const void*>(k_jcg<true>)
+                               : reinterpret_cast<const void*>(k_jcg<false>);
+  MGPBD_CUDA(cudaLaunchCooperativeKernel(fn, dim3(plan.grid), dim3(kPT), args,
+                                         static_cast<size_t>(plan.smem), s));
+  MGPBD_CHECK_LAUNCH();
+}
+
+}  // namespace mgpbd

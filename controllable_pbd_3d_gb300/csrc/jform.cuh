@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <vector>
 
 #include "kernels.cuh"
 
@@ -93,6 +94,73 @@ void launch_jcg_cheb_steps(const JView& j, const JVecs& v, JState* js, CgState* 
 // test, z = M^-1 r, beta (all kernels are no-ops once st->done)
 void launch_jcg_body(const JView& j, const JVecs& v, JState* js, CgState* st, int degree,
                      cudaStream_t s);
+// Grid barrier state of the persistent CG kernel (zeroed before each launch)
+struct GridSync {
+  unsigned long long count;  // arrivals; barrier n completes at n * grid
+  unsigned int err;          // 1: a block gave up waiting
+  unsigned int pad;
+};
+
+// float32 work vectors of the persistent CG (all nt long but partials)
+struct JcgVecs {
+  const float* b = nullptr;
+  float* x = nullptr;   // solution (compensated sum during the solve)
+  float* xc = nullptr;  // Kahan compensation of x
+  float* r = nullptr;
+  float* z = nullptr;
+  float* d = nullptr;
+  float* p = nullptr;
+  float* ap = nullptr;
+  double* partials = nullptr;
+  int64_t partials_capacity = 0;  // doubles; needs 3 * the plan's grid
+  GridSync* gs = nullptr;
+};
+// Work split of the persistent kernel for one mesh on the current device:
+// the cooperative grid, and, when the block data fits in shared memory
+// (staged), each block's vertex range (balanced by incident entries) and
+// 32-aligned tet range with the largest per-block counts.
+struct JcgPlan {
+  bool staged = false;
+  int grid = 0;   // resident blocks of the cooperative launch
+  int smem = 0;   // dynamic shared memory per block (staged)
+  int32_t vmax = 0, tmax = 0, emax = 0;
+  std::vector<int32_t> vb, tb;  // grid + 1 boundaries each (staged)
+};
+JcgPlan jcg_plan(const std::vector<int32_t>& inc_ptr, int32_t nv, int32_t nt);
+// The whole CG solve (init, iterations to the tolerance or maxiter, the
+// Chebyshev preconditioner of `degree`) as one cooperative kernel; st is
+// zeroed and then filled like the per-phase path fills it.  part_dev holds
+// plan.vb then plan.tb on the device (staged plans).  A barrier wait longer
+// than spin_limit_s sets MGPBD_STATUS_SYNC_TIMEOUT in st->status.
+void launch_jcg_persistent(const JView& j, const JcgVecs& v, const JcgPlan& plan,
+                           const int32_t* part_dev, const JState* js, CgState* st, double tol_abs,
+                           double tol_rel, int maxiter, int degree, double spin_limit_s,
+                           cudaStream_t s);
+
+// Work vectors of the primal persistent CG (pcg.cu): vertex vectors are
+// float4 per vertex (xyz used), s is per tet.
+struct PcgVecs {
+  const float* b = nullptr;  // dual right-hand side (nt)
+  float* dlam = nullptr;     // dual solution (nt)
+  float4 *y = nullptr, *yc = nullptr, *r = nullptr, *z = nullptr, *d = nullptr, *p = nullptr,
+         *q = nullptr, *rhs = nullptr, *bi0 = nullptr, *bi1 = nullptr;
+  float* s = nullptr;
+  double* partials = nullptr;
+  int64_t partials_capacity = 0;  // doubles; needs 4 * the plan's grid
+  GridSync* gs = nullptr;
+};
+// Whether a staged plan's shared memory also fits the primal kernel, and
+// the primal kernel's cooperative grid when nothing is staged.
+bool pcg_plan_fits(JcgPlan& plan);
+int pcg_unstaged_grid();
+// The dual solve A dlam = b by CG on the primal system K y = J^T alpha~^-1 b
+// (one cooperative kernel; see pcg.cu).  st is zeroed and then filled like
+// the dual path fills it (iters = primal CG iterations).
+void launch_pcg_primal(const JView& j, const PcgVecs& v, const JcgPlan& plan,
+                       const int32_t* part_dev, CgState* st, double tol_abs, double tol_rel,
+                       int maxiter, int degree, float cheb_lo, double spin_limit_s,
+                       cudaStream_t s);
+
 // deterministic start vector of the power iteration
 void launch_seed(float* v, int32_t n, cudaStream_t s);
 // x (float32 output) = xd

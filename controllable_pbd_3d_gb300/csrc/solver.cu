@@ -222,6 +222,16 @@ void Solver::init() {
   vertex_incidence(t_host.data(), nt_, nv_, ip, ie);
   upload(inc_ptr_, ip, s);
   upload(inc_ent_, ie, s);
+  if (cheb() && p_.persistent) {
+    jplan_ = jcg_plan(ip, nv_, nt_);
+    if (primal() && jplan_.staged && !pcg_plan_fits(jplan_)) jplan_.staged = false;
+    if (primal() && !jplan_.staged) jplan_.grid = pcg_unstaged_grid();
+    if (jplan_.staged) {
+      std::vector<int32_t> part(jplan_.vb);
+      part.insert(part.end(), jplan_.tb.begin(), jplan_.tb.end());
+      upload(jpart_, part, s);
+    }
+  }
 
   // first A at the current positions (cons/mgpbd_gpu.py:98-100)
   launch_constraints(x_, t_i_, dm_inv_.p, nt_, C_.p, gradC_.p, s);
@@ -238,6 +248,12 @@ void Solver::init() {
   inited_ = true;
   stats_ = mgpbd_stats{};
   stats_.n_levels = n_levels();
+  if (cheb() && p_.persistent) {
+    stats_.cg_path = jplan_.staged ? MGPBD_CGPATH_STAGED : MGPBD_CGPATH_PERSISTENT;
+    if (primal())
+      stats_.cg_path = jplan_.staged ? MGPBD_CGPATH_PRIMAL_STAGED : MGPBD_CGPATH_PRIMAL;
+    stats_.cg_grid = jplan_.grid;
+  }
   for (int32_t l = 0; l < n_levels() && l < 8; ++l) {
     stats_.rows[l] = levels_[l].n;
     stats_.nnz[l] = levels_[l].nnz;
@@ -374,6 +390,16 @@ void Solver::alloc_work() {
     jr_.alloc(nt_);
     jst_.alloc(1);
     MGPBD_CUDA(cudaMemsetAsync(jst_.p, 0, sizeof(JState), s));
+    jxc_.alloc(nt_);
+    jrf_.alloc(nt_);
+    jgs_.alloc(1);
+    if (primal()) {
+      for (auto& b : pv_) {
+        b.alloc(nv_);
+        MGPBD_CUDA(cudaMemsetAsync(b.p, 0, sizeof(float4) * nv_, s));
+      }
+      ps_.alloc(nt_);
+    }
     launch_seed(pw_v_.p, nt_, s);
   }
 }
@@ -440,6 +466,7 @@ void Solver::jform_setup() {
   constexpr int kSteps = 24;
   JView j = jview();
   launch_jform_prepare(j, inc_ent_.p, gV_.p, jdinv_.p, stream_);
+  if (primal()) return;  // the primal kernel estimates its own spectrum
   launch_jform_lanczos(j, pw_v_.p, jd_.p, pw_w_.p, partials_.p, jst_.p, kSteps, stream_);
   static_assert(2 * kMaxLanczos <= 64, "h_buf_ holds the Lanczos coefficients");
   MGPBD_CUDA(cudaMemcpyAsync(h_buf_, jst_.p->lz_a, sizeof(double) * kMaxLanczos,
@@ -456,6 +483,55 @@ void Solver::jform_setup() {
 // float32 copy of the float64 solution.
 int32_t Solver::pcg_cheb(const float* b, float* x) {
   cudaStream_t outer = stream_;
+  constexpr double kBarrierLimitS = 4.0;
+  if (primal()) {
+    PcgVecs v;
+    v.b = b;
+    v.dlam = x;
+    v.y = pv_[0].p;
+    v.yc = pv_[1].p;
+    v.r = pv_[2].p;
+    v.z = pv_[3].p;
+    v.d = pv_[4].p;
+    v.p = pv_[5].p;
+    v.q = pv_[6].p;
+    v.rhs = pv_[7].p;
+    v.bi0 = pv_[8].p;
+    v.bi1 = pv_[9].p;
+    v.s = ps_.p;
+    v.partials = partials_.p;
+    v.partials_capacity = static_cast<int64_t>(kMaxReduceBlocks) * 16;
+    v.gs = jgs_.p;
+    launch_pcg_primal(jview(), v, jplan_, jpart_.p, cg_state_.p, p_.tol_cg, p_.rel_tol_cg,
+                      p_.maxiter_cg, p_.cheb_degree, p_.cheb_lo, kBarrierLimitS, outer);
+    sync_read(h_state_, cg_state_.p, sizeof(CgState));
+    if (static_cast<uint32_t>(h_state_->status) & MGPBD_STATUS_SYNC_TIMEOUT)
+      throw Error(MGPBD_ECUDA, "primal CG kernel: a grid barrier wait timed out");
+    status_ |= static_cast<uint32_t>(h_state_->status);
+    return h_state_->iters;
+  }
+  if (p_.persistent) {
+    // one cooperative kernel for the whole solve
+    JcgVecs v;
+    v.b = b;
+    v.x = x;
+    v.xc = jxc_.p;
+    v.r = jrf_.p;
+    v.z = jz_.p;
+    v.d = jd_.p;
+    v.p = jp_.p;
+    v.ap = jap_.p;
+    v.partials = partials_.p;
+    v.partials_capacity = static_cast<int64_t>(kMaxReduceBlocks) * 16;
+    v.gs = jgs_.p;
+    launch_jcg_persistent(jview(), v, jplan_, jpart_.p, jst_.p, cg_state_.p, p_.tol_cg,
+                          p_.rel_tol_cg, p_.maxiter_cg, p_.cheb_degree, kBarrierLimitS, outer);
+    sync_read(h_state_, cg_state_.p, sizeof(CgState));
+    if (static_cast<uint32_t>(h_state_->status) & MGPBD_STATUS_SYNC_TIMEOUT)
+      throw Error(MGPBD_ECUDA, "persistent CG kernel: a grid barrier wait timed out");
+    status_ |= static_cast<uint32_t>(h_state_->status);
+    return h_state_->iters;
+  }
   if (!p_.use_graph) {
     // same kernels from the host; every kernel is a no-op once done is set
     JView j = jview();

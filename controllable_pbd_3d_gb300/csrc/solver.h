@@ -144,6 +144,13 @@ class Solver {
   DevBuf<float> jdinv_, jz_, jd_, jp_, jap_, pw_v_, pw_w_;
   DevBuf<double> jxd_, jr_;
   DevBuf<JState> jst_;
+  DevBuf<float> jxc_, jrf_;  // persistent CG: Kahan term of x, float32 residual
+  DevBuf<GridSync> jgs_;
+  JcgPlan jplan_;          // persistent CG work split
+  DevBuf<float4> pv_[10];  // primal CG vertex vectors
+  DevBuf<float> ps_;       // primal CG tet scratch
+  bool primal() const { return cheb() && p_.persistent && p_.primal; }
+  DevBuf<int32_t> jpart_;  // jplan_.vb then jplan_.tb
   cudaGraphExec_t jcg_exec_ = nullptr;
   const float* jcg_b_ = nullptr;
   float* jcg_x_ = nullptr;

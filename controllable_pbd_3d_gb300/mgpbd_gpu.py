@@ -86,7 +86,14 @@ class MGPBDSolverGPU:
     compliance     > 0: alpha~ = compliance / dt^2 for every tet;
     precond        'vcycle' (reference) or 'cheb' (FAST only: Chebyshev
                    polynomial of degree cheb_degree on [lmax*cheb_lo, lmax],
-                   matrix-free operator, no CSR assembly).
+                   matrix-free operator, no CSR assembly);
+    use_graph      FAST: one CUDA graph with a device-side loop per CG solve
+                   (False: the same kernels from a host loop);
+    persistent     FAST + 'cheb': each CG solve is one cooperative persistent
+                   kernel (False: one kernel per phase, per use_graph);
+    primal         FAST + 'cheb' + persistent: solve the dual system through
+                   the vertex-space system K y = J^T alpha~^-1 b (Woodbury),
+                   same stopping test on the dual residual.
   """
 
   def __init__(self, v_p, v_p_ref, v_invm, t_i, t_m, gravity, dt, mu=1e6, damp=1.0, maxiter=20,
@@ -96,7 +103,7 @@ class MGPBDSolverGPU:
                coarse_solver='jacobi', smoother='jacobi', max_levels=0, max_coarse=400,
                kinematic_pins=False, coarse_sweeps=0, cg_alias=False, compliance=0.0,
                precond='vcycle', cheb_degree=8, cheb_lo=0.01, use_graph=True,
-               check_finite=True):
+               persistent=True, primal=False, check_finite=True):
     if aggregation != 'tet':
       raise NotImplementedError(
           "aggregation='pyamg' needs PyAMG's smoothed-aggregation setup, which this "
@@ -162,6 +169,8 @@ class MGPBDSolverGPU:
     p.cheb_degree = int(cheb_degree)
     p.cheb_lo = float(cheb_lo)
     p.use_graph = int(bool(use_graph))
+    p.persistent = int(bool(persistent))
+    p.primal = int(bool(primal))
     self.params = p
     h = C.c_void_p()
     N.check(self._lib.mgpbd_create(C.byref(p), C.byref(h)), 'mgpbd_create')
@@ -234,6 +243,8 @@ class MGPBDSolverGPU:
         'cg_iters_last': s.cg_iters_last, 'n_levels': nl, 'residual0': s.residual0,
         'residual': s.residual, 'omega_last': s.omega_last, 'status': s.status,
         'rows': list(s.rows[:nl]), 'nnz': list(s.nnz[:nl]),
+        'cg_path': ('kernels', 'persistent', 'staged', 'primal', 'primal-staged')[s.cg_path],
+        'cg_grid': s.cg_grid,
     }
 
   def newton_log(self):

@@ -48,6 +48,8 @@ extern "C" {
 #define MGPBD_STATUS_CG_MAXITER 4u   /* a CG solve hit maxiter_cg              */
 #define MGPBD_STATUS_NEWTON_MAXITER 8u /* the Newton loop hit maxiter          */
 #define MGPBD_STATUS_STALL 16u       /* CG residual stopped decreasing         */
+#define MGPBD_STATUS_SYNC_TIMEOUT 32u /* a grid barrier wait of the persistent
+                                        CG kernel gave up (solve failed)      */
 
 /* ---- solver options ------------------------------------------------------ */
 /* Algorithm variants.  PARITY reproduces the reference step
@@ -112,6 +114,20 @@ typedef struct mgpbd_params {
    * that checks the device state every 8 iterations (for profilers that
    * cannot look inside conditional graphs). */
   int32_t use_graph;
+  /* FAST mode with MGPBD_PRECOND_CHEB: 1 (default) runs each CG solve as ONE
+   * cooperative persistent kernel (grid barriers between its phases, float32
+   * vectors, compensated solution sum); 0 runs the per-phase kernels
+   * (use_graph selects graph or host loop for those). */
+  int32_t persistent;
+  /* FAST mode, MGPBD_PRECOND_CHEB, persistent: 1 solves the dual system
+   * A dlam = b through the primal one, K y = J^T alpha~^-1 b with
+   * K = W^-1 + J^T alpha~^-1 J on the free vertices and dlam = alpha~^-1
+   * (b - J y) (Woodbury identity; block-Jacobi Chebyshev preconditioner,
+   * stopping on the same dual residual); 0 (default) runs CG on A itself.
+   * The primal solve starts from dlam = alpha~^-1 b, whose dual residual
+   * can exceed |b| by the stiffness ratio; in float32 some solves then stall
+   * short of a 1e-6 relative dual residual. */
+  int32_t primal;
 } mgpbd_params;
 
 #define MGPBD_PRECOND_VCYCLE 0
@@ -128,7 +144,17 @@ typedef struct mgpbd_stats {
   uint32_t status;          /* MGPBD_STATUS_* bits of the last solve          */
   int64_t nnz[8];           /* nonzeros per level                             */
   int64_t rows[8];          /* rows per level                                 */
+  int32_t cg_path;          /* MGPBD_CGPATH_* the CG solves run on            */
+  int32_t cg_grid;          /* blocks of the persistent kernel (0 otherwise)  */
 } mgpbd_stats;
+
+#define MGPBD_CGPATH_KERNELS 0      /* one kernel (or graph node) per operation */
+#define MGPBD_CGPATH_PERSISTENT 1   /* one cooperative kernel per solve, the
+                                       operator read from L2                   */
+#define MGPBD_CGPATH_STAGED 2       /* the same with each block's operator data
+                                       staged in shared memory                 */
+#define MGPBD_CGPATH_PRIMAL 3       /* primal system, one cooperative kernel    */
+#define MGPBD_CGPATH_PRIMAL_STAGED 4 /* the same, operator data staged         */
 
 typedef struct mgpbd_solver* mgpbd_handle;
 

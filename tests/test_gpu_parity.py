@@ -181,8 +181,15 @@ def test_matrix_free_apply_equals_csr(cuda, name):
     assert rel(np_(y), z[f'it0_jac_y{lvl}']) < 1e-4
 
 
+# the FAST-mode Chebyshev solve paths: one kernel per phase, the persistent
+# kernel on the dual system, the persistent kernel on the primal system
+CHEB_PATHS = {'kernels': dict(persistent=False), 'dual': dict(persistent=True, primal=False),
+              'primal': dict(persistent=True, primal=True)}
+
+
+@pytest.mark.parametrize('path', list(CHEB_PATHS))
 @pytest.mark.parametrize('degree', [1, 4, 8])
-def test_chebyshev_pcg_solves_the_system(cuda, degree):
+def test_chebyshev_pcg_solves_the_system(cuda, degree, path):
   """The matrix-free Chebyshev-preconditioned CG reaches the requested
   relative residual of the true system (checked in float64 on the host
   with the reference-order CSR matrix)."""
@@ -198,7 +205,7 @@ def test_chebyshev_pcg_solves_the_system(cuda, degree):
   s = MGPBDSolverGPU(xt, cuda.tensor(xr, device='cuda'), cuda.tensor(invm, device='cuda'),
                      cuda.tensor(t, device='cuda'), None, [0, -9.8, 0], 1 / 300, mu=1e5,
                      mode='fast', precond='cheb', cheb_degree=degree, maxiter_cg=3000,
-                     tol_cg=1e-12, rel_tol_cg=1e-6)
+                     tol_cg=1e-12, rel_tol_cg=1e-6, **CHEB_PATHS[path])
   s.init()
   s.make_prediction()
   s.lambdaf.zero_()
@@ -223,7 +230,8 @@ def test_chebyshev_pcg_solves_the_system(cuda, degree):
   del g
 
 
-def test_fast_cheb_matches_float64_oracle(cuda):
+@pytest.mark.parametrize('path', list(CHEB_PATHS))
+def test_fast_cheb_matches_float64_oracle(cuda, path):
   """FAST mode with the matrix-free Chebyshev PCG converges to the same
   positions as the float64 oracle (both solved tightly)."""
   from controllable_pbd_3d_gb300 import meshgen
@@ -241,7 +249,7 @@ def test_fast_cheb_matches_float64_oracle(cuda):
   xt = cuda.tensor(x0, device='cuda')
   s = MGPBDSolverGPU(xt, cuda.tensor(xr, device='cuda'), cuda.tensor(invm, device='cuda'),
                      cuda.tensor(t, device='cuda'), None, [0, -9.8, 0], 1 / 300, mode='fast',
-                     precond='cheb', **kw)
+                     precond='cheb', **CHEB_PATHS[path], **kw)
   s.init()
   for k in range(2):
     o.step(k)
@@ -258,6 +266,8 @@ def test_graph_and_host_loops_agree(cuda, precond):
   kw = dict(mode='fast', precond=precond, rel_tol_cg=1e-6, maxiter_cg=2000)
   if precond == 'vcycle':
     kw['smoother'] = 'safe'
+  else:
+    kw['persistent'] = False  # the per-phase kernels (graph vs host loop)
   s1, x1 = make_solver(cuda, z, use_graph=True, **kw)
   s2, x2 = make_solver(cuda, z, use_graph=False, **kw)
   for k in range(2):
@@ -265,6 +275,47 @@ def test_graph_and_host_loops_agree(cuda, precond):
     s2.step(k)
   np.testing.assert_array_equal(np_(x1), np_(x2))
   assert s1.stats()['cg_iters_total'] == s2.stats()['cg_iters_total']
+
+
+def _block_solver(cuda, n, **kw):
+  from controllable_pbd_3d_gb300 import meshgen
+  from controllable_pbd_3d_gb300.mgpbd_gpu import MGPBDSolverGPU
+  xr, t = meshgen.hex_grid_tets(n, n, n)
+  x0, _ = meshgen.hex_grid_tets(n, n, n, jitter=0.02, seed=5)
+  invm = np.ones(len(xr), np.float32)
+  invm[meshgen.grid_face_vertices(n, n, n, 1)] = 0
+  x = cuda.tensor(x0, device='cuda')
+  s = MGPBDSolverGPU(x, cuda.tensor(xr, device='cuda'), cuda.tensor(invm, device='cuda'),
+                     cuda.tensor(t, device='cuda'), None, [0, -9.8, 0], 1 / 300, mu=1e5,
+                     damp=0.993, maxiter=2, atol=1e-9, rtol=1e-9, tol_cg=1e-12,
+                     rel_tol_cg=1e-5, maxiter_cg=3000, mode='fast', precond='cheb', **kw)
+  s.init()
+  return s, x
+
+
+@pytest.mark.parametrize('primal', [False, True])
+@pytest.mark.parametrize('n,path', [(36, 'staged'), (44, 'persistent')])
+def test_persistent_cg_deterministic_and_matches_per_phase(cuda, n, path, primal):
+  """The one-kernel CG (dual or primal system) repeats bit for bit and
+  lands where the per-phase kernels (dual system, float64 residual) land:
+  on a 36^3 block (233,280 tets) whose per-block operator data is staged in
+  shared memory, and on a 44^3 block (425,920 tets) too large to stage,
+  where every phase strides over the grid reading from L2."""
+  want = {False: path, True: 'primal' if path == 'persistent' else 'primal-staged'}[primal]
+  runs = []
+  for persistent in (True, True, False):
+    s, x = _block_solver(cuda, n, persistent=persistent, primal=primal)
+    assert s.stats()['cg_path'] == (want if persistent else 'kernels')
+    s.step(0)
+    runs.append((np_(x), s.stats()['cg_iters_total'], s.stats()['status']))
+  (xa, ia, sa), (xb, ib, sb), (xc, ic, sc) = runs
+  np.testing.assert_array_equal(xa, xb)
+  assert ia == ib and sa == sb
+  assert ia > 0 and (sa & 1) == 0  # no NaN
+  if not primal:
+    assert abs(ia - ic) <= max(2, ic // 50), (ia, ic)
+  scale = float(np.abs(xc).max())
+  assert float(np.abs(xa - xc).max()) <= 1e-5 * scale
 
 
 def test_fast_mode_matches_parity_mode(cuda):
