@@ -58,10 +58,12 @@ def workload(n, seed=0):
 # workload: ~2000 iterations for the plain AMG-PCG, ~650 for the fast step)
 SOLVER_KW = dict(damp=1.0, maxiter=20, atol=1e-4, rtol=1e-2, maxiter_cg=6000, tol_cg=1e-12,
                  rel_tol_cg=1e-6, n_smooth=2, kinematic_pins=True)
-# the optimised step: each CG solve is one cooperative persistent kernel
-# (matrix-free operator, per-block operator data in shared memory, degree-8
-# Chebyshev preconditioner)
-FAST_KW = dict(mode='fast', precond='cheb', cheb_degree=8, cheb_lo=1e-3)
+# the optimised step: each CG solve is a primal (Woodbury) warm start to a
+# 1e-2 dual residual, then CG on the dual system to 1e-6, each one
+# cooperative persistent kernel (matrix-free operator, per-block operator
+# data in shared memory, degree-8 Chebyshev preconditioners)
+FAST_KW = dict(mode='fast', precond='cheb', cheb_degree=8, cheb_lo=1e-3, primal=True,
+               primal_tol=1e-2)
 # the plain float32 AMG-PCG: the reference's two-level tet-aggregation V-cycle
 # on CSR matrices with host-checked loops; the smoother weight is capped at
 # 4/(3 lambda_max) because omega = 2/3 diverges at this stiffness
@@ -353,6 +355,8 @@ def run_ours(args):
   kw.update(FAST_KW)
   if args.no_graph:
     kw['use_graph'] = False
+  if args.primal is not None:
+    kw['primal'] = bool(args.primal)
   s, x, compliance = make_solver(torch, args.size, kw)
   for i in range(args.warmup):
     s.step(i)
@@ -528,6 +532,8 @@ def main():
   ap.add_argument('--profile-solve', action='store_true')
   ap.add_argument('--profile-precond', default='cheb', choices=['cheb', 'vcycle'])
   ap.add_argument('--profile-maxiter', type=int, default=6000)
+  # 1/0: with / without the primal (Woodbury) warm start of each CG solve
+  ap.add_argument('--primal', type=int, default=None, choices=[0, 1])
   # Chebyshev solve as one persistent kernel, or one kernel per phase
   ap.add_argument('--profile-path', default='persistent', choices=['persistent', 'kernels'])
   args = ap.parse_args()

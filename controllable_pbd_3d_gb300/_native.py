@@ -50,7 +50,7 @@ class Params(C.Structure):
       ('rel_tol_cg', f32), ('coarse_solver', i32), ('smoother', i32), ('max_levels', i32),
       ('max_coarse', i32), ('kinematic_pins', i32), ('coarse_sweeps', i32), ('cg_alias', i32),
       ('compliance', f32), ('precond', i32), ('cheb_degree', i32), ('cheb_lo', f32),
-      ('use_graph', i32), ('persistent', i32), ('primal', i32),
+      ('use_graph', i32), ('persistent', i32), ('primal', i32), ('primal_tol', f32),
   ]
 
 

@@ -84,6 +84,7 @@ void mgpbd_default_params(mgpbd_params* p) {
   p->use_graph = 1;
   p->persistent = 1;
   p->primal = 0;
+  p->primal_tol = 1e-2f;
 }
 
 const char* mgpbd_strerror(int code) {

@@ -78,6 +78,7 @@ struct PArgs {
   int32_t emax, tmax, vmax;
   double tol_abs, tol_rel;
   int32_t maxiter, degree;
+  int32_t warm;  // 1: start from the x on entry instead of 0
   unsigned long long spin_ns;
 };
 
@@ -113,9 +114,9 @@ __device__ __forceinline__ int4 tet_q(const PArgs& a, const Own& o, int64_t t) {
   return a.ta.t_i[t];
 }
 
-// Vertex phase: u_v = w_v sum x_t g_{t,l} with x_t = z_t (+ beta p_t).
+// Vertex phase: u_v = w_v sum x_t g_{t,l} with x_t = src_t (+ beta p_t).
 template <int SRC, bool STAGED>
-__device__ __forceinline__ void vphase(const PArgs& a, const Own& o, float beta) {
+__device__ __forceinline__ void vphase(const PArgs& a, const Own& o, float beta, const float* src) {
   if (!STAGED) {
     const int lane = threadIdx.x % kVG;
     constexpr int kPerWarp = 32 / kVG;
@@ -125,7 +126,7 @@ __device__ __forceinline__ void vphase(const PArgs& a, const Own& o, float beta)
       const int64_t v = base + (threadIdx.x & 31) / kVG;
       const bool valid = v < a.nv;
       float w;
-      const float3 s = jv_group<SRC>(v, valid, lane, a.inc_ptr, a.gV, a.invm, a.z, a.p, beta, &w);
+      const float3 s = jv_group<SRC>(v, valid, lane, a.inc_ptr, a.gV, a.invm, src, a.p, beta, &w);
       if (valid && lane == 0) a.u[v] = make_float4(w * s.x, w * s.y, w * s.z, 0.0f);
     }
     return;
@@ -162,7 +163,7 @@ __device__ __forceinline__ void vphase(const PArgs& a, const Own& o, float beta)
         float xt = 0.0f;
         if (k < k1[i]) {
           const int32_t t = __float_as_int(o.e[k].w);
-          xt = SRC == kSrcZbP ? a.z[t] + beta * a.p[t] : a.z[t];
+          xt = SRC == kSrcZbP ? src[t] + beta * a.p[t] : src[t];
         }
         xs[i][c] = xt;
       }
@@ -184,7 +185,7 @@ __device__ __forceinline__ void vphase(const PArgs& a, const Own& o, float beta)
       for (int k = k0[i] + lane + kVS * kVE; k < k1[i]; k += kVS) {
         const float4 g = o.e[k];
         const int32_t t = __float_as_int(g.w);
-        const float xt = SRC == kSrcZbP ? a.z[t] + beta * a.p[t] : a.z[t];
+        const float xt = SRC == kSrcZbP ? src[t] + beta * a.p[t] : src[t];
         ax += xt * g.x;
         ay += xt * g.y;
         az += xt * g.z;
@@ -332,20 +333,31 @@ __global__ void __launch_bounds__(kPT, 1) k_jcg(PArgs a) {
   }
   __syncthreads();
 
-  // x = 0, r = b, p = 0, z = d = D^-1 b / theta; partials of b.b and b.z
+  // x = 0 (or the warm start x0), r = b - A x, p = 0, z = d = D^-1 r / theta;
+  // partials of b.b and r.z
+  if (a.warm) {
+    vphase<kSrcX, STAGED>(a, o, 0.0f, a.x);
+    if (!grid_sync(a, gen)) return;
+  }
   {
     float bb = 0.0f, bz = 0.0f;
     for (int64_t t = o.tbeg; t < o.tend; t += o.tstep) {
       const float bt = a.b[t];
-      a.x[t] = 0.0f;
+      float rt = bt;
+      if (a.warm) {
+        const float xt = a.x[t];
+        rt = bt - (tdot(a.ta, t, tet_q<STAGED>(a, o, t)) + __ldg(a.ta.alpha + t) * xt);
+      } else {
+        a.x[t] = 0.0f;
+      }
       a.xc[t] = 0.0f;
-      a.r[t] = bt;
+      a.r[t] = rt;
       a.p[t] = 0.0f;
-      const float zt = __ldg(a.ta.dinv + t) * bt * it;
+      const float zt = __ldg(a.ta.dinv + t) * rt * it;
       a.z[t] = zt;
       a.d[t] = zt;
       bb += bt * bt;
-      bz += bt * zt;
+      bz += rt * zt;
     }
     put_partial(bb, P0);
     put_partial(bz, P1);
@@ -373,7 +385,7 @@ __global__ void __launch_bounds__(kPT, 1) k_jcg(PArgs a) {
   // remaining Chebyshev steps of z = M^-1 r
   if (!done && m > 1) {
     for (int i = 1; i < m; ++i) {
-      vphase<kSrcX, STAGED>(a, o, 0.0f);
+      vphase<kSrcX, STAGED>(a, o, 0.0f, a.z);
       if (!grid_sync(a, gen)) return;
       if (i == m - 1) tphase_cheb<true, STAGED>(a, o, s_c1[i], s_c2[i], P2);
       else tphase_cheb<false, STAGED>(a, o, s_c1[i], s_c2[i], P2);
@@ -398,7 +410,7 @@ __global__ void __launch_bounds__(kPT, 1) k_jcg(PArgs a) {
   float bf = 0.0f;  // beta
   while (!done) {
     // u = W J^T (z + beta p)
-    vphase<kSrcZbP, STAGED>(a, o, bf);
+    vphase<kSrcZbP, STAGED>(a, o, bf, a.z);
     if (!grid_sync(a, gen)) return;
     // p = z + beta p; ap = A p; partials of p.Ap
     tphase_ap<STAGED>(a, o, bf, P0);
@@ -464,7 +476,7 @@ __global__ void __launch_bounds__(kPT, 1) k_jcg(PArgs a) {
     if (s_stop) break;
     if (m > 1) {
       for (int i = 1; i < m; ++i) {
-        vphase<kSrcX, STAGED>(a, o, 0.0f);
+        vphase<kSrcX, STAGED>(a, o, 0.0f, a.z);
         if (!grid_sync(a, gen)) return;
         if (i == m - 1) tphase_cheb<true, STAGED>(a, o, s_c1[i], s_c2[i], P2);
         else tphase_cheb<false, STAGED>(a, o, s_c1[i], s_c2[i], P2);
@@ -585,7 +597,7 @@ JcgPlan jcg_plan(const std::vector<int32_t>& inc_ptr, int32_t nv, int32_t nt) {
 
 void launch_jcg_persistent(const JView& j, const JcgVecs& v, const JcgPlan& plan,
                            const int32_t* part_dev, const JState* js, CgState* st, double tol_abs,
-                           double tol_rel, int maxiter, int degree, double spin_limit_s,
+                           double tol_rel, int maxiter, int degree, bool warm, double spin_limit_s,
                            cudaStream_t s) {
   require(degree >= 1 && degree <= kMaxCheb, MGPBD_EINVAL, "Chebyshev degree out of range");
   require(plan.grid > 0, MGPBD_ESTATE, "persistent CG plan not built");
@@ -624,6 +636,7 @@ void launch_jcg_persistent(const JView& j, const JcgVecs& v, const JcgPlan& plan
   a.tol_rel = tol_rel;
   a.maxiter = maxiter;
   a.degree = degree;
+  a.warm = warm ? 1 : 0;
   a.spin_ns = static_cast<unsigned long long>(spin_limit_s * 1e9);
   MGPBD_CUDA(cudaMemsetAsync(v.gs, 0, sizeof(GridSync), s));
   MGPBD_CUDA(cudaMemsetAsync(st, 0, sizeof(CgState), s));

@@ -130,11 +130,13 @@ JcgPlan jcg_plan(const std::vector<int32_t>& inc_ptr, int32_t nv, int32_t nt);
 // The whole CG solve (init, iterations to the tolerance or maxiter, the
 // Chebyshev preconditioner of `degree`) as one cooperative kernel; st is
 // zeroed and then filled like the per-phase path fills it.  part_dev holds
-// plan.vb then plan.tb on the device (staged plans).  A barrier wait longer
-// than spin_limit_s sets MGPBD_STATUS_SYNC_TIMEOUT in st->status.
+// plan.vb then plan.tb on the device (staged plans).  warm: start from the
+// x on entry (r = b - A x) instead of 0; the tolerance stays relative to
+// |b|.  A barrier wait longer than spin_limit_s sets
+// MGPBD_STATUS_SYNC_TIMEOUT in st->status.
 void launch_jcg_persistent(const JView& j, const JcgVecs& v, const JcgPlan& plan,
                            const int32_t* part_dev, const JState* js, CgState* st, double tol_abs,
-                           double tol_rel, int maxiter, int degree, double spin_limit_s,
+                           double tol_rel, int maxiter, int degree, bool warm, double spin_limit_s,
                            cudaStream_t s);
 
 // Work vectors of the primal persistent CG (pcg.cu): vertex vectors are
@@ -154,12 +156,14 @@ struct PcgVecs {
 bool pcg_plan_fits(JcgPlan& plan);
 int pcg_unstaged_grid();
 // The dual solve A dlam = b by CG on the primal system K y = J^T alpha~^-1 b
-// (one cooperative kernel; see pcg.cu).  st is zeroed and then filled like
-// the dual path fills it (iters = primal CG iterations).
+// (one cooperative kernel; see pcg.cu), stopping on the dual residual
+// (tol_abs, tol_rel |b|), on maxiter, or, with stall_its > 0, once the dual
+// residual has not fallen by 10 % for stall_its iterations.  st is zeroed
+// and then filled like the dual path fills it (iters = primal iterations).
 void launch_pcg_primal(const JView& j, const PcgVecs& v, const JcgPlan& plan,
                        const int32_t* part_dev, CgState* st, double tol_abs, double tol_rel,
-                       int maxiter, int degree, float cheb_lo, double spin_limit_s,
-                       cudaStream_t s);
+                       int maxiter, int degree, float cheb_lo, int stall_its,
+                       double spin_limit_s, cudaStream_t s);
 
 // deterministic start vector of the power iteration
 void launch_seed(float* v, int32_t n, cudaStream_t s);

@@ -73,6 +73,8 @@ struct QArgs {
   double tol_abs, tol_rel;
   int32_t maxiter, degree;
   float cheb_lo;
+  int32_t stall_its;  // > 0: stop once the dual residual has not fallen by
+                      // 10 % for this many iterations
   unsigned long long spin_ns;
 };
 
@@ -88,7 +90,8 @@ struct Own {
 
 // thread-0 state of the solve (identical in every block)
 struct Ctl {
-  double bb, tol2, rz, pap, alpha, beta, rres;
+  double bb, tol2, rz, pap, alpha, beta, rres, best;
+  int32_t since;  // iterations since the dual residual last fell by 10 %
   double ca[kBoot], cb[kBoot];  // bootstrap CG coefficients
   float c1[kMaxCheb], c2[kMaxCheb];
   float inv_theta, al, be;
@@ -436,6 +439,8 @@ __global__ void __launch_bounds__(kPT, 1) k_pcg(QArgs a) {
     o.w = nullptr;
   }
   if (threadIdx.x == 0) {
+    c.best = 1e300;
+    c.since = 0;
     c.iters = 0;
     c.nboot = 0;
     c.stop = 0;
@@ -500,6 +505,13 @@ __global__ void __launch_bounds__(kPT, 1) k_pcg(QArgs a) {
           } else if (c.iters >= a.maxiter) {
             c.status |= MGPBD_STATUS_CG_MAXITER;
             c.stop = 1;
+          } else if (a.stall_its > 0) {
+            if (se < 0.81 * c.best) {
+              c.best = se;
+              c.since = 0;
+            } else if (++c.since >= a.stall_its) {
+              c.stop = 1;
+            }
           }
         }
       }
@@ -765,8 +777,8 @@ int pcg_unstaged_grid() {
 
 void launch_pcg_primal(const JView& j, const PcgVecs& v, const JcgPlan& plan,
                        const int32_t* part_dev, CgState* st, double tol_abs, double tol_rel,
-                       int maxiter, int degree, float cheb_lo, double spin_limit_s,
-                       cudaStream_t s) {
+                       int maxiter, int degree, float cheb_lo, int stall_its,
+                       double spin_limit_s, cudaStream_t s) {
   require(degree >= 1 && degree <= kMaxCheb, MGPBD_EINVAL, "Chebyshev degree out of range");
   require(plan.grid > 0, MGPBD_ESTATE, "persistent CG plan not built");
   require(4LL * plan.grid <= v.partials_capacity, MGPBD_ERANGE, "partials buffer too small");
@@ -806,6 +818,7 @@ void launch_pcg_primal(const JView& j, const PcgVecs& v, const JcgPlan& plan,
   a.maxiter = maxiter;
   a.degree = degree;
   a.cheb_lo = cheb_lo;
+  a.stall_its = stall_its;
   a.spin_ns = static_cast<unsigned long long>(spin_limit_s * 1e9);
   MGPBD_CUDA(cudaMemsetAsync(v.gs, 0, sizeof(GridSync), s));
   MGPBD_CUDA(cudaMemsetAsync(st, 0, sizeof(CgState), s));

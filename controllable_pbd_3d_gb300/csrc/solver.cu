@@ -224,8 +224,13 @@ void Solver::init() {
   upload(inc_ent_, ie, s);
   if (cheb() && p_.persistent) {
     jplan_ = jcg_plan(ip, nv_, nt_);
-    if (primal() && jplan_.staged && !pcg_plan_fits(jplan_)) jplan_.staged = false;
-    if (primal() && !jplan_.staged) jplan_.grid = pcg_unstaged_grid();
+    if (primal()) {
+      pplan_ = jplan_;
+      if (!pplan_.staged || !pcg_plan_fits(pplan_)) {
+        pplan_.staged = false;
+        pplan_.grid = pcg_unstaged_grid();
+      }
+    }
     if (jplan_.staged) {
       std::vector<int32_t> part(jplan_.vb);
       part.insert(part.end(), jplan_.tb.begin(), jplan_.tb.end());
@@ -251,7 +256,7 @@ void Solver::init() {
   if (cheb() && p_.persistent) {
     stats_.cg_path = jplan_.staged ? MGPBD_CGPATH_STAGED : MGPBD_CGPATH_PERSISTENT;
     if (primal())
-      stats_.cg_path = jplan_.staged ? MGPBD_CGPATH_PRIMAL_STAGED : MGPBD_CGPATH_PRIMAL;
+      stats_.cg_path = pplan_.staged ? MGPBD_CGPATH_PRIMAL_STAGED : MGPBD_CGPATH_PRIMAL;
     stats_.cg_grid = jplan_.grid;
   }
   for (int32_t l = 0; l < n_levels() && l < 8; ++l) {
@@ -466,7 +471,6 @@ void Solver::jform_setup() {
   constexpr int kSteps = 24;
   JView j = jview();
   launch_jform_prepare(j, inc_ent_.p, gV_.p, jdinv_.p, stream_);
-  if (primal()) return;  // the primal kernel estimates its own spectrum
   launch_jform_lanczos(j, pw_v_.p, jd_.p, pw_w_.p, partials_.p, jst_.p, kSteps, stream_);
   static_assert(2 * kMaxLanczos <= 64, "h_buf_ holds the Lanczos coefficients");
   MGPBD_CUDA(cudaMemcpyAsync(h_buf_, jst_.p->lz_a, sizeof(double) * kMaxLanczos,
@@ -484,34 +488,49 @@ void Solver::jform_setup() {
 int32_t Solver::pcg_cheb(const float* b, float* x) {
   cudaStream_t outer = stream_;
   constexpr double kBarrierLimitS = 4.0;
-  if (primal()) {
-    PcgVecs v;
-    v.b = b;
-    v.dlam = x;
-    v.y = pv_[0].p;
-    v.yc = pv_[1].p;
-    v.r = pv_[2].p;
-    v.z = pv_[3].p;
-    v.d = pv_[4].p;
-    v.p = pv_[5].p;
-    v.q = pv_[6].p;
-    v.rhs = pv_[7].p;
-    v.bi0 = pv_[8].p;
-    v.bi1 = pv_[9].p;
-    v.s = ps_.p;
-    v.partials = partials_.p;
-    v.partials_capacity = static_cast<int64_t>(kMaxReduceBlocks) * 16;
-    v.gs = jgs_.p;
-    launch_pcg_primal(jview(), v, jplan_, jpart_.p, cg_state_.p, p_.tol_cg, p_.rel_tol_cg,
-                      p_.maxiter_cg, p_.cheb_degree, p_.cheb_lo, kBarrierLimitS, outer);
-    sync_read(h_state_, cg_state_.p, sizeof(CgState));
-    if (static_cast<uint32_t>(h_state_->status) & MGPBD_STATUS_SYNC_TIMEOUT)
-      throw Error(MGPBD_ECUDA, "primal CG kernel: a grid barrier wait timed out");
-    status_ |= static_cast<uint32_t>(h_state_->status);
-    return h_state_->iters;
-  }
   if (p_.persistent) {
-    // one cooperative kernel for the whole solve
+    int32_t its = 0, left = p_.maxiter_cg;
+    bool warm = false;
+    if (primal()) {
+      // warm start: CG on the primal system to a loose dual residual (or
+      // until it stalls), dlam = alpha~^-1 (b - J y) into x
+      constexpr int kPrimalStall = 16;
+      PcgVecs v;
+      v.b = b;
+      v.dlam = x;
+      v.y = pv_[0].p;
+      v.yc = pv_[1].p;
+      v.r = pv_[2].p;
+      v.z = pv_[3].p;
+      v.d = pv_[4].p;
+      v.p = pv_[5].p;
+      v.q = pv_[6].p;
+      v.rhs = pv_[7].p;
+      v.bi0 = pv_[8].p;
+      v.bi1 = pv_[9].p;
+      v.s = ps_.p;
+      v.partials = partials_.p;
+      v.partials_capacity = static_cast<int64_t>(kMaxReduceBlocks) * 16;
+      v.gs = jgs_.p;
+      const double tol = std::max<double>(p_.primal_tol, p_.rel_tol_cg);
+      launch_pcg_primal(jview(), v, pplan_, jpart_.p, cg_state_.p, p_.tol_cg, tol, p_.maxiter_cg,
+                        p_.cheb_degree, p_.cheb_lo, kPrimalStall, kBarrierLimitS, outer);
+      sync_read(h_state_, cg_state_.p, sizeof(CgState));
+      const uint32_t st = static_cast<uint32_t>(h_state_->status);
+      if (st & MGPBD_STATUS_SYNC_TIMEOUT)
+        throw Error(MGPBD_ECUDA, "primal CG kernel: a grid barrier wait timed out");
+      // the dual solve below decides convergence; keep only the alarms
+      status_ |= st & (MGPBD_STATUS_NAN | MGPBD_STATUS_PAP_NONPOS);
+      if (st & MGPBD_STATUS_NAN) return h_state_->iters;
+      its = h_state_->iters;
+      left = p_.maxiter_cg - its;
+      warm = true;
+      if (left <= 0) {
+        status_ |= MGPBD_STATUS_CG_MAXITER;
+        return its;
+      }
+    }
+    // one cooperative kernel for the (rest of the) solve
     JcgVecs v;
     v.b = b;
     v.x = x;
@@ -525,12 +544,12 @@ int32_t Solver::pcg_cheb(const float* b, float* x) {
     v.partials_capacity = static_cast<int64_t>(kMaxReduceBlocks) * 16;
     v.gs = jgs_.p;
     launch_jcg_persistent(jview(), v, jplan_, jpart_.p, jst_.p, cg_state_.p, p_.tol_cg,
-                          p_.rel_tol_cg, p_.maxiter_cg, p_.cheb_degree, kBarrierLimitS, outer);
+                          p_.rel_tol_cg, left, p_.cheb_degree, warm, kBarrierLimitS, outer);
     sync_read(h_state_, cg_state_.p, sizeof(CgState));
     if (static_cast<uint32_t>(h_state_->status) & MGPBD_STATUS_SYNC_TIMEOUT)
       throw Error(MGPBD_ECUDA, "persistent CG kernel: a grid barrier wait timed out");
     status_ |= static_cast<uint32_t>(h_state_->status);
-    return h_state_->iters;
+    return its + h_state_->iters;
   }
   if (!p_.use_graph) {
     // same kernels from the host; every kernel is a no-op once done is set

@@ -147,6 +147,7 @@ class Solver {
   DevBuf<float> jxc_, jrf_;  // persistent CG: Kahan term of x, float32 residual
   DevBuf<GridSync> jgs_;
   JcgPlan jplan_;          // persistent CG work split
+  JcgPlan pplan_;          // the same for the primal warm start
   DevBuf<float4> pv_[10];  // primal CG vertex vectors
   DevBuf<float> ps_;       // primal CG tet scratch
   bool primal() const { return cheb() && p_.persistent && p_.primal; }

@@ -91,9 +91,9 @@ class MGPBDSolverGPU:
                    (False: the same kernels from a host loop);
     persistent     FAST + 'cheb': each CG solve is one cooperative persistent
                    kernel (False: one kernel per phase, per use_graph);
-    primal         FAST + 'cheb' + persistent: solve the dual system through
-                   the vertex-space system K y = J^T alpha~^-1 b (Woodbury),
-                   same stopping test on the dual residual.
+    primal         FAST + 'cheb' + persistent: warm-start each solve through
+                   the vertex-space system K y = J^T alpha~^-1 b (Woodbury)
+                   to a dual residual of primal_tol |b|, then CG on A;
   """
 
   def __init__(self, v_p, v_p_ref, v_invm, t_i, t_m, gravity, dt, mu=1e6, damp=1.0, maxiter=20,
@@ -103,7 +103,7 @@ class MGPBDSolverGPU:
                coarse_solver='jacobi', smoother='jacobi', max_levels=0, max_coarse=400,
                kinematic_pins=False, coarse_sweeps=0, cg_alias=False, compliance=0.0,
                precond='vcycle', cheb_degree=8, cheb_lo=0.01, use_graph=True,
-               persistent=True, primal=False, check_finite=True):
+               persistent=True, primal=False, primal_tol=1e-2, check_finite=True):
     if aggregation != 'tet':
       raise NotImplementedError(
           "aggregation='pyamg' needs PyAMG's smoothed-aggregation setup, which this "
@@ -171,6 +171,7 @@ class MGPBDSolverGPU:
     p.use_graph = int(bool(use_graph))
     p.persistent = int(bool(persistent))
     p.primal = int(bool(primal))
+    p.primal_tol = float(primal_tol)
     self.params = p
     h = C.c_void_p()
     N.check(self._lib.mgpbd_create(C.byref(p), C.byref(h)), 'mgpbd_create')

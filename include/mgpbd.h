@@ -119,15 +119,18 @@ typedef struct mgpbd_params {
    * vectors, compensated solution sum); 0 runs the per-phase kernels
    * (use_graph selects graph or host loop for those). */
   int32_t persistent;
-  /* FAST mode, MGPBD_PRECOND_CHEB, persistent: 1 solves the dual system
-   * A dlam = b through the primal one, K y = J^T alpha~^-1 b with
-   * K = W^-1 + J^T alpha~^-1 J on the free vertices and dlam = alpha~^-1
-   * (b - J y) (Woodbury identity; block-Jacobi Chebyshev preconditioner,
-   * stopping on the same dual residual); 0 (default) runs CG on A itself.
-   * The primal solve starts from dlam = alpha~^-1 b, whose dual residual
-   * can exceed |b| by the stiffness ratio; in float32 some solves then stall
-   * short of a 1e-6 relative dual residual. */
+  /* FAST mode, MGPBD_PRECOND_CHEB, persistent: 1 warm-starts each solve
+   * through the primal system K y = J^T alpha~^-1 b with K = W^-1 +
+   * J^T alpha~^-1 J on the free vertices, dlam = alpha~^-1 (b - J y)
+   * (Woodbury identity; block-Jacobi Chebyshev preconditioner), run until
+   * the dual residual |b - A dlam| falls below primal_tol |b| or stalls;
+   * CG on A then continues from that dlam to the usual tolerance.  The
+   * primal start dlam = alpha~^-1 b can have a dual residual far above |b|
+   * (by the stiffness ratio), so in float32 the primal CG alone cannot
+   * always reach 1e-6; it does the coarse part of the work at about half
+   * the cost per unit of residual reduction.  0 (default): CG on A only. */
   int32_t primal;
+  float primal_tol;  /* relative dual residual of the hand-over (1e-2)     */
 } mgpbd_params;
 
 #define MGPBD_PRECOND_VCYCLE 0
