@@ -59,6 +59,7 @@ class Stats(C.Structure):
       ('newton_iters', i32), ('cg_iters_total', i32), ('cg_iters_last', i32), ('n_levels', i32),
       ('residual0', f64), ('residual', f64), ('omega_last', f64), ('status', C.c_uint32),
       ('nnz', i64 * 8), ('rows', i64 * 8), ('cg_path', i32), ('cg_grid', i32),
+      ('cg_iters_warm', i32), ('cg_launches', i32), ('ms_warm', f64), ('ms_dual', f64),
   ]
 
 

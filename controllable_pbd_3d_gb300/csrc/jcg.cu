@@ -99,10 +99,11 @@ __device__ __forceinline__ bool grid_sync(const PArgs& a, unsigned long long& ge
   return pdev::grid_sync(a.gs, &a.st->status, a.spin_ns, gen);
 }
 
-// sum_l g_{t,l} . u_{q_l} for tet t with indices q
+// sum_l g_{t,l} . u_{q_l} for tet t with indices q (a.gradC: the three
+// gradient planes)
 __device__ __forceinline__ float tdot(const TArgs& a, int64_t t, int4 q) {
-  const float4 g0 = __ldg(a.gradC + 3 * t), g1 = __ldg(a.gradC + 3 * t + 1),
-               g2 = __ldg(a.gradC + 3 * t + 2);
+  const float4 g0 = __ldg(a.gradC + t), g1 = __ldg(a.gradC + a.nt + t),
+               g2 = __ldg(a.gradC + 2LL * a.nt + t);
   const float4 u0 = a.u[q.x], u1 = a.u[q.y], u2 = a.u[q.z], u3 = a.u[q.w];
   return (g0.x * u0.x + g0.y * u0.y + g0.z * u0.z) + (g0.w * u1.x + g1.x * u1.y + g1.y * u1.z) +
          (g1.z * u2.x + g1.w * u2.y + g2.x * u2.z) + (g2.y * u3.x + g2.z * u3.y + g2.w * u3.z);
@@ -605,7 +606,8 @@ void launch_jcg_persistent(const JView& j, const JcgVecs& v, const JcgPlan& plan
   require(!plan.staged || part_dev != nullptr, MGPBD_ESTATE, "staged plan without partition");
   PArgs a;
   a.ta.t_i = reinterpret_cast<const int4*>(j.t_i);
-  a.ta.gradC = reinterpret_cast<const float4*>(j.gradC);
+  require(j.gT != nullptr, MGPBD_ESTATE, "persistent CG needs the gradient planes");
+  a.ta.gradC = j.gT;
   a.ta.u = j.u;
   a.ta.alpha = j.alpha;
   a.ta.dinv = j.dinv;

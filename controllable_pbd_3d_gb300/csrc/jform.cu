@@ -24,7 +24,7 @@ constexpr int kT = 256;  // threads per block
 __global__ void k_jprep(const int32_t* __restrict__ inc_ent, const float* __restrict__ gradC,
                         const int4* __restrict__ t_i, const float* __restrict__ invm,
                         const float* __restrict__ alpha, int32_t nt, float4* __restrict__ gV,
-                        float* __restrict__ dinv) {
+                        float* __restrict__ dinv, float4* __restrict__ gT) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < 4LL * nt; k += stride) {
     const int32_t e = inc_ent[k];
@@ -41,6 +41,12 @@ __global__ void k_jprep(const int32_t* __restrict__ inc_ent, const float* __rest
       d += w[l] * (g[3 * l] * g[3 * l] + g[3 * l + 1] * g[3 * l + 1] + g[3 * l + 2] * g[3 * l + 2]);
     d += alpha[t];
     dinv[t] = fabsf(d) > 1e-30f ? 1.0f / d : 0.0f;
+    if (gT) {
+      const float4* g4 = reinterpret_cast<const float4*>(g);
+      gT[t] = g4[0];
+      gT[nt + t] = g4[1];
+      gT[2LL * nt + t] = g4[2];
+    }
   }
 }
 
@@ -416,10 +422,10 @@ TArgs targs(const JView& j) {
 }  // namespace
 
 void launch_jform_prepare(const JView& j, const int32_t* inc_ent, float4* gV, float* dinv,
-                          cudaStream_t s) {
+                          float4* gT, cudaStream_t s) {
   int g = tgrid(4LL * j.nt);
   k_jprep<<<g, kT, 0, s>>>(inc_ent, j.gradC, reinterpret_cast<const int4*>(j.t_i), j.invm, j.alpha,
-                           j.nt, gV, dinv);
+                           j.nt, gV, dinv, gT);
   MGPBD_CHECK_LAUNCH();
 }
 

@@ -48,6 +48,7 @@ struct JView {
   int32_t nt = 0, nv = 0;
   const int32_t* t_i = nullptr;      // (nt, 4)
   const float* gradC = nullptr;      // (nt, 4, 3)
+  const float4* gT = nullptr;        // gradC as 3 planes of nt float4 (persistent CG)
   const float4* gV = nullptr;        // (4 nt) vertex-major (g, tet id)
   const int32_t* inc_ptr = nullptr;  // (nv + 1)
   const float* invm = nullptr;       // (nv)
@@ -56,9 +57,12 @@ struct JView {
   float4* u = nullptr;               // (nv) vertex scratch
 };
 
-// gV[k] = (gradC[inc_ent[k]], tet id) and 1/diag(A) per tet
+// gV[k] = (gradC[inc_ent[k]], tet id) and 1/diag(A) per tet; with gT, also
+// the gradients as three planes (gT[t], gT[nt + t], gT[2 nt + t] = the
+// float4s 0, 1, 2 of tet t), so a warp's loads of one float4 per tet are
+// contiguous
 void launch_jform_prepare(const JView& j, const int32_t* inc_ent, float4* gV, float* dinv,
-                          cudaStream_t s);
+                          float4* gT, cudaStream_t s);
 // y = A x (plain), for tests and the power iteration
 void launch_jform_apply(const JView& j, const float* x, float* y, cudaStream_t s);
 // `steps` Lanczos steps on S = D^-1/2 A D^-1/2 from a fixed start vector;
@@ -94,7 +98,7 @@ void launch_jcg_cheb_steps(const JView& j, const JVecs& v, JState* js, CgState* 
 // test, z = M^-1 r, beta (all kernels are no-ops once st->done)
 void launch_jcg_body(const JView& j, const JVecs& v, JState* js, CgState* st, int degree,
                      cudaStream_t s);
-// Grid barrier state of the persistent CG kernel (zeroed before each launch)
+// Grid barrier state of the persistent CG kernels (zeroed before each launch)
 struct GridSync {
   unsigned long long count;  // arrivals; barrier n completes at n * grid
   unsigned int err;          // 1: a block gave up waiting

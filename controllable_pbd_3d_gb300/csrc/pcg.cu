@@ -54,7 +54,7 @@ constexpr int kBoot = 24; // block-Jacobi PCG iterations that estimate lambda_ma
 struct QArgs {
   int32_t nt, nv;
   const int4* t_i;
-  const float4* gradC;  // 3 float4 per tet: the 12 gradient entries
+  const float4* gradC;  // the 12 gradient entries as three planes of nt float4
   const float* alpha;   // alpha~
   const float* invm;
   const int32_t* inc_ptr;
@@ -141,8 +141,8 @@ __device__ __forceinline__ void tphase(const QArgs& a, const Own& o, float beta,
       e[i] = 0.0f;
       if (t < o.tend) {
         const int4 q = tet_q<STAGED>(a, o, t);
-        const float4 g0 = __ldg(a.gradC + 3 * t), g1 = __ldg(a.gradC + 3 * t + 1),
-                     g2 = __ldg(a.gradC + 3 * t + 2);
+        const float4 g0 = __ldg(a.gradC + t), g1 = __ldg(a.gradC + a.nt + t),
+                     g2 = __ldg(a.gradC + 2LL * a.nt + t);
         float3 v0 = f3(V[q.x]), v1 = f3(V[q.y]), v2 = f3(V[q.z]), v3 = f3(V[q.w]);
         if (MODE == kT1) {
           const float3 p0 = f3(a.p[q.x]), p1 = f3(a.p[q.y]), p2 = f3(a.p[q.z]), p3 = f3(a.p[q.w]);
@@ -787,7 +787,8 @@ void launch_pcg_primal(const JView& j, const PcgVecs& v, const JcgPlan& plan,
   a.nt = j.nt;
   a.nv = j.nv;
   a.t_i = reinterpret_cast<const int4*>(j.t_i);
-  a.gradC = reinterpret_cast<const float4*>(j.gradC);
+  require(j.gT != nullptr, MGPBD_ESTATE, "persistent CG needs the gradient planes");
+  a.gradC = j.gT;
   a.alpha = j.alpha;
   a.invm = j.invm;
   a.inc_ptr = j.inc_ptr;

@@ -125,6 +125,16 @@ Solver::~Solver() {
   if (h_buf_) cudaFreeHost(h_buf_);
   if (h_state_) cudaFreeHost(h_state_);
   if (h_cf_) cudaFreeHost(h_cf_);
+  for (cudaEvent_t e : ev_)
+    if (e) cudaEventDestroy(e);
+}
+
+// elapsed time between two events recorded on the solver stream, once the
+// second has completed (the callers have synchronised)
+double Solver::event_ms(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.0f;
+  MGPBD_CUDA(cudaEventElapsedTime(&ms, a, b));
+  return ms;
 }
 
 void Solver::require_init() const {
@@ -173,6 +183,8 @@ void Solver::init() {
   if (!h_buf_) MGPBD_CUDA(cudaMallocHost(&h_buf_, sizeof(double) * 64));
   if (!h_state_) MGPBD_CUDA(cudaMallocHost(&h_state_, sizeof(CgState)));
   if (!h_cf_) MGPBD_CUDA(cudaMallocHost(&h_cf_, sizeof(ChebCoef)));
+  for (cudaEvent_t& e : ev_)
+    if (!e) MGPBD_CUDA(cudaEventCreate(&e));
   x_old_.alloc(3LL * nv_);
   x_pred_.alloc(3LL * nv_);
   dpos_.alloc(3LL * nv_);
@@ -398,6 +410,7 @@ void Solver::alloc_work() {
     jxc_.alloc(nt_);
     jrf_.alloc(nt_);
     jgs_.alloc(1);
+    if (p_.persistent) gT_.alloc(3LL * nt_);
     if (primal()) {
       for (auto& b : pv_) {
         b.alloc(nv_);
@@ -415,7 +428,7 @@ void Solver::apply_matrix(int matrix_free, const float* x, float* y) {
   require_init();
   if (matrix_free) {
     JView j = jview();
-    if (matrix_free == 1) launch_jform_prepare(j, inc_ent_.p, gV_.p, jdinv_.p, stream_);
+    if (matrix_free == 1) launch_jform_prepare(j, inc_ent_.p, gV_.p, jdinv_.p, gT_.p, stream_);
     launch_jform_apply(j, x, y, stream_);
   } else {
     launch_spmv(levels_[0].view(), x, y, stream_);
@@ -440,6 +453,7 @@ JView Solver::jview() {
   j.nv = nv_;
   j.t_i = t_i_;
   j.gradC = gradC_.p;
+  j.gT = gT_.p;
   j.gV = gV_.p;
   j.inc_ptr = inc_ptr_.p;
   j.invm = invm_;
@@ -470,7 +484,7 @@ JVecs Solver::jvecs(const float* b, float* x) {
 void Solver::jform_setup() {
   constexpr int kSteps = 24;
   JView j = jview();
-  launch_jform_prepare(j, inc_ent_.p, gV_.p, jdinv_.p, stream_);
+  launch_jform_prepare(j, inc_ent_.p, gV_.p, jdinv_.p, gT_.p, stream_);
   launch_jform_lanczos(j, pw_v_.p, jd_.p, pw_w_.p, partials_.p, jst_.p, kSteps, stream_);
   static_assert(2 * kMaxLanczos <= 64, "h_buf_ holds the Lanczos coefficients");
   MGPBD_CUDA(cudaMemcpyAsync(h_buf_, jst_.p->lz_a, sizeof(double) * kMaxLanczos,
@@ -513,9 +527,14 @@ int32_t Solver::pcg_cheb(const float* b, float* x) {
       v.partials_capacity = static_cast<int64_t>(kMaxReduceBlocks) * 16;
       v.gs = jgs_.p;
       const double tol = std::max<double>(p_.primal_tol, p_.rel_tol_cg);
+      MGPBD_CUDA(cudaEventRecord(ev_[0], outer));
       launch_pcg_primal(jview(), v, pplan_, jpart_.p, cg_state_.p, p_.tol_cg, tol, p_.maxiter_cg,
                         p_.cheb_degree, p_.cheb_lo, kPrimalStall, kBarrierLimitS, outer);
+      MGPBD_CUDA(cudaEventRecord(ev_[1], outer));
       sync_read(h_state_, cg_state_.p, sizeof(CgState));
+      stats_.ms_warm += event_ms(ev_[0], ev_[1]);
+      stats_.cg_launches += 1;
+      stats_.cg_iters_warm += h_state_->iters;
       const uint32_t st = static_cast<uint32_t>(h_state_->status);
       if (st & MGPBD_STATUS_SYNC_TIMEOUT)
         throw Error(MGPBD_ECUDA, "primal CG kernel: a grid barrier wait timed out");
@@ -543,9 +562,13 @@ int32_t Solver::pcg_cheb(const float* b, float* x) {
     v.partials = partials_.p;
     v.partials_capacity = static_cast<int64_t>(kMaxReduceBlocks) * 16;
     v.gs = jgs_.p;
+    MGPBD_CUDA(cudaEventRecord(ev_[0], outer));
     launch_jcg_persistent(jview(), v, jplan_, jpart_.p, jst_.p, cg_state_.p, p_.tol_cg,
                           p_.rel_tol_cg, left, p_.cheb_degree, warm, kBarrierLimitS, outer);
+    MGPBD_CUDA(cudaEventRecord(ev_[1], outer));
     sync_read(h_state_, cg_state_.p, sizeof(CgState));
+    stats_.ms_dual += event_ms(ev_[0], ev_[1]);
+    stats_.cg_launches += 1;
     if (static_cast<uint32_t>(h_state_->status) & MGPBD_STATUS_SYNC_TIMEOUT)
       throw Error(MGPBD_ECUDA, "persistent CG kernel: a grid barrier wait timed out");
     status_ |= static_cast<uint32_t>(h_state_->status);
@@ -976,6 +999,10 @@ void Solver::solve(int32_t frame) {
   stats_.cg_iters_total = 0;
   stats_.cg_iters_last = 0;
   stats_.omega_last = 1.0;
+  stats_.cg_iters_warm = 0;
+  stats_.cg_launches = 0;
+  stats_.ms_warm = 0.0;
+  stats_.ms_dual = 0.0;
   log_.clear();
   auto now = [] {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();

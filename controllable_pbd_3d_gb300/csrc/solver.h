@@ -131,6 +131,8 @@ class Solver {
   double* h_buf_ = nullptr;    // pinned host scratch
   CgState* h_state_ = nullptr;
   ChebCoef* h_cf_ = nullptr;   // pinned staging of the Chebyshev coefficients
+  cudaEvent_t ev_[2] = {nullptr, nullptr};  // around each persistent CG launch
+  static double event_ms(cudaEvent_t a, cudaEvent_t b);
 
   // captured CG loop (FAST mode)
   cudaGraphExec_t cg_exec_ = nullptr;
@@ -146,6 +148,7 @@ class Solver {
   DevBuf<JState> jst_;
   DevBuf<float> jxc_, jrf_;  // persistent CG: Kahan term of x, float32 residual
   DevBuf<GridSync> jgs_;
+  DevBuf<float4> gT_;      // persistent CG: gradients as three planes
   JcgPlan jplan_;          // persistent CG work split
   JcgPlan pplan_;          // the same for the primal warm start
   DevBuf<float4> pv_[10];  // primal CG vertex vectors

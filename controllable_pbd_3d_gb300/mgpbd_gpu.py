@@ -245,7 +245,8 @@ class MGPBDSolverGPU:
         'residual': s.residual, 'omega_last': s.omega_last, 'status': s.status,
         'rows': list(s.rows[:nl]), 'nnz': list(s.nnz[:nl]),
         'cg_path': ('kernels', 'persistent', 'staged', 'primal', 'primal-staged')[s.cg_path],
-        'cg_grid': s.cg_grid,
+        'cg_grid': s.cg_grid, 'cg_iters_warm': s.cg_iters_warm, 'cg_launches': s.cg_launches,
+        'ms_warm': s.ms_warm, 'ms_dual': s.ms_dual,
     }
 
   def newton_log(self):

@@ -149,6 +149,10 @@ typedef struct mgpbd_stats {
   int64_t rows[8];          /* rows per level                                 */
   int32_t cg_path;          /* MGPBD_CGPATH_* the CG solves run on            */
   int32_t cg_grid;          /* blocks of the persistent kernel (0 otherwise)  */
+  int32_t cg_iters_warm;    /* of cg_iters_total: primal warm-start iterations */
+  int32_t cg_launches;      /* persistent kernel launches in the last solve   */
+  double ms_warm;           /* GPU time of the primal warm-start kernels and  */
+  double ms_dual;           /* of the dual persistent kernels, last solve     */
 } mgpbd_stats;
 
 #define MGPBD_CGPATH_KERNELS 0      /* one kernel (or graph node) per operation */
