@@ -79,6 +79,7 @@ struct PArgs {
   double tol_abs, tol_rel;
   int32_t maxiter, degree;
   int32_t warm;  // 1: start from the x on entry instead of 0
+  float4* ulo;   // warm start: low part of u (u = a.u + ulo, float64 sums)
   unsigned long long spin_ns;
 };
 
@@ -113,6 +114,83 @@ template <bool STAGED>
 __device__ __forceinline__ int4 tet_q(const PArgs& a, const Own& o, int64_t t) {
   if (STAGED) return o.q[t - o.tb0];
   return a.ta.t_i[t];
+}
+
+// Warm start, vertex phase in float64: u_v = w_v sum x_t g_{t,l} summed in
+// float64 and stored as a float pair (a.u = rounded sum, a.ulo = the rest).
+// The residual b - A x of a good start x is a small difference of large
+// terms; float32 sums would bury it in their rounding (~1e-7 of the terms),
+// and CG would then converge to the wrong target.  Runs once per solve.
+template <bool STAGED>
+__device__ __forceinline__ void vphase_warm(const PArgs& a, const Own& o) {
+  const int lane = threadIdx.x % 4;
+  int64_t gidx, ngroups, nloop;
+  if (STAGED) {
+    gidx = threadIdx.x / 4;
+    ngroups = blockDim.x / 4;
+    nloop = o.nvb;
+  } else {
+    gidx = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / 4;
+    ngroups = (int64_t)gridDim.x * blockDim.x / 4;
+    nloop = a.nv;
+  }
+  for (int64_t base = 0; base < nloop; base += ngroups) {
+    const int64_t lv = base + gidx;
+    float w = 0.0f;
+    int32_t k0 = 0, k1 = 0;
+    if (lv < nloop) {
+      if (STAGED) {
+        w = o.w[lv];
+        k0 = o.off[lv];
+        k1 = o.off[lv + 1] - 1;
+      } else {
+        w = a.invm[lv];
+        k0 = a.inc_ptr[lv];
+        k1 = a.inc_ptr[lv + 1];
+      }
+    }
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    for (int32_t k = k0 + lane; k < k1; k += 4) {
+      const float4 g = STAGED ? o.e[k] : __ldg(a.gV + k);
+      const double xt = a.x[__float_as_int(g.w)];
+      sx += xt * g.x;
+      sy += xt * g.y;
+      sz += xt * g.z;
+    }
+#pragma unroll
+    for (int sh = 2; sh > 0; sh >>= 1) {
+      sx += __shfl_xor_sync(0xffffffffu, sx, sh, 4);
+      sy += __shfl_xor_sync(0xffffffffu, sy, sh, 4);
+      sz += __shfl_xor_sync(0xffffffffu, sz, sh, 4);
+    }
+    if (lane == 0 && lv < nloop) {
+      const int64_t v = STAGED ? o.vb0 + lv : lv;
+      sx *= w;
+      sy *= w;
+      sz *= w;
+      const float hx = (float)sx, hy = (float)sy, hz = (float)sz;
+      a.u[v] = make_float4(hx, hy, hz, 0.0f);
+      a.ulo[v] = make_float4((float)(sx - hx), (float)(sy - hy), (float)(sz - hz), 0.0f);
+    }
+  }
+}
+
+// (A x)_t in float64 from the float pair u + ulo (warm start)
+template <bool STAGED>
+__device__ __forceinline__ double tdot_warm(const PArgs& a, const Own& o, int64_t t) {
+  const int4 q = tet_q<STAGED>(a, o, t);
+  const int32_t vs[4] = {q.x, q.y, q.z, q.w};
+  const float4 g0 = __ldg(a.ta.gradC + t), g1 = __ldg(a.ta.gradC + a.ta.nt + t),
+               g2 = __ldg(a.ta.gradC + 2LL * a.ta.nt + t);
+  const float gg[12] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w, g2.x, g2.y, g2.z, g2.w};
+  double acc = 0.0;
+#pragma unroll
+  for (int l = 0; l < 4; ++l) {
+    const float4 hi = a.u[vs[l]], lo = a.ulo[vs[l]];
+    acc += (double)gg[3 * l] * ((double)hi.x + lo.x) + (double)gg[3 * l + 1] * ((double)hi.y + lo.y) +
+           (double)gg[3 * l + 2] * ((double)hi.z + lo.z);
+  }
+  return acc + (double)__ldg(a.ta.alpha + t) * a.x[t];
 }
 
 // Vertex phase: u_v = w_v sum x_t g_{t,l} with x_t = src_t (+ beta p_t).
@@ -337,7 +415,7 @@ __global__ void __launch_bounds__(kPT, 1) k_jcg(PArgs a) {
   // x = 0 (or the warm start x0), r = b - A x, p = 0, z = d = D^-1 r / theta;
   // partials of b.b and r.z
   if (a.warm) {
-    vphase<kSrcX, STAGED>(a, o, 0.0f, a.x);
+    vphase_warm<STAGED>(a, o);
     if (!grid_sync(a, gen)) return;
   }
   {
@@ -346,8 +424,7 @@ __global__ void __launch_bounds__(kPT, 1) k_jcg(PArgs a) {
       const float bt = a.b[t];
       float rt = bt;
       if (a.warm) {
-        const float xt = a.x[t];
-        rt = bt - (tdot(a.ta, t, tet_q<STAGED>(a, o, t)) + __ldg(a.ta.alpha + t) * xt);
+        rt = (float)((double)bt - tdot_warm<STAGED>(a, o, t));
       } else {
         a.x[t] = 0.0f;
       }
@@ -639,6 +716,8 @@ void launch_jcg_persistent(const JView& j, const JcgVecs& v, const JcgPlan& plan
   a.maxiter = maxiter;
   a.degree = degree;
   a.warm = warm ? 1 : 0;
+  a.ulo = v.ulo;
+  require(!warm || v.ulo != nullptr, MGPBD_EINVAL, "warm start needs the ulo scratch");
   a.spin_ns = static_cast<unsigned long long>(spin_limit_s * 1e9);
   MGPBD_CUDA(cudaMemsetAsync(v.gs, 0, sizeof(GridSync), s));
   MGPBD_CUDA(cudaMemsetAsync(st, 0, sizeof(CgState), s));

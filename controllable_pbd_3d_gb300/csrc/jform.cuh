@@ -118,6 +118,7 @@ struct JcgVecs {
   double* partials = nullptr;
   int64_t partials_capacity = 0;  // doubles; needs 3 * the plan's grid
   GridSync* gs = nullptr;
+  float4* ulo = nullptr;  // warm start: nv float4 scratch
 };
 // Work split of the persistent kernel for one mesh on the current device:
 // the cooperative grid, and, when the block data fits in shared memory

@@ -562,6 +562,7 @@ int32_t Solver::pcg_cheb(const float* b, float* x) {
     v.partials = partials_.p;
     v.partials_capacity = static_cast<int64_t>(kMaxReduceBlocks) * 16;
     v.gs = jgs_.p;
+    v.ulo = primal() ? pv_[6].p : nullptr;  // the primal Kp vector, free by now
     MGPBD_CUDA(cudaEventRecord(ev_[0], outer));
     launch_jcg_persistent(jview(), v, jplan_, jpart_.p, jst_.p, cg_state_.p, p_.tol_cg,
                           p_.rel_tol_cg, left, p_.cheb_degree, warm, kBarrierLimitS, outer);

@@ -1,0 +1,70 @@
+"""Packing independent bodies into one block-diagonal MGPBD system."""
+
+import numpy as np
+import pytest
+
+from controllable_pbd_3d_gb300.batch import pack_bodies, random_bodies
+
+
+def test_pack_bodies_is_block_diagonal():
+  from oracle.mgpbd_oracle import sparsity_pattern
+  bodies = random_bodies(4, seed=3, dims=(2, 4))
+  xr, x0, invm, t_i, voff, toff = pack_bodies(bodies)
+  assert voff[-1] == len(xr) == len(x0) == len(invm)
+  assert toff[-1] * 4 == len(t_i)
+  t = t_i.reshape(-1, 4)
+  for b, body in enumerate(bodies):
+    tb = t[toff[b]:toff[b + 1]]
+    assert tb.min() >= voff[b] and tb.max() < voff[b + 1]
+    np.testing.assert_array_equal(tb - voff[b], body.t_i.reshape(-1, 4))
+  # the dual matrix couples tets only within a body
+  ip, ix = sparsity_pattern(t_i, len(t))
+  body_of = np.searchsorted(toff, np.arange(len(t)), side='right') - 1
+  rows = np.repeat(np.arange(len(t)), np.diff(ip))
+  np.testing.assert_array_equal(body_of[rows], body_of[ix])
+
+
+def test_random_bodies_ranges():
+  bodies = random_bodies(16, seed=0)
+  for b in bodies:
+    n = len(b.t_i) // 20  # 5 tets per hex
+    assert 6 ** 3 <= n <= 30 ** 3
+    assert 1e-8 <= b.compliance <= 1e-5
+    assert (b.invm == 0).any() and (b.invm == 1).any()
+
+
+@pytest.mark.gpu
+def test_batched_solve_equals_per_body_solves(cuda):
+  """One CG solve of the packed system gives every body the solution of
+  its own system (block diagonal), for bodies of different sizes and
+  compliances."""
+  from controllable_pbd_3d_gb300.batch import BodyBatch
+  from controllable_pbd_3d_gb300.mgpbd_gpu import MGPBDSolverGPU
+  g, dt = [0.0, -9.8, 0.0], 1 / 300
+  # the dual persistent solve (the primal warm start is for moderate
+  # stiffness; these bodies go down to compliance 1e-8)
+  kw = dict(mode='fast', precond='cheb', rel_tol_cg=1e-9, tol_cg=1e-14, maxiter_cg=6000,
+            primal=False)
+  bodies = random_bodies(3, seed=1, dims=(3, 7))
+
+  def first_solve(s):
+    s.make_prediction()
+    s.lambdaf.zero_()
+    s._compute_C_and_gradC()
+    s._residual_norm_gpu()
+    s._fill_A_and_update_gpu()
+    s._gpu_solver.solve(s._b_gpu, s._dlam_gpu)
+    return s._dlam_gpu.detach().cpu().numpy().copy()
+
+  batch = BodyBatch(bodies, g, dt, **kw)
+  batch.init()
+  dl = first_solve(batch.solver)
+  for b, body in enumerate(bodies):
+    x = cuda.tensor(body.x0, device='cuda')
+    s = MGPBDSolverGPU(x, cuda.tensor(body.x_ref, device='cuda'),
+                       cuda.tensor(body.invm, device='cuda'), cuda.tensor(body.t_i, device='cuda'),
+                       None, g, dt, compliance=body.compliance, **kw)
+    s.init()
+    ref = first_solve(s)
+    got = dl[batch.tet_off[b]:batch.tet_off[b + 1]]
+    assert float(np.abs(got - ref).max()) <= 1e-4 * float(np.abs(ref).max()), b

@@ -328,3 +328,48 @@ def test_fast_mode_matches_parity_mode(cuda):
     s2.step(k)
   assert float(np.abs(np_(x1) - np_(x2)).max()) <= 1e-6
   assert s1.stats()['cg_iters_total'] == s2.stats()['cg_iters_total']
+
+
+@pytest.mark.parametrize('path,comp', [('kernels', 2.7e-8), ('dual', 2.7e-8), ('dual', 1.5e-6),
+                                       ('primal', 1.5e-6), ('primal', 4.5e-7)])
+def test_cheb_solution_matches_direct_solve_on_stiff_body(cuda, path, comp):
+  """The first Newton system of a small stiff body (750 tets, cell size
+  1/40): the FAST solve's dlam against a float64 sparse direct solve of the
+  same system (built from the solver's own b and gradients), to 1e-4.  The
+  dual solves hold down to compliance 2.7e-8; the primal warm start only
+  where it is accurate (compliance >= ~4e-7 at this cell size: stiffer,
+  its hand-over leaves errors the float32 dual CG does not remove)."""
+  import scipy.sparse as sp
+  import scipy.sparse.linalg as spl
+  from controllable_pbd_3d_gb300 import meshgen
+  from controllable_pbd_3d_gb300.mgpbd_gpu import MGPBDSolverGPU
+  nx, ny, nz = 5, 5, 6
+  xr, t = meshgen.hex_grid_tets(nx, ny, nz, h=1 / 40)
+  x0, _ = meshgen.hex_grid_tets(nx, ny, nz, h=1 / 40, jitter=0.01, seed=9)
+  invm = np.ones(len(xr), np.float32)
+  invm[meshgen.grid_face_vertices(nx, ny, nz, axis=1, side='max')] = 0
+  dt = 1 / 300
+  s = MGPBDSolverGPU(cuda.tensor(x0, device='cuda'), cuda.tensor(xr, device='cuda'),
+                     cuda.tensor(invm, device='cuda'), cuda.tensor(t, device='cuda'), None,
+                     [0, -9.8, 0], dt, compliance=comp, mode='fast', precond='cheb',
+                     rel_tol_cg=1e-9, tol_cg=1e-14, maxiter_cg=6000, **CHEB_PATHS[path])
+  s.init()
+  s.make_prediction()
+  s.lambdaf.zero_()
+  s._compute_C_and_gradC()
+  s._residual_norm_gpu()
+  s._fill_A_and_update_gpu()
+  s._gpu_solver.solve(s._b_gpu, s._dlam_gpu)
+  b = np_(s._b_gpu).astype(np.float64)
+  g = np_(s.gradC).astype(np.float64)
+  nt, nv = len(t) // 4, len(xr)
+  tt = t.reshape(nt, 4)
+  rows = np.repeat(np.arange(nt), 12)
+  cols = (3 * tt[:, :, None] + np.arange(3)[None, None, :]).reshape(-1)
+  J = sp.csr_matrix((g.reshape(-1), (rows, cols)), shape=(nt, 3 * nv))
+  A = (J @ sp.diags(np.repeat(invm.astype(np.float64), 3)) @ J.T +
+       sp.diags(np.full(nt, comp / dt / dt))).tocsc()
+  exact = spl.spsolve(A, b)
+  got = np_(s._dlam_gpu).astype(np.float64)
+  err = float(np.abs(got - exact).max() / np.abs(exact).max())
+  assert err <= 1e-4, err
