@@ -60,6 +60,7 @@ class Stats(C.Structure):
       ('residual0', f64), ('residual', f64), ('omega_last', f64), ('status', C.c_uint32),
       ('nnz', i64 * 8), ('rows', i64 * 8), ('cg_path', i32), ('cg_grid', i32),
       ('cg_iters_warm', i32), ('cg_launches', i32), ('ms_warm', f64), ('ms_dual', f64),
+      ('warm_amp', f64), ('warm_declined', i32), ('pad', i32),
   ]
 
 

@@ -163,11 +163,13 @@ int pcg_unstaged_grid();
 // The dual solve A dlam = b by CG on the primal system K y = J^T alpha~^-1 b
 // (one cooperative kernel; see pcg.cu), stopping on the dual residual
 // (tol_abs, tol_rel |b|), on maxiter, or, with stall_its > 0, once the dual
-// residual has not fallen by 10 % for stall_its iterations.  st is zeroed
-// and then filled like the dual path fills it (iters = primal iterations).
+// residual has not fallen by 10 % for stall_its iterations.  With max_amp >
+// 0 it declines at once (st->flags = 1) when the dual residual of its start
+// exceeds max_amp |b|; st->rz_new holds that ratio.  st is zeroed and then
+// filled like the dual path fills it (iters = primal iterations).
 void launch_pcg_primal(const JView& j, const PcgVecs& v, const JcgPlan& plan,
                        const int32_t* part_dev, CgState* st, double tol_abs, double tol_rel,
-                       int maxiter, int degree, float cheb_lo, int stall_its,
+                       int maxiter, int degree, float cheb_lo, int stall_its, double max_amp,
                        double spin_limit_s, cudaStream_t s);
 
 // deterministic start vector of the power iteration

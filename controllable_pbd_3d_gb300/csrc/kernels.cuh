@@ -101,7 +101,7 @@ struct CgState {
   double rz, rz_new, pap, alpha, beta, rr, rr0, tol2;
   int32_t iters, done, status, maxiter;
   int32_t body_runs;  // executions of the captured loop body
-  int32_t pad;
+  int32_t flags;      // primal warm start: 1 = declined (too stiff to help)
 };
 // the fused vector kernels read the device state; all return early once done
 void launch_cg_init(CgState* st, const double* partials_rz, int blocks, double tol_abs,

@@ -75,6 +75,8 @@ struct QArgs {
   float cheb_lo;
   int32_t stall_its;  // > 0: stop once the dual residual has not fallen by
                       // 10 % for this many iterations
+  double max_amp;     // > 0: decline (stop at once, flags = 1) when the dual
+                      // residual of the start exceeds max_amp |b|
   unsigned long long spin_ns;
 };
 
@@ -90,7 +92,8 @@ struct Own {
 
 // thread-0 state of the solve (identical in every block)
 struct Ctl {
-  double bb, tol2, rz, pap, alpha, beta, rres, best;
+  double bb, tol2, rz, pap, alpha, beta, rres, best, amp0;
+  int32_t declined;
   int32_t since;  // iterations since the dual residual last fell by 10 %
   double ca[kBoot], cb[kBoot];  // bootstrap CG coefficients
   float c1[kMaxCheb], c2[kMaxCheb];
@@ -440,6 +443,8 @@ __global__ void __launch_bounds__(kPT, 1) k_pcg(QArgs a) {
   }
   if (threadIdx.x == 0) {
     c.best = 1e300;
+    c.amp0 = -1.0;
+    c.declined = 0;
     c.since = 0;
     c.iters = 0;
     c.nboot = 0;
@@ -497,7 +502,17 @@ __global__ void __launch_bounds__(kPT, 1) k_pcg(QArgs a) {
         const double se = warp_sum_partials(P3, G);
         if (threadIdx.x == 0) {
           c.rres = se;
-          if (!isfinite(se)) {
+          if (c.amp0 < 0.0) {
+            // the start y = 0, i.e. dlam = alpha~^-1 b: its dual residual
+            // over |b| measures how much float32 accuracy the hand-over loses
+            c.amp0 = c.bb > 0.0 ? sqrt(se / c.bb) : 0.0;
+            if (a.max_amp > 0.0 && c.amp0 > a.max_amp) {
+              c.declined = 1;
+              c.stop = 1;
+            }
+          }
+          if (c.stop) {
+          } else if (!isfinite(se)) {
             c.status |= MGPBD_STATUS_NAN;
             c.stop = 1;
           } else if (se < c.tol2) {
@@ -740,6 +755,8 @@ __global__ void __launch_bounds__(kPT, 1) k_pcg(QArgs a) {
     st->done = 1;
     st->maxiter = a.maxiter;
     st->body_runs = c.nboot;
+    st->flags = c.declined;
+    st->rz_new = c.amp0;
     atomicOr(reinterpret_cast<unsigned int*>(&st->status), c.status);
   }
 }
@@ -777,7 +794,7 @@ int pcg_unstaged_grid() {
 
 void launch_pcg_primal(const JView& j, const PcgVecs& v, const JcgPlan& plan,
                        const int32_t* part_dev, CgState* st, double tol_abs, double tol_rel,
-                       int maxiter, int degree, float cheb_lo, int stall_its,
+                       int maxiter, int degree, float cheb_lo, int stall_its, double max_amp,
                        double spin_limit_s, cudaStream_t s) {
   require(degree >= 1 && degree <= kMaxCheb, MGPBD_EINVAL, "Chebyshev degree out of range");
   require(plan.grid > 0, MGPBD_ESTATE, "persistent CG plan not built");
@@ -820,6 +837,7 @@ void launch_pcg_primal(const JView& j, const PcgVecs& v, const JcgPlan& plan,
   a.degree = degree;
   a.cheb_lo = cheb_lo;
   a.stall_its = stall_its;
+  a.max_amp = max_amp;
   a.spin_ns = static_cast<unsigned long long>(spin_limit_s * 1e9);
   MGPBD_CUDA(cudaMemsetAsync(v.gs, 0, sizeof(GridSync), s));
   MGPBD_CUDA(cudaMemsetAsync(st, 0, sizeof(CgState), s));

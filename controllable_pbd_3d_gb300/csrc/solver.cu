@@ -507,8 +507,13 @@ int32_t Solver::pcg_cheb(const float* b, float* x) {
     bool warm = false;
     if (primal()) {
       // warm start: CG on the primal system to a loose dual residual (or
-      // until it stalls), dlam = alpha~^-1 (b - J y) into x
+      // until it stalls), dlam = alpha~^-1 (b - J y) into x.  Declined when
+      // the start's dual residual exceeds kPrimalMaxAmp |b|: measured on
+      // stiff bodies, above ~1e6 the hand-over loses accuracy the float32
+      // dual CG does not win back (1e-3 .. 1e-2 in dlam), below it the
+      // solution matches a float64 direct solve to ~1e-5.
       constexpr int kPrimalStall = 16;
+      constexpr double kPrimalMaxAmp = 1e6;
       PcgVecs v;
       v.b = b;
       v.dlam = x;
@@ -529,7 +534,8 @@ int32_t Solver::pcg_cheb(const float* b, float* x) {
       const double tol = std::max<double>(p_.primal_tol, p_.rel_tol_cg);
       MGPBD_CUDA(cudaEventRecord(ev_[0], outer));
       launch_pcg_primal(jview(), v, pplan_, jpart_.p, cg_state_.p, p_.tol_cg, tol, p_.maxiter_cg,
-                        p_.cheb_degree, p_.cheb_lo, kPrimalStall, kBarrierLimitS, outer);
+                        p_.cheb_degree, p_.cheb_lo, kPrimalStall, kPrimalMaxAmp, kBarrierLimitS,
+                        outer);
       MGPBD_CUDA(cudaEventRecord(ev_[1], outer));
       sync_read(h_state_, cg_state_.p, sizeof(CgState));
       stats_.ms_warm += event_ms(ev_[0], ev_[1]);
@@ -543,7 +549,9 @@ int32_t Solver::pcg_cheb(const float* b, float* x) {
       if (st & MGPBD_STATUS_NAN) return h_state_->iters;
       its = h_state_->iters;
       left = p_.maxiter_cg - its;
-      warm = true;
+      warm = h_state_->flags == 0;
+      stats_.warm_amp = h_state_->rz_new;
+      if (!warm) stats_.warm_declined += 1;
       if (left <= 0) {
         status_ |= MGPBD_STATUS_CG_MAXITER;
         return its;
@@ -1004,6 +1012,8 @@ void Solver::solve(int32_t frame) {
   stats_.cg_launches = 0;
   stats_.ms_warm = 0.0;
   stats_.ms_dual = 0.0;
+  stats_.warm_amp = 0.0;
+  stats_.warm_declined = 0;
   log_.clear();
   auto now = [] {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();

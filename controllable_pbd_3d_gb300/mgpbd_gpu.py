@@ -246,7 +246,8 @@ class MGPBDSolverGPU:
         'rows': list(s.rows[:nl]), 'nnz': list(s.nnz[:nl]),
         'cg_path': ('kernels', 'persistent', 'staged', 'primal', 'primal-staged')[s.cg_path],
         'cg_grid': s.cg_grid, 'cg_iters_warm': s.cg_iters_warm, 'cg_launches': s.cg_launches,
-        'ms_warm': s.ms_warm, 'ms_dual': s.ms_dual,
+        'ms_warm': s.ms_warm, 'ms_dual': s.ms_dual, 'warm_amp': s.warm_amp,
+        'warm_declined': s.warm_declined,
     }
 
   def newton_log(self):

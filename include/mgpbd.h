@@ -128,7 +128,10 @@ typedef struct mgpbd_params {
    * primal start dlam = alpha~^-1 b can have a dual residual far above |b|
    * (by the stiffness ratio), so in float32 the primal CG alone cannot
    * always reach 1e-6; it does the coarse part of the work at about half
-   * the cost per unit of residual reduction.  0 (default): CG on A only. */
+   * the cost per unit of residual reduction.  The warm start is declined
+   * (CG on A from 0) when that ratio exceeds 1e6: beyond it the hand-over
+   * loses accuracy the float32 dual CG does not win back.  0 (default):
+   * CG on A only. */
   int32_t primal;
   float primal_tol;  /* relative dual residual of the hand-over (1e-2)     */
 } mgpbd_params;
@@ -153,6 +156,9 @@ typedef struct mgpbd_stats {
   int32_t cg_launches;      /* persistent kernel launches in the last solve   */
   double ms_warm;           /* GPU time of the primal warm-start kernels and  */
   double ms_dual;           /* of the dual persistent kernels, last solve     */
+  double warm_amp;          /* dual residual / |b| of the primal start (last) */
+  int32_t warm_declined;    /* Newton iterations whose warm start declined    */
+  int32_t pad;
 } mgpbd_stats;
 
 #define MGPBD_CGPATH_KERNELS 0      /* one kernel (or graph node) per operation */

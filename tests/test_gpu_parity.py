@@ -331,14 +331,16 @@ def test_fast_mode_matches_parity_mode(cuda):
 
 
 @pytest.mark.parametrize('path,comp', [('kernels', 2.7e-8), ('dual', 2.7e-8), ('dual', 1.5e-6),
-                                       ('primal', 1.5e-6), ('primal', 4.5e-7)])
+                                       ('primal', 1.5e-6), ('primal', 4.5e-7), ('primal', 1.9e-7),
+                                       ('primal', 2.7e-8)])
 def test_cheb_solution_matches_direct_solve_on_stiff_body(cuda, path, comp):
   """The first Newton system of a small stiff body (750 tets, cell size
   1/40): the FAST solve's dlam against a float64 sparse direct solve of the
   same system (built from the solver's own b and gradients), to 1e-4.  The
-  dual solves hold down to compliance 2.7e-8; the primal warm start only
-  where it is accurate (compliance >= ~4e-7 at this cell size: stiffer,
-  its hand-over leaves errors the float32 dual CG does not remove)."""
+  dual solves hold down to compliance 2.7e-8.  The primal warm start is
+  taken where it is accurate (start amplification ~2e5 at 1.5e-6, ~6.5e5 at
+  4.5e-7) and declined where its hand-over would leave errors the float32
+  dual CG does not remove (~1.5e6 at 1.9e-7, ~1.1e7 at 2.7e-8)."""
   import scipy.sparse as sp
   import scipy.sparse.linalg as spl
   from controllable_pbd_3d_gb300 import meshgen
@@ -373,3 +375,6 @@ def test_cheb_solution_matches_direct_solve_on_stiff_body(cuda, path, comp):
   got = np_(s._dlam_gpu).astype(np.float64)
   err = float(np.abs(got - exact).max() / np.abs(exact).max())
   assert err <= 1e-4, err
+  if path == 'primal':
+    st = s.stats()
+    assert st['warm_declined'] == (1 if comp < 3e-7 else 0), st['warm_amp']
