@@ -304,22 +304,31 @@ def roofline_from_steps(st, nt, nv, degree, hbm_peak, peak_kind):
 
 def roofline_csr(torch, s, hbm_peak, peak_kind, reps=40):
   """Level-0 weighted Jacobi sweep of the CSR V-cycle (the dominant launch
-  of the plain AMG-PCG: 4 per CG iteration), vectorised row kernel."""
+  of the plain AMG-PCG: 4 per CG iteration) and the level-0 SpMV, both the
+  vectorised row kernel, timed with CUDA events (launches captured into a
+  CUDA graph; the 207 MB matrix does not fit in L2)."""
   A = s._gpu_solver._gpu_As[0]
   n, nnz = A.n_rows, A.nnz
   b = torch.randn(n, device='cuda')
   x = torch.randn(n, device='cuda')
   y = torch.empty_like(x)
-  dt = _event_time(torch, lambda: s.level_sweep(0, 1, x, b, y, 0.5), reps)
-  # algorithmic bytes: values + column ids + row pointers + x gathered once,
-  # b, 1/diag read, x_new written
-  bytes_ = 8 * nnz + 4 * (n + 1) + 4 * n * 4
-  achieved = bytes_ / dt / 1e9
-  return {'kernel': 'k_csr_rows_vec<8,4,kJacobi> (level-0 weighted Jacobi sweep, CSR)',
-          'bound': 'hbm', 'achieved': round(achieved, 1), 'peak': hbm_peak, 'unit': 'GB/s',
-          'frac': round(achieved / hbm_peak, 4), 'peak_kind': peak_kind,
-          'algorithmic_bytes_per_launch': bytes_, 'launch_us': round(dt * 1e6, 2),
-          'traffic': None}
+  out = {}
+  for name, f, extra in (
+      ('jacobi', lambda: s.level_sweep(0, 1, x, b, y, 0.5), 4 * n * 4),
+      ('spmv', lambda: s.level_sweep(0, 0, x, None, y), 4 * n * 2)):
+    dt = _event_time(torch, f, reps)
+    # algorithmic bytes: values + column ids + row pointers, plus x gathered
+    # once, y written (and b, 1/diag read for the sweep)
+    bytes_ = 8 * nnz + 4 * (n + 1) + extra
+    achieved = bytes_ / dt / 1e9
+    out[name] = {'bound': 'hbm', 'achieved': round(achieved, 1), 'peak': hbm_peak, 'unit': 'GB/s',
+                 'frac': round(achieved / hbm_peak, 4), 'peak_kind': peak_kind,
+                 'algorithmic_bytes_per_launch': bytes_, 'launch_us': round(dt * 1e6, 2),
+                 'traffic': None}
+  roof = dict(out['jacobi'])
+  roof['kernel'] = 'k_csr_rows_vec<4,6,kJacobi> (level-0 weighted Jacobi sweep, CSR)'
+  roof['spmv'] = dict(out['spmv'], kernel='k_csr_rows_vec<4,6,kSpmv> (level-0 SpMV, CSR)')
+  return roof
 
 
 # CG iterations per Newton iteration the plain AMG-PCG needs on this

@@ -503,11 +503,14 @@ void rows_dispatch(const CsrView& a, const float* x, const float* b, float* y, f
   if (a.n <= 0) return;
   double avg = a.n ? (double)a.nnz / a.n : 0.0;
   if (a.padded && OP != kJacobiZero) {
-    // one pass of G lanes x U float4 covers 4*G*U elements of a row
-    int G = avg >= 40 ? 8 : 4;
+    // one pass of G lanes x U float4 covers 4*G*U elements of a row; 4 lanes
+    // x 6 float4 (96 elements) suits the ~81-nonzero rows of the level-0
+    // ARAP matrix: measured on GB300 at 40^3 (207 MB matrix), SpMV 5.0 TB/s
+    // against 4.3 TB/s for 8 x 4 and 4.8 TB/s for 4 x 8
+    const int G = 4;
     int grid = OP == kSpmvDot ? reduce_blocks(a.n) : grid_for(a.n, kThreads / G);
-    if (G == 8)
-      k_csr_rows_vec<8, 4, OP><<<grid, kThreads, 0, s>>>(a.n, a.indptr, a.indices, a.data, x, b,
+    if (avg >= 40)
+      k_csr_rows_vec<4, 6, OP><<<grid, kThreads, 0, s>>>(a.n, a.indptr, a.indices, a.data, x, b,
                                                           a.diag_inv, y, w, wp, partials, st);
     else
       k_csr_rows_vec<4, 4, OP><<<grid, kThreads, 0, s>>>(a.n, a.indptr, a.indices, a.data, x, b,
