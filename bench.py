@@ -488,6 +488,8 @@ def run_profile_solve(args):
   kw.update(FAST_KW if args.profile_precond == 'cheb' else PLAIN_KW)
   kw['use_graph'] = False
   kw['persistent'] = args.profile_path == 'persistent'
+  if args.primal is not None:
+    kw['primal'] = bool(args.primal)
   kw['maxiter_cg'] = args.profile_maxiter
   s, x, _ = make_solver(torch, args.size, kw)
   s.make_prediction()
