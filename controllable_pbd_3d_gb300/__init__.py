@@ -5,10 +5,11 @@ The compute runs in libmgpbd.so (hand-written CUDA + C++); this package
 is the ctypes binding and the Python mirrors of the reference classes.
 """
 
+from .adaptive import AdaptiveZone, MGPBDAdaptiveSolver  # noqa: F401
 from .batch import Body, BodyBatch  # noqa: F401
 from .framework import MGPBDConstraint, PbdFramework  # noqa: F401
 from .mgpbd_gpu import MGPBDSolverGPU  # noqa: F401
 from .solver_benchmark import SolverBenchmark  # noqa: F401
 
 __all__ = ['MGPBDSolverGPU', 'SolverBenchmark', 'MGPBDConstraint', 'PbdFramework', 'Body',
-           'BodyBatch']
+           'BodyBatch', 'AdaptiveZone', 'MGPBDAdaptiveSolver']

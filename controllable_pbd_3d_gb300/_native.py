@@ -107,6 +107,12 @@ _SIGS = {
     'mgpbd_apply_dpos': (C.c_int, [vp, f64]),
     'mgpbd_apply_matrix': (C.c_int, [vp, i32, vp, vp]),
     'mgpbd_level_sweep': (C.c_int, [vp, i32, i32, vp, vp, vp, f32]),
+    'mgpbd_zone_proximity': (C.c_int, [vp, vp, f32, f32, f32, f32]),
+    'mgpbd_zone_strain': (C.c_int, [vp, vp, vp, f32, f32]),
+    'mgpbd_zone_expand': (C.c_int, [vp, vp, i32]),
+    'mgpbd_mask_alpha': (C.c_int, [vp, vp, vp]),
+    'mgpbd_restore_alpha': (C.c_int, [vp, vp]),
+    'mgpbd_host_face_adjacency': (C.c_int, [vp, i32, vp, vp, vp]),
     'mgpbd_csr_spmv': (C.c_int, [i32, vp, vp, vp, vp, vp, vp]),
     'mgpbd_csr_jacobi': (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp, f32, vp]),
     'mgpbd_csr_diag_inv': (C.c_int, [i32, vp, vp, vp, vp, vp]),

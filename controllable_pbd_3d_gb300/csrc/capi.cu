@@ -271,6 +271,33 @@ int mgpbd_apply_matrix(mgpbd_handle h, int32_t matrix_free, const float* x, floa
   return guarded([&] { h->impl.apply_matrix(matrix_free, x, y); });
 }
 
+int mgpbd_zone_proximity(mgpbd_handle h, int32_t* active, float cx, float cy, float cz,
+                         float radius) {
+  if (!h || !active) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.zone_proximity(active, cx, cy, cz, radius); });
+}
+
+int mgpbd_zone_strain(mgpbd_handle h, int32_t* active, const float* x_old, float threshold,
+                      float dt) {
+  if (!h || !active || !(dt > 0.0f)) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.zone_strain(active, x_old, threshold, dt); });
+}
+
+int mgpbd_zone_expand(mgpbd_handle h, int32_t* active, int32_t n_rings) {
+  if (!h || !active || n_rings < 0) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.zone_expand(active, n_rings); });
+}
+
+int mgpbd_mask_alpha(mgpbd_handle h, const int32_t* active, float* saved_alpha) {
+  if (!h || !active || !saved_alpha) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.mask_alpha(active, saved_alpha); });
+}
+
+int mgpbd_restore_alpha(mgpbd_handle h, const float* saved_alpha) {
+  if (!h || !saved_alpha) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.restore_alpha(saved_alpha); });
+}
+
 int mgpbd_level_sweep(mgpbd_handle h, int32_t level, int32_t op, const float* x, const float* b,
                       float* y, float omega) {
   if (!h || !x || !y || (op == 1 && !b)) return MGPBD_EINVAL;
@@ -394,6 +421,17 @@ int mgpbd_host_tet_hierarchy(const int32_t* t_i, int32_t nt, int32_t max_coarse,
     *n_levels = static_cast<int32_t>(sz.size());
     std::memcpy(sizes, sz.data(), sizeof(int32_t) * sz.size());
     if (!aggs.empty()) std::memcpy(agg_ids, aggs[0].data(), sizeof(int32_t) * aggs[0].size());
+  });
+}
+
+int mgpbd_host_face_adjacency(const int32_t* t_i, int32_t nt, int64_t* nnz, int32_t* indptr,
+                              int32_t* indices) {
+  if (!t_i || nt < 0 || !nnz) return MGPBD_EINVAL;
+  return guarded([&] {
+    mgpbd::Csr a = mgpbd::face_adjacency(t_i, nt);
+    *nnz = a.nnz();
+    if (indptr) std::copy(a.indptr.begin(), a.indptr.end(), indptr);
+    if (indices) std::copy(a.indices.begin(), a.indices.end(), indices);
   });
 }
 

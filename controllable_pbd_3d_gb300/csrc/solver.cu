@@ -2,6 +2,7 @@
 // around the multigrid-preconditioned CG of GPUMultigridSolver
 // (cons/mgpcg_gpu.py:214-329), on one CUDA stream.
 #include "solver.h"
+#include "zone.cuh"
 
 #include <algorithm>
 #include <chrono>
@@ -433,6 +434,51 @@ void Solver::apply_matrix(int matrix_free, const float* x, float* y) {
   } else {
     launch_spmv(levels_[0].view(), x, y, stream_);
   }
+}
+
+// ---- adaptive zones ------------------------------------------------------
+void Solver::zone_proximity(int32_t* active, float cx, float cy, float cz, float radius) {
+  require_init();
+  require(active != nullptr, MGPBD_EINVAL, "active must be a device array of nt int32");
+  launch_zone_proximity(t_i_, x_, nt_, cx, cy, cz, radius, active, stream_);
+}
+
+void Solver::zone_strain(int32_t* active, const float* x_old, float threshold, float dt) {
+  require_init();
+  require(active != nullptr, MGPBD_EINVAL, "active must be a device array of nt int32");
+  require(dt > 0.0f, MGPBD_EINVAL, "dt must be positive");
+  launch_zone_strain(t_i_, x_, x_old ? x_old : x_old_.p, nt_, threshold, dt, active, stream_);
+}
+
+void Solver::zone_expand(int32_t* active, int32_t n_rings) {
+  require_init();
+  require(active != nullptr && n_rings >= 0, MGPBD_EINVAL, "bad zone expansion arguments");
+  if (!adj_ptr_.p) {
+    std::vector<int32_t> t_host(4LL * nt_);
+    MGPBD_CUDA(cudaMemcpyAsync(t_host.data(), t_i_, sizeof(int32_t) * t_host.size(),
+                               cudaMemcpyDeviceToHost, stream_));
+    MGPBD_CUDA(cudaStreamSynchronize(stream_));
+    Csr a = face_adjacency(t_host.data(), nt_);
+    upload(adj_ptr_, a.indptr, stream_);
+    std::vector<int32_t> idx(a.indices);
+    if (idx.empty()) idx.push_back(0);
+    upload(adj_, idx, stream_);
+    zone_scratch_.alloc(nt_);
+  }
+  launch_zone_expand(adj_ptr_.p, adj_.p, nt_, n_rings, active, zone_scratch_.p, stream_);
+}
+
+void Solver::mask_alpha(const int32_t* active, float* saved) {
+  require_init();
+  require(active != nullptr && saved != nullptr, MGPBD_EINVAL, "bad alpha mask arguments");
+  launch_mask_alpha(active, alpha_.p, saved, nt_, stream_);
+}
+
+void Solver::restore_alpha(const float* saved) {
+  require_init();
+  require(saved != nullptr, MGPBD_EINVAL, "saved must be a device array of nt float");
+  MGPBD_CUDA(cudaMemcpyAsync(alpha_.p, saved, sizeof(float) * nt_, cudaMemcpyDeviceToDevice,
+                             stream_));
 }
 
 // one row-kernel pass over the library's CSR of `level`: op 0 y = A x,

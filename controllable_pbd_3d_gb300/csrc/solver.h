@@ -70,6 +70,12 @@ class Solver {
   // matrix_free: 0 CSR values, 1 gradients (prepared first), 2 gradients
   // as prepared by the last call
   void apply_matrix(int matrix_free, const float* x, float* y);
+  // adaptive zones (cons/adaptive_zone.py, cons/mgpbd_adaptive.py)
+  void zone_proximity(int32_t* active, float cx, float cy, float cz, float radius);
+  void zone_strain(int32_t* active, const float* x_old, float threshold, float dt);
+  void zone_expand(int32_t* active, int32_t n_rings);
+  void mask_alpha(const int32_t* active, float* saved);
+  void restore_alpha(const float* saved);
   void level_sweep(int32_t level, int32_t op, const float* x, const float* b, float* y,
                    float omega);
 
@@ -148,6 +154,7 @@ class Solver {
   DevBuf<JState> jst_;
   DevBuf<float> jxc_, jrf_;  // persistent CG: Kahan term of x, float32 residual
   DevBuf<GridSync> jgs_;
+  DevBuf<int32_t> adj_ptr_, adj_, zone_scratch_;  // face adjacency (built on first use)
   DevBuf<float4> gT_;      // persistent CG: gradients as three planes
   JcgPlan jplan_;          // persistent CG work split
   JcgPlan pplan_;          // the same for the primal warm start

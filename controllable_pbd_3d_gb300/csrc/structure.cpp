@@ -238,9 +238,15 @@ Csr build_pattern(const int32_t* t_i, int32_t nt) {
 }
 
 // ---------------------------------------------------------------------------
-// cons/tet_aggregation.py:11-37 (face adjacency) and :40-127 (pass 1).
-int32_t tet_aggregate(const int32_t* t_i, int32_t nt, int32_t max_agg_size,
-                      std::vector<int32_t>& agg_ids) {
+// cons/tet_aggregation.py:11-37: tets sharing a face that exactly two tets
+// have, as (first appearance of the face, tet, tet), in order of first
+// appearance (the order the reference fills its adjacency sets in).
+struct FacePair {
+  int64_t first;
+  int32_t t0, t1;
+};
+
+static std::vector<FacePair> face_pairs(const int32_t* t_i, int32_t nt) {
   // faces keyed by the sorted vertex triple, in order of first appearance
   std::vector<FaceRec> faces(4LL * nt);
   for (int32_t t = 0; t < nt; ++t) {
@@ -259,11 +265,7 @@ int32_t tet_aggregate(const int32_t* t_i, int32_t nt, int32_t max_agg_size,
     if (x.c != y.c) return x.c < y.c;
     return x.occ < y.occ;
   });
-  struct Pair {
-    int64_t first;
-    int32_t t0, t1;
-  };
-  std::vector<Pair> pairs;
+  std::vector<FacePair> pairs;
   pairs.reserve(2LL * nt);
   for (size_t s = 0; s < faces.size();) {
     size_t e = s + 1;
@@ -273,11 +275,38 @@ int32_t tet_aggregate(const int32_t* t_i, int32_t nt, int32_t max_agg_size,
     if (e - s == 2) pairs.push_back({faces[s].occ, faces[s].tet, faces[s + 1].tet});
     s = e;
   }
-  std::vector<FaceRec>().swap(faces);
   std::sort(pairs.begin(), pairs.end(),
-            [](const Pair& x, const Pair& y) { return x.first < y.first; });
+            [](const FacePair& x, const FacePair& y) { return x.first < y.first; });
+  return pairs;
+}
+
+Csr face_adjacency(const int32_t* t_i, int32_t nt) {
+  const std::vector<FacePair> pairs = face_pairs(t_i, nt);
+  Csr a;
+  a.n_rows = a.n_cols = nt;
+  a.indptr.assign(nt + 1, 0);
+  for (const FacePair& p : pairs) {
+    ++a.indptr[p.t0 + 1];
+    ++a.indptr[p.t1 + 1];
+  }
+  for (int32_t t = 0; t < nt; ++t) a.indptr[t + 1] += a.indptr[t];
+  a.indices.resize(a.indptr[nt]);
+  std::vector<int32_t> fill(a.indptr.begin(), a.indptr.end() - 1);
+  for (const FacePair& p : pairs) {
+    a.indices[fill[p.t0]++] = p.t1;
+    a.indices[fill[p.t1]++] = p.t0;
+  }
+  for (int32_t t = 0; t < nt; ++t)
+    std::sort(a.indices.begin() + a.indptr[t], a.indices.begin() + a.indptr[t + 1]);
+  return a;
+}
+
+// cons/tet_aggregation.py:40-127 (pass 1).
+int32_t tet_aggregate(const int32_t* t_i, int32_t nt, int32_t max_agg_size,
+                      std::vector<int32_t>& agg_ids) {
+  const std::vector<FacePair> pairs = face_pairs(t_i, nt);
   std::vector<SetEmu> adj(nt);
-  for (const Pair& p : pairs) {
+  for (const FacePair& p : pairs) {
     adj[p.t0].add(p.t1);
     adj[p.t1].add(p.t0);
   }

@@ -52,6 +52,10 @@ Galerkin galerkin_structural(const Csr& fine, const int32_t* agg_ids, int32_t n_
 // more levels are requested).  Deterministic; visits rows in order.
 int32_t graph_aggregate(const Csr& a, int32_t max_agg_size, std::vector<int32_t>& agg_ids);
 
+// cons/tet_aggregation.py:11-37 as CSR: row t = the tets sharing a face
+// with t that no third tet shares, ascending.
+Csr face_adjacency(const int32_t* t_i, int32_t nt);
+
 // vertex -> (tet, local slot) incidence, tets ascending per vertex, used for
 // the deterministic scatter of dlambda into dpos.
 void vertex_incidence(const int32_t* t_i, int32_t nt, int32_t nv,

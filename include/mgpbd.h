@@ -278,6 +278,32 @@ int mgpbd_apply_dpos(mgpbd_handle h, double omega);
  * matrix_free = 2 does the same reusing the vertex-major gradients of the
  * previous call; matrix_free = 0 multiplies by the assembled CSR values. */
 int mgpbd_apply_matrix(mgpbd_handle h, int32_t matrix_free, const float* x, float* y);
+/* ---- adaptive zones (cons/adaptive_zone.py:14-91) --------------------------
+ * `active` is a caller-owned device array of nt int32 (0 passive, 1 active),
+ * the reference's AdaptiveZone.tet_active. */
+/* AdaptiveZone.update_by_proximity (:40-55): active iff a vertex of the tet
+ * (current positions) lies strictly within `radius` of (cx, cy, cz). */
+int mgpbd_zone_proximity(mgpbd_handle h, int32_t* active, float cx, float cy, float cz,
+                         float radius);
+/* AdaptiveZone.update_by_strain (:57-72): active iff the fastest vertex of
+ * the tet moved faster than `threshold`, speed = |x - x_old| / dt; x_old is
+ * a device (nv, 3) array, or NULL for the solver's v_p_old. */
+int mgpbd_zone_strain(mgpbd_handle h, int32_t* active, const float* x_old, float threshold,
+                      float dt);
+/* AdaptiveZone.expand_zone (:74-85): n_rings rings of growth across faces
+ * shared by exactly two tets (the adjacency of cons/tet_aggregation.py:11-37,
+ * built on the first call). */
+int mgpbd_zone_expand(mgpbd_handle h, int32_t* active, int32_t n_rings);
+/* MGPBDAdaptiveSolver._apply_active_mask / _restore_mask
+ * (cons/mgpbd_adaptive.py:66-93): saved_alpha (device, nt float) receives
+ * alpha~; passive tets get alpha~ = 1e20 (no force); restore copies it back. */
+int mgpbd_mask_alpha(mgpbd_handle h, const int32_t* active, float* saved_alpha);
+int mgpbd_restore_alpha(mgpbd_handle h, const float* saved_alpha);
+/* Host: the face adjacency above as CSR (rows ascending); indptr nt + 1,
+ * indices *nnz (pass NULL arrays to query nnz first). */
+int mgpbd_host_face_adjacency(const int32_t* t_i, int32_t nt, int64_t* nnz, int32_t* indptr,
+                              int32_t* indices);
+
 /* One pass of the library's vectorised CSR row kernel on multigrid level
  * `level`: op 0 y = A x (GPUSparseMatrix.spmv, cons/sparse_gpu.py:123-132),
  * op 1 y = x + omega D^-1 (b - A x) (jacobi_smooth, :134-144). */

@@ -643,3 +643,40 @@ class MGPBDOracle:
       omega = self.line_search() if self.use_line_search else 1.0
       self.apply(omega)
       self.log.append((ite, r, it, omega))
+
+
+# ---------------------------------------------------------------------------
+# Adaptive zones (cons/adaptive_zone.py:40-85), float32 like the reference.
+
+def zone_proximity(x, t_i, center, radius):
+  """cons/adaptive_zone.py:40-55: 1 iff a vertex is strictly within radius."""
+  t = np.asarray(t_i).reshape(-1, 4)
+  p = np.asarray(x, np.float32)[t]                     # (nt, 4, 3)
+  d = p - np.asarray(center, np.float32)
+  d2 = (d[..., 0] * d[..., 0] + d[..., 1] * d[..., 1]) + d[..., 2] * d[..., 2]
+  r2 = np.float32(radius) * np.float32(radius)
+  return (d2 < r2).any(axis=1).astype(np.int32)
+
+
+def zone_strain(x, x_old, t_i, threshold, dt):
+  """cons/adaptive_zone.py:57-72: 1 iff the fastest vertex moved faster
+  than threshold (speed = |x - x_old| / dt)."""
+  t = np.asarray(t_i).reshape(-1, 4)
+  d = np.asarray(x, np.float32)[t] - np.asarray(x_old, np.float32)[t]
+  n2 = (d[..., 0] * d[..., 0] + d[..., 1] * d[..., 1]) + d[..., 2] * d[..., 2]
+  speed = np.sqrt(n2) / np.float32(dt)
+  vmax = np.maximum(speed.max(axis=1), np.float32(0.0))
+  return (vmax > np.float32(threshold)).astype(np.int32)
+
+
+def zone_expand(active, adj, n_rings):
+  """cons/adaptive_zone.py:74-85 with adj from face_adjacency_sets."""
+  active = np.asarray(active, np.int32).copy()
+  for _ in range(n_rings):
+    new = active.copy()
+    for t in range(len(active)):
+      if active[t] == 1:
+        for nb in adj[t]:
+          new[nb] = 1
+    active = new
+  return active
