@@ -127,6 +127,12 @@ int mgpbd_set_mesh(mgpbd_handle h, const float* x_ref, const float* invm, const 
   return guarded([&] { h->impl.set_mesh(x_ref, invm, t_i, nv, nt, x, v); });
 }
 
+int mgpbd_set_hierarchy(mgpbd_handle h, const int32_t* agg_ids, int32_t n_levels,
+                        const int32_t* level_sizes) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.set_hierarchy(agg_ids, n_levels, level_sizes); });
+}
+
 int mgpbd_init(mgpbd_handle h) {
   if (!h) return MGPBD_EINVAL;
   return guarded([&] { h->impl.init(); });

@@ -142,6 +142,36 @@ void Solver::require_init() const {
   require(inited_, MGPBD_ESTATE, "mgpbd_init has not been called");
 }
 
+// Caller-provided aggregation hierarchy (used by the next init instead of
+// the built-in tet aggregation): level_sizes[0] = nt, and for each level l
+// the level_sizes[l] entries of agg_ids from offset sum(level_sizes[0..l))
+// map level-l rows onto [0, level_sizes[l+1]), every coarse row used.
+void Solver::set_hierarchy(const int32_t* agg_ids, int32_t n_levels, const int32_t* level_sizes) {
+  require(x_ && t_i_, MGPBD_ESTATE, "mgpbd_set_mesh must come before mgpbd_set_hierarchy");
+  require(n_levels >= 2 && n_levels <= 8, MGPBD_EINVAL, "n_levels must be in [2, 8]");
+  require(level_sizes != nullptr && agg_ids != nullptr, MGPBD_EINVAL, "null hierarchy array");
+  require(level_sizes[0] == nt_, MGPBD_EINVAL, "level_sizes[0] must equal nt");
+  std::vector<int32_t> sizes(level_sizes, level_sizes + n_levels);
+  std::vector<std::vector<int32_t>> aggs;
+  int64_t off = 0;
+  for (int32_t l = 0; l + 1 < n_levels; ++l) {
+    require(sizes[l + 1] >= 1 && sizes[l + 1] <= sizes[l], MGPBD_EINVAL,
+            "each level must be smaller than the one above");
+    std::vector<int32_t> a(agg_ids + off, agg_ids + off + sizes[l]);
+    std::vector<uint8_t> used(sizes[l + 1], 0);
+    for (int32_t v : a) {
+      require(v >= 0 && v < sizes[l + 1], MGPBD_EINVAL, "aggregate id out of range");
+      used[v] = 1;
+    }
+    for (uint8_t u : used) require(u != 0, MGPBD_EINVAL, "empty aggregate");
+    aggs.push_back(std::move(a));
+    off += sizes[l];
+  }
+  user_sizes_ = std::move(sizes);
+  user_aggs_ = std::move(aggs);
+  inited_ = false;
+}
+
 void Solver::set_mesh(const float* x_ref, const float* invm, const int32_t* t_i, int32_t nv,
                       int32_t nt, float* x, float* v) {
   require(x_ref && invm && t_i && x && v, MGPBD_EINVAL, "null mesh pointer");
@@ -155,6 +185,8 @@ void Solver::set_mesh(const float* x_ref, const float* invm, const int32_t* t_i,
   x_ = x;
   v_ = v;
   inited_ = false;
+  user_sizes_.clear();
+  user_aggs_.clear();
   if (cg_exec_) {
     cudaGraphExecDestroy(cg_exec_);
     cg_exec_ = nullptr;
@@ -284,7 +316,12 @@ void Solver::build_hierarchy(const std::vector<int32_t>& t_host, const std::vect
   // tet hierarchy (cons/tet_aggregation.py:145-211, max_levels = 4)
   std::vector<int32_t> sizes;
   std::vector<std::vector<int32_t>> aggs;
-  tet_hierarchy(t_host.data(), nt_, max_coarse, 4, sizes, aggs);
+  if (!user_sizes_.empty()) {
+    sizes = user_sizes_;
+    aggs = user_aggs_;
+  } else {
+    tet_hierarchy(t_host.data(), nt_, max_coarse, 4, sizes, aggs);
+  }
   std::vector<float> fine_vals = a0;
   for (size_t l = 0; l < aggs.size(); ++l) {
     Level& F = levels_[l];

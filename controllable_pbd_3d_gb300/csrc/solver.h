@@ -51,6 +51,7 @@ class Solver {
   void set_stream(cudaStream_t s) { stream_ = s; }
   void set_mesh(const float* x_ref, const float* invm, const int32_t* t_i, int32_t nv, int32_t nt,
                 float* x, float* v);
+  void set_hierarchy(const int32_t* agg_ids, int32_t n_levels, const int32_t* level_sizes);
   void init();
   void step(int32_t frame);
   void make_prediction();
@@ -157,6 +158,8 @@ class Solver {
   DevBuf<int32_t> adj_ptr_, adj_, zone_scratch_;  // face adjacency (built on first use)
   DevBuf<float4> gT_;      // persistent CG: gradients as three planes
   JcgPlan jplan_;          // persistent CG work split
+  std::vector<int32_t> user_sizes_;               // mgpbd_set_hierarchy
+  std::vector<std::vector<int32_t>> user_aggs_;
   JcgPlan pplan_;          // the same for the primal warm start
   DevBuf<float4> pv_[10];  // primal CG vertex vectors
   DevBuf<float> ps_;       // primal CG tet scratch

@@ -203,6 +203,22 @@ class MGPBDSolverGPU:
     return device_view(ptr.value, shape)
 
   # cons/mgpbd_gpu.py:92-114
+  def set_hierarchy(self, aggs):
+    """Use the aggregation hierarchy `aggs` (a list of per-level aggregate
+    id arrays: aggs[l] maps level-l rows to level-(l+1) rows) instead of
+    the built-in tet aggregation at the next init()."""
+    sizes = [self.n_tets]
+    for a in aggs:
+      a = np.asarray(a)
+      if len(a) != sizes[-1]:
+        raise ValueError('aggs[l] must have one id per level-l row')
+      sizes.append(int(a.max()) + 1 if len(a) else 0)
+    flat = np.ascontiguousarray(np.concatenate([np.asarray(a, np.int32) for a in aggs]))
+    sz = np.asarray(sizes, np.int32)
+    N.check(self._lib.mgpbd_set_hierarchy(self._h, flat.ctypes.data, len(sizes), sz.ctypes.data),
+            'mgpbd_set_hierarchy')
+    self._inited = False
+
   def init(self):
     self._stream()
     N.check(self._lib.mgpbd_init(self._h), 'mgpbd_init')

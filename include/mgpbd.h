@@ -199,6 +199,16 @@ int mgpbd_set_mesh(mgpbd_handle h, const float* x_ref, const float* invm,
                    const int32_t* t_i, int32_t nv, int32_t nt, float* x,
                    float* v);
 
+/* Optional, between mgpbd_set_mesh and mgpbd_init: the aggregation
+ * hierarchy to use instead of the built-in tet aggregation
+ * (cons/tet_aggregation.py:145-211 / GPUMultigridSolver.setup's Ps,
+ * cons/mgpcg_gpu.py:30-173).  Host arrays: level_sizes[n_levels] with
+ * level_sizes[0] = nt; agg_ids holds, level after level, level_sizes[l]
+ * aggregate ids in [0, level_sizes[l+1]) (every id used).  2 <= n_levels
+ * <= 8.  mgpbd_set_mesh clears it. */
+int mgpbd_set_hierarchy(mgpbd_handle h, const int32_t* agg_ids, int32_t n_levels,
+                        const int32_t* level_sizes);
+
 /* Replaces MGPBDSolverGPU.init (cons/mgpbd_gpu.py:92-114): rest shape,
  * sparsity pattern, first A, tet hierarchy, multigrid setup. */
 int mgpbd_init(mgpbd_handle h);

@@ -378,3 +378,44 @@ def test_cheb_solution_matches_direct_solve_on_stiff_body(cuda, path, comp):
   if path == 'primal':
     st = s.stats()
     assert st['warm_declined'] == (1 if comp < 3e-7 else 0), st['warm_amp']
+
+
+def test_set_hierarchy(cuda):
+  """mgpbd_set_hierarchy: the built-in hierarchy passed back in reproduces
+  the default solver bit for bit; a different one (pairs of consecutive
+  tets) is used as given."""
+  from controllable_pbd_3d_gb300 import meshgen
+  from controllable_pbd_3d_gb300.mgpbd_gpu import MGPBDSolverGPU
+  from oracle.mgpbd_oracle import tet_hierarchy
+  n = 6
+  xr, t = meshgen.hex_grid_tets(n, n, n)
+  x0, _ = meshgen.hex_grid_tets(n, n, n, jitter=0.02, seed=4)
+  invm = np.ones(len(xr), np.float32)
+  invm[meshgen.grid_face_vertices(n, n, n, 1)] = 0
+  nt = len(t) // 4
+  kw = dict(mu=1e5, maxiter=4, maxiter_cg=200, tol_cg=1e-9)
+
+  def make():
+    x = cuda.tensor(x0, device='cuda')
+    return MGPBDSolverGPU(x, cuda.tensor(xr, device='cuda'), cuda.tensor(invm, device='cuda'),
+                          cuda.tensor(t, device='cuda'), None, [0, -9.8, 0], 1 / 300, **kw), x
+
+  s0, x0t = make()
+  s0.init()
+  aggs, sizes = tet_hierarchy(t, nt)
+  s1, x1t = make()
+  s1.set_hierarchy(aggs)
+  s1.init()
+  np.testing.assert_array_equal(np_(s1._gpu_solver._agg[0]), aggs[0])
+  for k in range(2):
+    s0.step(k)
+    s1.step(k)
+  np.testing.assert_array_equal(np_(x0t), np_(x1t))
+  pairs = np.arange(nt, dtype=np.int32) // 2
+  s2, x2t = make()
+  s2.set_hierarchy([pairs])
+  s2.init()
+  np.testing.assert_array_equal(np_(s2._gpu_solver._agg[0]), pairs)
+  assert s2.stats()['rows'] == [nt, (nt + 1) // 2]
+  s2.step(0)
+  assert np.isfinite(np_(x2t)).all()
