@@ -450,6 +450,8 @@ def run_ours(args):
       'config': {'workload': f'{args.size}^3 hex cube, 5 tets/hex', 'n_verts': n_verts,
                  'n_tets': n_tets, 'nnz_level0': st0['nnz'][0], 'levels': st0['rows'],
                  'compliance': compliance, 'dt': DT, 'rel_res_cg': 1e-6, 'mode': 'fast',
+                 'solver': ('primal warm start + dual persistent Chebyshev-8 CG'
+                            if kw.get('primal') else 'dual persistent Chebyshev-8 CG'),
                  'l2': 'level-0 matrix 207 MB > L2, no flush', 'parallelism': f'replicas{ws}'},
       'newton_iters_per_step': newton / args.steps, 'cg_iters_per_step': cg / args.steps,
       'cg_iters_per_s': round(ws * cg / t_max, 1), 'gpu_launches': int(launches),
