@@ -1,4 +1,5 @@
-"""ctypes binding of libmgpbd.so (the C ABI declared in include/mgpbd.h).
+"""ctypes binding of libmgpbd.so (the C ABI declared in include/mgpbd.h and
+include/mgpbd_local.h).
 
 The library is built in-tree by `controllable_pbd_3d_gb300.build`.  Loading
 never falls back to another implementation: if the library is missing or a
@@ -52,6 +53,23 @@ class Params(C.Structure):
       ('compliance', f32), ('precond', i32), ('cheb_degree', i32), ('cheb_lo', f32),
       ('use_graph', i32), ('persistent', i32), ('primal', i32), ('primal_tol', f32),
   ]
+
+
+class XpbdParams(C.Structure):
+  """mgpbd_xpbd_params (include/mgpbd_local.h)."""
+  _fields_ = [('dt', f32), ('hydro_alpha', f32), ('devia_alpha', f32), ('method', i32)]
+
+
+class VbdParams(C.Structure):
+  """mgpbd_vbd_params (include/mgpbd_local.h)."""
+  _fields_ = [('dt', f32), ('damp', f32), ('youngs_modulus', f32), ('poissons_ratio', f32),
+              ('damping', f32), ('rho', f32), ('gravity', f32 * 3), ('n_iterations', i32),
+              ('method', i32)]
+
+
+XPBD_METHOD = {'default': 0, 'gauss_seidel': 1, 'graph_coloring': 2}
+VBD_METHOD = {'serial': 0, 'color': 1}
+VBD_FIELD = {'v_v': 0, 'v_p_old': 1, 'x_tilde': 2, 'Dm_inv': 3, 'rest_vol': 4}
 
 
 class Stats(C.Structure):
@@ -127,6 +145,31 @@ _SIGS = {
     'mgpbd_host_aggregate': (C.c_int, [vp, i32, i32, vp, P_i32]),
     'mgpbd_host_tet_hierarchy': (C.c_int, [vp, i32, i32, i32, P_i32, vp, vp]),
     'mgpbd_host_galerkin': (C.c_int, [i32, vp, vp, vp, vp, i32, P_i64, P_i64, vp, vp, vp, vp]),
+    # include/mgpbd_local.h
+    'mgpbd_color_elements': (C.c_int, [vp, i32, i32, i32, vp, vp, P_i32]),
+    'mgpbd_color_vertices': (C.c_int, [vp, i32, i32, i32, vp, vp, P_i32]),
+    'mgpbd_greedy_coloring': (C.c_int, [vp, vp, i32, vp, vp, P_i32]),
+    'mgpbd_xpbd_create': (C.c_int, [C.POINTER(XpbdParams), C.POINTER(vp)]),
+    'mgpbd_xpbd_destroy': (None, [vp]),
+    'mgpbd_xpbd_set_stream': (C.c_int, [vp, vp]),
+    'mgpbd_xpbd_set_mesh': (C.c_int, [vp, vp, vp, vp, vp, vp, i32, i32]),
+    'mgpbd_xpbd_preupdate': (C.c_int, [vp]),
+    'mgpbd_xpbd_update': (C.c_int, [vp, i32]),
+    'mgpbd_xpbd_lambdas': (C.c_int, [vp, C.POINTER(vp), C.POINTER(vp)]),
+    'mgpbd_xpbd_n_colors': (C.c_int, [vp, P_i32]),
+    'mgpbd_vbd_create': (C.c_int, [C.POINTER(VbdParams), C.POINTER(vp)]),
+    'mgpbd_vbd_destroy': (None, [vp]),
+    'mgpbd_vbd_set_stream': (C.c_int, [vp, vp]),
+    'mgpbd_vbd_set_mesh': (C.c_int, [vp, vp, vp, vp, vp, i32, i32]),
+    'mgpbd_vbd_init': (C.c_int, [vp]),
+    'mgpbd_vbd_make_prediction': (C.c_int, [vp]),
+    'mgpbd_vbd_solve': (C.c_int, [vp]),
+    'mgpbd_vbd_update_vel': (C.c_int, [vp]),
+    'mgpbd_vbd_step': (C.c_int, [vp]),
+    'mgpbd_vbd_omegas': (C.c_int, [vp, vp]),
+    'mgpbd_vbd_field': (C.c_int, [vp, i32, C.POINTER(vp), P_i64]),
+    'mgpbd_vbd_n_colors': (C.c_int, [vp, P_i32]),
+    'mgpbd_vbd_lame': (C.c_int, [vp, C.POINTER(f32), C.POINTER(f32)]),
 }
 
 _lock = threading.Lock()

@@ -11,13 +11,24 @@
 #include <vector>
 
 #include "common.h"
+#include "../../include/mgpbd_local.h"
+#include "coloring.h"
 #include "kernels.cuh"
+#include "local.cuh"
 #include "solver.h"
 #include "structure.h"
 
 struct mgpbd_solver {
   mgpbd::Solver impl;
   explicit mgpbd_solver(const mgpbd_params& p) : impl(p) {}
+};
+struct mgpbd_xpbd {
+  mgpbd::Xpbd impl;
+  explicit mgpbd_xpbd(const mgpbd_xpbd_params& p) : impl(p) {}
+};
+struct mgpbd_vbd {
+  mgpbd::Vbd impl;
+  explicit mgpbd_vbd(const mgpbd_vbd_params& p) : impl(p) {}
 };
 
 namespace {
@@ -48,6 +59,13 @@ int guarded(F&& f) {
 }
 
 cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// copies a colouring into caller arrays of the documented capacities
+void put_coloring(const mgpbd::Coloring& c, int32_t* ordered, int32_t* offsets, int32_t* n_colors) {
+  std::copy(c.ordered.begin(), c.ordered.end(), ordered);
+  std::copy(c.offsets.begin(), c.offsets.end(), offsets);
+  *n_colors = c.n_colors;
+}
 
 }  // namespace
 
@@ -463,6 +481,151 @@ int mgpbd_host_galerkin(int32_t n, const int32_t* indptr, const int32_t* indices
       std::memcpy(contrib_off, g.contrib_off.data(), sizeof(int32_t) * g.contrib_off.size());
     }
   });
+}
+
+// ---- comparison solvers (include/mgpbd_local.h) ----------------------------
+
+int mgpbd_color_elements(const int32_t* elems, int32_t n_elements, int32_t verts_per_element,
+                         int32_t n_vertices, int32_t* ordered, int32_t* offsets,
+                         int32_t* n_colors) {
+  if (!ordered || !offsets || !n_colors) return MGPBD_EINVAL;
+  return guarded([&] {
+    put_coloring(mgpbd::color_elements(elems, n_elements, verts_per_element, n_vertices), ordered,
+                 offsets, n_colors);
+  });
+}
+
+int mgpbd_color_vertices(const int32_t* elems, int32_t n_elements, int32_t verts_per_element,
+                         int32_t n_vertices, int32_t* ordered, int32_t* offsets,
+                         int32_t* n_colors) {
+  if (!ordered || !offsets || !n_colors) return MGPBD_EINVAL;
+  return guarded([&] {
+    put_coloring(mgpbd::color_vertices(elems, n_elements, verts_per_element, n_vertices), ordered,
+                 offsets, n_colors);
+  });
+}
+
+int mgpbd_greedy_coloring(const int32_t* adj_ptr, const int32_t* adj, int32_t n,
+                          int32_t* ordered, int32_t* offsets, int32_t* n_colors) {
+  if (!ordered || !offsets || !n_colors) return MGPBD_EINVAL;
+  return guarded(
+      [&] { put_coloring(mgpbd::greedy_coloring_csr(adj_ptr, adj, n), ordered, offsets, n_colors); });
+}
+
+int mgpbd_xpbd_create(const mgpbd_xpbd_params* params, mgpbd_xpbd_handle* out) {
+  if (!params || !out) return MGPBD_EINVAL;
+  *out = nullptr;
+  return guarded([&] { *out = new mgpbd_xpbd(*params); });
+}
+
+void mgpbd_xpbd_destroy(mgpbd_xpbd_handle h) { delete h; }
+
+int mgpbd_xpbd_set_stream(mgpbd_xpbd_handle h, void* stream) {
+  if (!h) return MGPBD_EINVAL;
+  h->impl.set_stream(as_stream(stream));
+  return MGPBD_OK;
+}
+
+int mgpbd_xpbd_set_mesh(mgpbd_xpbd_handle h, float* x, const float* x_ref, const float* invm,
+                        const int32_t* t_i, const float* t_m, int32_t nv, int32_t nt) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.set_mesh(x, x_ref, invm, t_i, t_m, nv, nt); });
+}
+
+int mgpbd_xpbd_preupdate(mgpbd_xpbd_handle h) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.preupdate(); });
+}
+
+int mgpbd_xpbd_update(mgpbd_xpbd_handle h, int32_t n_passes) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.update(n_passes); });
+}
+
+int mgpbd_xpbd_lambdas(mgpbd_xpbd_handle h, float** hydro, float** devia) {
+  if (!h || !hydro || !devia) return MGPBD_EINVAL;
+  *hydro = h->impl.lambda_h();
+  *devia = h->impl.lambda_d();
+  return *hydro ? MGPBD_OK : MGPBD_ESTATE;
+}
+
+int mgpbd_xpbd_n_colors(mgpbd_xpbd_handle h, int32_t* n_colors) {
+  if (!h || !n_colors) return MGPBD_EINVAL;
+  *n_colors = h->impl.n_colors();
+  return MGPBD_OK;
+}
+
+int mgpbd_vbd_create(const mgpbd_vbd_params* params, mgpbd_vbd_handle* out) {
+  if (!params || !out) return MGPBD_EINVAL;
+  *out = nullptr;
+  return guarded([&] { *out = new mgpbd_vbd(*params); });
+}
+
+void mgpbd_vbd_destroy(mgpbd_vbd_handle h) { delete h; }
+
+int mgpbd_vbd_set_stream(mgpbd_vbd_handle h, void* stream) {
+  if (!h) return MGPBD_EINVAL;
+  h->impl.set_stream(as_stream(stream));
+  return MGPBD_OK;
+}
+
+int mgpbd_vbd_set_mesh(mgpbd_vbd_handle h, float* x, const float* x_ref, const float* invm,
+                       const int32_t* t_i, int32_t nv, int32_t nt) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.set_mesh(x, x_ref, invm, t_i, nv, nt); });
+}
+
+int mgpbd_vbd_init(mgpbd_vbd_handle h) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.init(); });
+}
+
+int mgpbd_vbd_make_prediction(mgpbd_vbd_handle h) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.make_prediction(); });
+}
+
+int mgpbd_vbd_solve(mgpbd_vbd_handle h) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.solve(); });
+}
+
+int mgpbd_vbd_update_vel(mgpbd_vbd_handle h) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.update_vel(); });
+}
+
+int mgpbd_vbd_step(mgpbd_vbd_handle h) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.step(); });
+}
+
+int mgpbd_vbd_omegas(mgpbd_vbd_handle h, float* omegas) {
+  if (!h || !omegas) return MGPBD_EINVAL;
+  const auto& o = h->impl.omegas();
+  std::copy(o.begin(), o.end(), omegas);
+  return MGPBD_OK;
+}
+
+int mgpbd_vbd_field(mgpbd_vbd_handle h, int32_t field, void** dev_ptr, int64_t* count) {
+  if (!h || !dev_ptr || !count) return MGPBD_EINVAL;
+  return guarded([&] {
+    *dev_ptr = h->impl.field(field, count);
+    mgpbd::require(*dev_ptr != nullptr, MGPBD_ESTATE, "vbd: set_mesh has not been called");
+  });
+}
+
+int mgpbd_vbd_n_colors(mgpbd_vbd_handle h, int32_t* n_colors) {
+  if (!h || !n_colors) return MGPBD_EINVAL;
+  *n_colors = h->impl.n_colors();
+  return MGPBD_OK;
+}
+
+int mgpbd_vbd_lame(mgpbd_vbd_handle h, float* mu, float* lam) {
+  if (!h || !mu || !lam) return MGPBD_EINVAL;
+  *mu = h->impl.mu();
+  *lam = h->impl.lam();
+  return MGPBD_OK;
 }
 
 }  // extern "C"

@@ -3,13 +3,17 @@
 Usage (needs a checkout of JamesYang-7/Controllable_PBD_3D; not available on
 the GPU machines, which only read the committed `.npz` files):
 
-    python tests/golden/make_golden.py --ref /root/reference [--only structure|step]
+    python tests/golden/make_golden.py --ref /root/reference [--only structure|local|step]
 
 Taichi is not installed, so `taichi_cpu_shim` stands in for it (see that
 module's docstring for what it can and cannot reproduce).  The reference
 modules are imported unmodified:
 
 * `cons/tet_aggregation.py` (pure numpy/scipy) gives the aggregation;
+* `utils/graph_coloring.py` (pure numpy) gives the tet and vertex
+  colourings, and `cons/deform3d.py` (`Deform3D`, driven by
+  `cons/framework.py`) and `cons/vbd.py` (`VBDSolver`) give the comparison
+  solvers' substeps (`local.npz`);
 * `cons/mgpbd_gpu.py` (`MGPBDSolverGPU`) gives the sparsity pattern
   (`_build_sparsity_pattern`), the per-tet precompute, constraint
   gradients, matrix fill, the GPU multigrid setup (`cons/mgpcg_gpu.py`) and
@@ -345,6 +349,153 @@ def step_fixture(ref, mg, name, build, kw, substeps, out, cg_alias):
   print(f'[step] {name}{suffix}: {len(recs)} newton iterations ({time.time() - t0:.1f}s)', flush=True)
 
 
+# ----------------------------------------------------------------------------
+# comparison solvers: Deform3D (cons/deform3d.py), VBDSolver (cons/vbd.py)
+# and the greedy colourings (utils/graph_coloring.py)
+# ----------------------------------------------------------------------------
+
+COLOR_CASES = ('box5x4x5', 'cube6', 'box12x3x7', 'simple_sphere', 'spot', 'cube_tet')
+
+
+def lumped_case(xr, x0, t, pinned):
+  """The reference's mass model (utils/geom3d.py:48-59, data/tet_data.py:39-44):
+  vertex mass = sum of |vol| / 4, invm = 1 / mass (pinned -> 0), t_m = |vol|."""
+  import utils.geom3d as g3
+  _, vm, tm = g3.compute_vertex_mass(np.asarray(xr, np.float64), np.asarray(t, np.int64))
+  invm = (1.0 / vm).astype(np.float32)
+  invm[np.asarray(pinned, np.int64)] = 0.0
+  return xr, x0, t, invm, tm.astype(np.float32)
+
+
+def box_lumped(nx, ny, nz, jitter, seed):
+  xr, x0, t, _ = grid_case(nx, ny, nz, jitter, seed)
+  return lumped_case(xr, x0, t, meshgen.grid_face_vertices(nx, ny, nz, axis=1, side='max'))
+
+
+def sphere_lumped(ref, jitter, seed):
+  v, t, _ = meshgen.parse_medit_mesh(os.path.join(ref, 'assets/simple_sphere/simple_sphere.mesh'))
+  rng = np.random.default_rng(seed)
+  x0 = (v + rng.uniform(-jitter, jitter, v.shape)).astype(np.float32)
+  return lumped_case(v.astype(np.float32), x0, t, [0, 11])
+
+
+def disjoint_tets(n, jitter, seed):
+  """n separate unit-ish tets (no shared vertex): the parallel default
+  method of Deform3D then has no races and equals the serial order."""
+  rng = np.random.default_rng(seed)
+  base = np.array([[0, 0, 0], [0.1, 0, 0], [0, 0.1, 0], [0, 0, 0.1]], np.float64)
+  xr = np.concatenate([base + [0.3 * k, 0, 0] for k in range(n)]).astype(np.float32)
+  x0 = (xr + rng.uniform(-jitter, jitter, xr.shape)).astype(np.float32)
+  t = np.arange(4 * n, dtype=np.int32)
+  return lumped_case(xr, x0, t, [0])
+
+
+LOCAL_CASES = {
+    # name: (builder, solver, solver kwargs, substeps, passes per substep, gravity)
+    'xpbd_gs_box': (lambda ref: box_lumped(4, 3, 4, 0.05, 11), 'xpbd',
+                    dict(hydro_alpha=1e-5, devia_alpha=1e-4, method='gauss_seidel'), 2, 10,
+                    (0.0, -9.8, 0.0)),
+    'xpbd_color_box': (lambda ref: box_lumped(4, 3, 4, 0.05, 11), 'xpbd',
+                       dict(hydro_alpha=1e-5, devia_alpha=1e-4, method='graph_coloring'), 2, 10,
+                       (0.0, -9.8, 0.0)),
+    'xpbd_gs_sphere': (lambda ref: sphere_lumped(ref, 0.02, 3), 'xpbd',
+                       dict(hydro_alpha=0.0, devia_alpha=1e-4, method='gauss_seidel'), 2, 10,
+                       (0.0, 0.0, 0.0)),
+    'xpbd_default_disjoint': (lambda ref: disjoint_tets(24, 0.01, 5), 'xpbd',
+                              dict(hydro_alpha=1e-6, devia_alpha=1e-4, method='default'), 2, 6,
+                              (0.0, -9.8, 0.0)),
+    'vbd_serial_box': (lambda ref: box_lumped(4, 3, 4, 0.05, 11), 'vbd',
+                       dict(youngs_modulus=1e4, poissons_ratio=0.3, n_iterations=10,
+                            method='serial'), 2, 0, (0.0, -9.8, 0.0)),
+    'vbd_color_box': (lambda ref: box_lumped(4, 3, 4, 0.05, 11), 'vbd',
+                      dict(youngs_modulus=1e4, poissons_ratio=0.3, n_iterations=10,
+                           method='color'), 2, 0, (0.0, -9.8, 0.0)),
+    'vbd_color_cheb_box': (lambda ref: box_lumped(4, 3, 4, 0.05, 11), 'vbd',
+                           dict(youngs_modulus=1e4, poissons_ratio=0.3, n_iterations=8,
+                                rho=0.7, damping=0.05, method='color'), 2, 0, (0.0, -9.8, 0.0)),
+    'vbd_serial_sphere': (lambda ref: sphere_lumped(ref, 0.02, 3), 'vbd',
+                          dict(youngs_modulus=1e6, poissons_ratio=0.3, n_iterations=50,
+                               method='serial'), 1, 0, (0.0, 0.0, 0.0)),
+}
+
+LOCAL_DT = 1.0 / 300.0
+LOCAL_DAMP = 0.993
+
+
+def local_fixtures(ref, out):
+  import taichi as ti
+  from utils import graph_coloring as gc
+  import cons.deform3d as d3
+  import cons.vbd as vbd
+  from cons import framework
+  res = {}
+  for name in COLOR_CASES:
+    t0 = time.time()
+    xr, _, t, _ = (STRUCTURE_CASES[name][0])(ref)
+    nt, nv = len(t) // 4, len(xr)
+    ce = gc.color_elements(t, nt, 4, nv)
+    cv = gc.color_vertices(t, nt, 4, nv)
+    res[f'color/{name}/t_i'] = np.asarray(t, np.int32)
+    res[f'color/{name}/nv'] = np.array(nv)
+    res[f'color/{name}/elem_ordered'] = ce.ordered_indices
+    res[f'color/{name}/elem_offsets'] = np.asarray(ce.color_offsets, np.int32)
+    res[f'color/{name}/vert_ordered'] = cv.ordered_indices
+    res[f'color/{name}/vert_offsets'] = np.asarray(cv.color_offsets, np.int32)
+    print(f'[color] {name}: {ce.num_colors} tet colours, {cv.num_colors} vertex colours '
+          f'({time.time() - t0:.1f}s)', flush=True)
+  for name, (build, kind, kw, substeps, passes, g) in LOCAL_CASES.items():
+    t0 = time.time()
+    xr, x0, t, invm, tm = build(ref)
+    n, nt = len(xr), len(t) // 4
+    v_p = ti.Vector.field(3, dtype=ti.f32, shape=n)
+    v_p.from_numpy(x0)
+    v_p_ref = ti.Vector.field(3, dtype=ti.f32, shape=n)
+    v_p_ref.from_numpy(xr)
+    v_invm = ti.field(ti.f32, n)
+    v_invm.from_numpy(invm)
+    t_i = ti.field(ti.i32, len(t))
+    t_i.from_numpy(t)
+    t_m = ti.field(ti.f32, nt)
+    t_m.from_numpy(tm)
+    case = {'x_ref': xr, 'x0': x0, 't_i': np.asarray(t, np.int32), 'invm': invm, 't_m': tm,
+            'gravity': np.array(g, np.float32), 'dt': np.array(LOCAL_DT),
+            'damp': np.array(LOCAL_DAMP), 'substeps': np.array(substeps),
+            'passes': np.array(passes)}
+    traj = []
+    if kind == 'xpbd':
+      cons = d3.Deform3D(v_p, v_p_ref, v_invm, t_i, t_m, LOCAL_DT, **kw)
+      pbd = framework.pbd_framework(v_p, ti.Vector(list(g)), LOCAL_DT, LOCAL_DAMP)
+      pbd.add_cons(cons, 0)
+      pbd.init_rest_status(0)
+      for _ in range(substeps):
+        pbd.step(passes)
+        traj.append(v_p.to_numpy())
+      case['hydro_lambda'] = cons.hydro_lambda.to_numpy()
+      case['devia_lambda'] = cons.devia_lambda.to_numpy()
+      case['v_final'] = pbd.v_v.to_numpy()
+    else:
+      s = vbd.VBDSolver(v_p, v_p_ref, v_invm, t_i, t_m, ti.Vector(list(g)), LOCAL_DT,
+                        damp=LOCAL_DAMP, **kw)
+      s.init()
+      case['dm_inv'] = s.Dm_inv.to_numpy()
+      case['rest_vol'] = s.rest_vol.to_numpy()
+      case['adj_offsets'] = s.vert_adj_offsets.to_numpy()
+      case['adj_tets'] = s.vert_tet_adj.to_numpy()
+      case['adj_local'] = s.vert_local_id.to_numpy()
+      for k in range(substeps):
+        s.step(k)
+        traj.append(v_p.to_numpy())
+      case['v_final'] = s.v_v.to_numpy()
+      case['mu_lam'] = np.array([s.mu, s.lam])
+    case['x_traj'] = np.stack(traj)
+    for k, v in kw.items():
+      case['kw_' + k] = np.array(v)
+    for k, v in case.items():
+      res[f'{name}/{k}'] = v
+    print(f'[local] {name}: nv={n} nt={nt} ({time.time() - t0:.1f}s)', flush=True)
+  np.savez_compressed(os.path.join(out, 'local.npz'), **res)
+
+
 def main():
   ap = argparse.ArgumentParser()
   ap.add_argument('--ref', default='/root/reference')
@@ -354,6 +505,8 @@ def main():
   mg, ta = load_reference(a.ref)
   if a.only in (None, 'structure'):
     structure_fixtures(a.ref, mg, ta, a.out)
+  if a.only in (None, 'local'):
+    local_fixtures(a.ref, a.out)
   if a.only in (None, 'step'):
     for name, (build, kw, n) in STEP_CASES.items():
       for alias in (False, True):

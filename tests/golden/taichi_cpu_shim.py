@@ -10,6 +10,9 @@ can be stored as golden fixtures.  Installing this module as `taichi` in
   *view*, so `ti.atomic_add(field[i], v)` and `field[i] += v` update storage;
 * scalar arithmetic stays float32 (numpy's weak Python-scalar promotion);
 * kernel return values become Python floats, as Taichi returns them;
+* vector / matrix methods (`dot`, `norm_sqr`, `cross`, `outer_product`,
+  `inverse`, `determinant`, `Matrix.identity`) as float32 numpy operations
+  (inverse and determinant through float64 LAPACK);
 * `ti.svd` is the rotation-variant SVD (U, V proper rotations, the sign of
   det F carried by the last singular value), computed in float64 from
   LAPACK and rounded to float32.
@@ -47,8 +50,25 @@ class TiArray(np.ndarray):
     return np.add.reduce(np.asarray(self) * np.asarray(o))
 
   def norm_sqr(self):
-    a = np.asarray(self)
-    return np.add.reduce(a * a)
+    # sum of squares of every entry, in row-major order (vectors and
+    # matrices alike)
+    a = np.asarray(self).reshape(-1)
+    acc = a.dtype.type(0)
+    for v in a:
+      acc = acc + v * v
+    return acc
+
+  def cross(self, o):
+    a, b = np.asarray(self), np.asarray(o)
+    return np.array([a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2],
+                     a[0] * b[1] - a[1] * b[0]], dtype=a.dtype).view(TiArray)
+
+  def outer_product(self, o):
+    return np.outer(np.asarray(self), np.asarray(o)).view(TiArray)
+
+  @property
+  def n(self):
+    return self.shape[-1]
 
   def norm(self):
     return np.sqrt(self.norm_sqr())
@@ -123,6 +143,10 @@ class Matrix:
   @staticmethod
   def cols(cols):
     return np.stack([np.asarray(c) for c in cols], axis=1).view(TiArray)
+
+  @staticmethod
+  def identity(dt=f32, n=3):
+    return np.eye(n, dtype=dt).view(TiArray)
 
 
 MatrixField = TiArray

@@ -1,5 +1,6 @@
-"""The C-ABI library: it loads, exports every symbol include/mgpbd.h
-declares, and its host-only entry points validate arguments.  No GPU."""
+"""The C-ABI library: it loads, exports every symbol include/mgpbd.h and
+include/mgpbd_local.h declare, and its host-only entry points validate
+arguments.  No GPU."""
 
 import ctypes as C
 import os
@@ -14,8 +15,11 @@ from controllable_pbd_3d_gb300 import _native as N
 
 
 def declared():
-  hdr = open(os.path.join(ROOT, 'include', 'mgpbd.h')).read()
-  return sorted(set(re.findall(r'\b(mgpbd_[a-z_0-9]+)\s*\(', hdr)))
+  names = set()
+  for h in ('mgpbd.h', 'mgpbd_local.h'):
+    hdr = open(os.path.join(ROOT, 'include', h)).read()
+    names |= set(re.findall(r'\b(mgpbd_[a-z_0-9]+)\s*\(', hdr))
+  return sorted(names)
 
 
 def test_library_loads_and_exports_every_declared_symbol():
@@ -32,6 +36,11 @@ def test_library_loads_and_exports_every_declared_symbol():
 
 def test_ctypes_signatures_cover_the_header():
   assert set(N._SIGS) == set(declared())
+
+
+def test_local_params_struct_layout():
+  assert C.sizeof(N.XpbdParams) == 16
+  assert C.sizeof(N.VbdParams) == 4 * 11
 
 
 def test_params_struct_layout():
