@@ -377,6 +377,87 @@ class CpuSampler:
     return 1.0 / (NEWTON_PER_SUBSTEP * (t_other + cg_per_newton * t_cg))
 
 
+def net_forward_bytes(n, nnz):
+  """Algorithmic bytes of one weights pass of the coarse network: layer 1
+  (CSR row: indptr, column, value; 1/diag and field of each neighbour; the
+  scaled value written; 64 bf16 features written) and two fused layers
+  (column + scaled value per nonzero, the neighbour's 64 bf16 features per
+  nonzero, own features read and written), plus the field and norm passes."""
+  l1 = 4 * (n + 1) + nnz * (4 + 4 + 4 + 4 + 4) + n * (4 + 128)
+  layer = nnz * (4 + 4 + 128) + n * (128 + 128)
+  return l1 + 2 * layer + n * 16
+
+
+def learned_leg(torch, args, hbm, kind):
+  """The learned coarse correction on the same workload: pairs recorded by
+  one plain Newton iteration, the network trained on them on the GPU, then
+  the plain V-cycle PCG with its coarse sweeps replaced by the learned
+  correction, timed like the plain leg."""
+  from controllable_pbd_3d_gb300.learned import CoarseNet, coarse_energy
+  peaks_all = json.load(open(os.path.join(HERE, 'MEASURED_PEAKS.json'))) if os.path.exists(
+      os.path.join(HERE, 'MEASURED_PEAKS.json')) else {}
+  tc_peak = float(peaks_all.get('bf16_tflops', 1900.0))
+  kwr = dict(SOLVER_KW)
+  kwr.update(PLAIN_KW)
+  kwr['maxiter'] = 1
+  sr, _, _ = make_solver(torch, args.size, kwr)
+  sr.record_coarse(256, 4)
+  sr.step(0)
+  rc, ec = sr.recorded_coarse()
+  g = sr.coarse_graph().snapshot()
+  net = CoarseNet(seed=1)
+  torch.cuda.synchronize()
+  t0 = time.perf_counter()
+  losses = net.fit(g, rc, steps=600, batch=8, lr=2e-3)
+  torch.cuda.synchronize()
+  t_train = time.perf_counter() - t0
+  held = slice(max(0, rc.shape[0] - 32), rc.shape[0])
+  e_net = coarse_energy(g, rc[held], net.correction(g, rc[held])).mean().item()
+  e_plain = coarse_energy(g, rc[held], ec[held]).mean().item()
+  # the weights pass (network forward) with CUDA events on this stream
+  for _ in range(3):
+    net.weights(g)
+  t_fwd = _event_time(torch, lambda: net.weights(g), 20)
+  fb = net_forward_bytes(g.n, g.nnz)
+  flops = 2 * 2 * g.n * 128 * 64  # the two tensor-core layers
+  roof = {'kernel': 'coarse network weights pass (k_net_l1 + 2 x k_net_layer: gather + '
+                    'mma.sync bf16 tile GEMM + epilogue)', 'bound': 'hbm',
+          'achieved': round(fb / t_fwd / 1e9, 1), 'peak': hbm, 'unit': 'GB/s',
+          'frac': round(fb / t_fwd / 1e9 / hbm, 4), 'peak_kind': kind,
+          'algorithmic_bytes_per_launch': int(fb), 'launch_us': round(t_fwd * 1e6, 2),
+          'tensor_tflops': round(flops / t_fwd / 1e12, 3),
+          'tensor_frac': round(flops / t_fwd / 1e12 / tc_peak, 5),
+          'working_set_note': 'the graph (ah, columns) and the bf16 features (11 MB) stay in L2; '
+                              'the neighbour gathers are L2 traffic', 'traffic': None}
+  del sr
+  kwl = dict(SOLVER_KW)
+  kwl.update(PLAIN_KW)
+  kwl['precond'] = 'learned'
+  sl, _, _ = make_solver(torch, args.size, kwl)
+  sl.set_coarse_net(net)
+  k = max(1, min(args.steps, args.plain_steps))
+  tl, stl = time_steps(torch, sl, k, 0)
+  out = {'value': round(k / tl, 4), 'unit': UNIT, 'steps': k,
+         'newton_iters_per_step': sum(x['newton_iters'] for x in stl) / k,
+         'cg_iters_per_step': sum(x['cg_iters_total'] for x in stl) / k,
+         'learned_solves': sum(x['learned_solves'] for x in stl),
+         'fallbacks': sum(x['learned_fallbacks'] for x in stl),
+         'rejected': sum(x['learned_rejected'] for x in stl),
+         'config': 'the plain leg with the coarse sweeps replaced by e_c = w * r_c / diag(A_c), '
+                   'w = c sigmoid(y), c = 1.9 / row sums of |Ah|, y from the 3-layer '
+                   'message-passing network (hidden 64, bf16 tensor-core layers) on the '
+                   'level-1 graph, computed once per Newton iteration; judge threshold 0.1 of '
+                   'the plain coarse-energy decrease',
+         'train': {'pairs': int(rc.shape[0]), 'adam_steps': 600, 'batch': 8,
+                   'seconds': round(t_train, 3), 'loss_first10': float(losses[:10].mean()),
+                   'loss_last20': float(losses[-20:].mean()),
+                   'coarse_energy_network': e_net, 'coarse_energy_plain_sweeps': e_plain},
+         'roofline': roof}
+  del sl
+  torch.cuda.empty_cache()
+  return out
+
+
 def run_ours(args):
   import torch
   ws, rank, local = dist_init(args)
@@ -471,6 +552,11 @@ def run_ours(args):
   if plain is not None:
     out['plain_fp32_amg_pcg'] = plain
     out['speedup_vs_plain'] = round(value / ws / plain['value'], 2)
+  if not args.no_learned:
+    lrn = learned_leg(torch, args, hbm, kind)
+    if plain is not None:
+      lrn['speedup_vs_plain'] = round(lrn['value'] / plain['value'], 3)
+    out['learned_amg_pcg'] = lrn
   if rank == 0 and not args.no_cpu_baseline:
     cpu = CpuSampler(args.size)
     cpu.sample()  # warm-up (first-touch of the host arrays)
@@ -565,6 +651,7 @@ def main():
   ap.add_argument('--no-cpu-baseline', action='store_true')
   ap.add_argument('--no-plain', action='store_true')
   ap.add_argument('--plain-steps', type=int, default=1)
+  ap.add_argument('--no-learned', action='store_true')
   # same kernels launched from a host loop instead of one CUDA graph per
   # CG solve (ncu cannot profile kernels inside conditional graphs)
   ap.add_argument('--no-graph', action='store_true')

@@ -30,6 +30,12 @@ MGPBD_COARSE_JACOBI = 0
 MGPBD_COARSE_DENSE_F64 = 1
 MGPBD_SMOOTH_JACOBI = 0
 MGPBD_SMOOTH_JACOBI_SAFE = 1
+MGPBD_PRECOND_VCYCLE = 0
+MGPBD_PRECOND_CHEB = 1
+MGPBD_PRECOND_LEARNED = 2
+MGPBD_NET_PARAMS = 16769
+MGPBD_NET_LOSS_WEIGHTS = 0
+MGPBD_NET_LOSS_FIELD = 1
 
 STATUS_NAN = 1
 STATUS_PAP_NONPOS = 2
@@ -52,6 +58,7 @@ class Params(C.Structure):
       ('max_coarse', i32), ('kinematic_pins', i32), ('coarse_sweeps', i32), ('cg_alias', i32),
       ('compliance', f32), ('precond', i32), ('cheb_degree', i32), ('cheb_lo', f32),
       ('use_graph', i32), ('persistent', i32), ('primal', i32), ('primal_tol', f32),
+      ('learned_accept', f32),
   ]
 
 
@@ -78,7 +85,9 @@ class Stats(C.Structure):
       ('residual0', f64), ('residual', f64), ('omega_last', f64), ('status', C.c_uint32),
       ('nnz', i64 * 8), ('rows', i64 * 8), ('cg_path', i32), ('cg_grid', i32),
       ('cg_iters_warm', i32), ('cg_launches', i32), ('ms_warm', f64), ('ms_dual', f64),
-      ('warm_amp', f64), ('warm_declined', i32), ('pad', i32),
+      ('warm_amp', f64), ('warm_declined', i32), ('learned_fallbacks', i32),
+      ('learned_rejected', i32), ('learned_solves', i32), ('coarse_energy_learned', f64),
+      ('coarse_energy_plain', f64),
   ]
 
 
@@ -141,6 +150,19 @@ _SIGS = {
     'mgpbd_xpay': (C.c_int, [i32, f32, vp, vp, vp]),
     'mgpbd_scale': (C.c_int, [i32, f32, vp, vp]),
     'mgpbd_refill_coarse': (C.c_int, [vp]),
+    'mgpbd_net_create': (C.c_int, [C.c_uint64, C.POINTER(vp)]),
+    'mgpbd_net_destroy': (None, [vp]),
+    'mgpbd_net_params': (C.c_int, [vp, C.POINTER(vp), C.POINTER(vp)]),
+    'mgpbd_net_sync_params': (C.c_int, [vp, vp]),
+    'mgpbd_net_forward': (C.c_int, [vp, i32, i64, vp, vp, vp, vp, vp, vp, vp]),
+    'mgpbd_net_weights': (C.c_int, [vp, i32, i64, vp, vp, vp, vp, vp, vp]),
+    'mgpbd_net_apply': (C.c_int, [i32, vp, vp, vp, vp, vp]),
+    'mgpbd_net_loss_grad': (C.c_int, [vp, i32, i64, vp, vp, vp, vp, vp, i32, i32, P_f64, vp]),
+    'mgpbd_net_adam': (C.c_int, [vp, f32, f32, f32, f32, vp]),
+    'mgpbd_net_train': (C.c_int, [vp, i32, i64, vp, vp, vp, vp, vp, i32, i32, i32, f32, vp, vp]),
+    'mgpbd_set_coarse_net': (C.c_int, [vp, vp]),
+    'mgpbd_record_coarse': (C.c_int, [vp, vp, vp, i32, i32]),
+    'mgpbd_record_count': (C.c_int, [vp, P_i32]),
     'mgpbd_host_pattern': (C.c_int, [vp, i32, P_i64, vp, vp]),
     'mgpbd_host_aggregate': (C.c_int, [vp, i32, i32, vp, P_i32]),
     'mgpbd_host_tet_hierarchy': (C.c_int, [vp, i32, i32, i32, P_i32, vp, vp]),
@@ -155,6 +177,7 @@ _SIGS = {
     'mgpbd_xpbd_set_mesh': (C.c_int, [vp, vp, vp, vp, vp, vp, i32, i32]),
     'mgpbd_xpbd_preupdate': (C.c_int, [vp]),
     'mgpbd_xpbd_update': (C.c_int, [vp, i32]),
+    'mgpbd_xpbd_synchronize': (C.c_int, [vp]),
     'mgpbd_xpbd_lambdas': (C.c_int, [vp, C.POINTER(vp), C.POINTER(vp)]),
     'mgpbd_xpbd_n_colors': (C.c_int, [vp, P_i32]),
     'mgpbd_vbd_create': (C.c_int, [C.POINTER(VbdParams), C.POINTER(vp)]),
@@ -166,6 +189,7 @@ _SIGS = {
     'mgpbd_vbd_solve': (C.c_int, [vp]),
     'mgpbd_vbd_update_vel': (C.c_int, [vp]),
     'mgpbd_vbd_step': (C.c_int, [vp]),
+    'mgpbd_vbd_synchronize': (C.c_int, [vp]),
     'mgpbd_vbd_omegas': (C.c_int, [vp, vp]),
     'mgpbd_vbd_field': (C.c_int, [vp, i32, C.POINTER(vp), P_i64]),
     'mgpbd_vbd_n_colors': (C.c_int, [vp, P_i32]),

@@ -15,12 +15,17 @@
 #include "coloring.h"
 #include "kernels.cuh"
 #include "local.cuh"
+#include "mpnn.cuh"
 #include "solver.h"
 #include "structure.h"
 
 struct mgpbd_solver {
   mgpbd::Solver impl;
   explicit mgpbd_solver(const mgpbd_params& p) : impl(p) {}
+};
+struct mgpbd_net {
+  mgpbd::CoarseNet impl;
+  explicit mgpbd_net(uint64_t seed) : impl(seed) {}
 };
 struct mgpbd_xpbd {
   mgpbd::Xpbd impl;
@@ -103,6 +108,7 @@ void mgpbd_default_params(mgpbd_params* p) {
   p->persistent = 1;
   p->primal = 0;
   p->primal_tol = 1e-2f;
+  p->learned_accept = 0.1f;
 }
 
 const char* mgpbd_strerror(int code) {
@@ -264,6 +270,128 @@ int mgpbd_pcg(mgpbd_handle h, const float* b, float* x, int32_t* cg_iters) {
     int32_t it = h->impl.pcg(b, x);
     if (cg_iters) *cg_iters = it;
   });
+}
+
+// ---- learned coarse correction -------------------------------------------
+
+namespace {
+mgpbd::NetGraph net_graph(int32_t n, int64_t nnz, const int32_t* indptr, const int32_t* indices,
+                          const float* data, const float* diag_inv) {
+  mgpbd::require(n > 0 && nnz >= n && indptr && indices && data && diag_inv, MGPBD_EINVAL,
+                 "net: empty graph, nnz < n or null CSR array");
+  mgpbd::NetGraph g;
+  g.n = n;
+  g.nnz = nnz;
+  g.indptr = indptr;
+  g.indices = indices;
+  g.data = data;
+  g.diag_inv = diag_inv;
+  return g;
+}
+}  // namespace
+
+int mgpbd_net_create(uint64_t seed, mgpbd_net_handle* out) {
+  if (!out) return MGPBD_EINVAL;
+  *out = nullptr;
+  return guarded([&] { *out = new mgpbd_net(seed); });
+}
+
+void mgpbd_net_destroy(mgpbd_net_handle net) { delete net; }
+
+int mgpbd_net_params(mgpbd_net_handle net, float** params, float** grad) {
+  if (!net) return MGPBD_EINVAL;
+  if (params) *params = net->impl.params();
+  if (grad) *grad = net->impl.grad();
+  return MGPBD_OK;
+}
+
+int mgpbd_net_sync_params(mgpbd_net_handle net, void* stream) {
+  if (!net) return MGPBD_EINVAL;
+  return guarded([&] { net->impl.sync_params(as_stream(stream)); });
+}
+
+int mgpbd_net_forward(mgpbd_net_handle net, int32_t n, int64_t nnz, const int32_t* indptr,
+                      const int32_t* indices, const float* data, const float* diag_inv,
+                      const float* r, float* e, void* stream) {
+  if (!net || !r || !e) return MGPBD_EINVAL;
+  return guarded([&] {
+    net->impl.forward(net_graph(n, nnz, indptr, indices, data, diag_inv), r, e, as_stream(stream));
+  });
+}
+
+int mgpbd_net_weights(mgpbd_net_handle net, int32_t n, int64_t nnz, const int32_t* indptr,
+                      const int32_t* indices, const float* data, const float* diag_inv,
+                      float* w, void* stream) {
+  if (!net || !w) return MGPBD_EINVAL;
+  return guarded([&] {
+    net->impl.weights(net_graph(n, nnz, indptr, indices, data, diag_inv), w, as_stream(stream));
+  });
+}
+
+int mgpbd_net_apply(int32_t n, const float* w, const float* diag_inv, const float* r, float* e,
+                    void* stream) {
+  if (n < 0 || (n > 0 && (!w || !diag_inv || !r || !e))) return MGPBD_EINVAL;
+  return guarded([&] {
+    if (n > 0) mgpbd::apply_coarse_weights(n, w, diag_inv, r, e, as_stream(stream));
+  });
+}
+
+int mgpbd_net_loss_grad(mgpbd_net_handle net, int32_t n, int64_t nnz, const int32_t* indptr,
+                        const int32_t* indices, const float* data, const float* diag_inv,
+                        const float* samples, int32_t n_samples, int32_t mode, double* loss,
+                        void* stream) {
+  if (!net || !samples || n_samples <= 0) return MGPBD_EINVAL;
+  return guarded([&] {
+    cudaStream_t s = as_stream(stream);
+    mgpbd::DevBuf<double> d(1);
+    net->impl.loss_grad(net_graph(n, nnz, indptr, indices, data, diag_inv), samples, n_samples, 0,
+                        n_samples, d.p, mode, s);
+    double h = 0.0;
+    MGPBD_CUDA(cudaMemcpyAsync(&h, d.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+    MGPBD_CUDA(cudaStreamSynchronize(s));
+    if (loss) *loss = h;
+  });
+}
+
+int mgpbd_net_adam(mgpbd_net_handle net, float lr, float beta1, float beta2, float eps,
+                   void* stream) {
+  if (!net) return MGPBD_EINVAL;
+  return guarded([&] { net->impl.adam(lr, beta1, beta2, eps, as_stream(stream)); });
+}
+
+int mgpbd_net_train(mgpbd_net_handle net, int32_t n, int64_t nnz, const int32_t* indptr,
+                    const int32_t* indices, const float* data, const float* diag_inv,
+                    const float* samples, int32_t n_samples, int32_t batch, int32_t steps,
+                    float lr, double* losses, void* stream) {
+  if (!net || !samples || n_samples <= 0 || batch <= 0 || steps < 0) return MGPBD_EINVAL;
+  return guarded([&] {
+    if (steps == 0) return;
+    cudaStream_t s = as_stream(stream);
+    mgpbd::DevBuf<double> d(steps);
+    net->impl.train(net_graph(n, nnz, indptr, indices, data, diag_inv), samples, n_samples, batch,
+                    steps, lr, d.p, s);
+    std::vector<double> h(steps);
+    MGPBD_CUDA(cudaMemcpyAsync(h.data(), d.p, sizeof(double) * steps, cudaMemcpyDeviceToHost, s));
+    MGPBD_CUDA(cudaStreamSynchronize(s));
+    if (losses) std::copy(h.begin(), h.end(), losses);
+  });
+}
+
+int mgpbd_set_coarse_net(mgpbd_handle h, mgpbd_net_handle net) {
+  if (!h) return MGPBD_EINVAL;
+  h->impl.set_coarse_net(net ? &net->impl : nullptr);
+  return MGPBD_OK;
+}
+
+int mgpbd_record_coarse(mgpbd_handle h, float* rc, float* ec, int32_t capacity, int32_t every) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.record_coarse(rc, ec, capacity, every); });
+}
+
+int mgpbd_record_count(mgpbd_handle h, int32_t* count) {
+  if (!h || !count) return MGPBD_EINVAL;
+  *count = h->impl.record_count();
+  return MGPBD_OK;
 }
 
 int mgpbd_vcycle(mgpbd_handle h, const float* r, float* z) {
@@ -542,6 +670,11 @@ int mgpbd_xpbd_update(mgpbd_xpbd_handle h, int32_t n_passes) {
   return guarded([&] { h->impl.update(n_passes); });
 }
 
+int mgpbd_xpbd_synchronize(mgpbd_xpbd_handle h) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.synchronize(); });
+}
+
 int mgpbd_xpbd_lambdas(mgpbd_xpbd_handle h, float** hydro, float** devia) {
   if (!h || !hydro || !devia) return MGPBD_EINVAL;
   *hydro = h->impl.lambda_h();
@@ -598,6 +731,11 @@ int mgpbd_vbd_update_vel(mgpbd_vbd_handle h) {
 int mgpbd_vbd_step(mgpbd_vbd_handle h) {
   if (!h) return MGPBD_EINVAL;
   return guarded([&] { h->impl.step(); });
+}
+
+int mgpbd_vbd_synchronize(mgpbd_vbd_handle h) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.synchronize(); });
 }
 
 int mgpbd_vbd_omegas(mgpbd_vbd_handle h, float* omegas) {

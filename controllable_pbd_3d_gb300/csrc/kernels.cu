@@ -695,6 +695,19 @@ __global__ void k_cg_beta(CgState* st, const double* __restrict__ p, int blocks)
   }
 }
 
+// Restart of a CG solve from its current iterate: rz from the partials,
+// the status bits in clear_mask dropped; iteration count and tolerance kept.
+__global__ void k_cg_restart(CgState* st, const double* __restrict__ p, int blocks,
+                             int32_t clear_mask) {
+  double rz = sum_partials(p, blocks);
+  if (threadIdx.x == 0) {
+    st->rz = rz;
+    st->status &= ~clear_mask;
+    if (!isfinite(rz)) st->status |= MGPBD_STATUS_NAN;
+    st->done = (st->iters >= st->maxiter || !isfinite(rz)) ? 1 : 0;
+  }
+}
+
 __global__ void k_cg_update_p(const CgState* __restrict__ st, const float* __restrict__ z,
                               float* __restrict__ p, int64_t n) {
   if (st->done) return;
@@ -979,6 +992,11 @@ void launch_cg_check(CgState* st, const double* p, int blocks, cudaStream_t s) {
 }
 void launch_cg_beta(CgState* st, const double* p, int blocks, cudaStream_t s) {
   k_cg_beta<<<1, kThreads, 0, s>>>(st, p, blocks);
+  MGPBD_CHECK_LAUNCH();
+}
+void launch_cg_restart(CgState* st, const double* p, int blocks, int32_t clear_mask,
+                       cudaStream_t s) {
+  k_cg_restart<<<1, kThreads, 0, s>>>(st, p, blocks, clear_mask);
   MGPBD_CHECK_LAUNCH();
 }
 void launch_cg_update_p(const CgState* st, const float* z, float* p, int64_t n, cudaStream_t s) {

@@ -112,6 +112,9 @@ void launch_cg_update_xr(const CgState* st, const float* p, const float* ap, flo
                          int64_t n, double* partials, cudaStream_t s);
 void launch_cg_check(CgState* st, const double* partials_rr, int blocks, cudaStream_t s);
 void launch_cg_beta(CgState* st, const double* partials_rz, int blocks, cudaStream_t s);
+// restart from the current iterate: rz from partials, drops status bits
+void launch_cg_restart(CgState* st, const double* partials_rz, int blocks, int32_t clear_mask,
+                       cudaStream_t s);
 // p = z + beta p
 void launch_cg_update_p(const CgState* st, const float* z, float* p, int64_t n, cudaStream_t s);
 

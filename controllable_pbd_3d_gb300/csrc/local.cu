@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <string>
 
 #include "coloring.h"
 #include "persist.cuh"
@@ -509,6 +510,38 @@ void upload(DevBuf<int32_t>& d, const std::vector<int32_t>& h, cudaStream_t s) {
 
 // ---------------------------------------------------------------------------
 
+LazyStatus::~LazyStatus() {
+  if (ev_) cudaEventDestroy(ev_);
+  if (host_) cudaFreeHost(host_);
+}
+
+void LazyStatus::record(const int32_t* dev, cudaStream_t s) {
+  if (!host_) {
+    MGPBD_CUDA(cudaMallocHost(&host_, sizeof(int32_t)));
+    *host_ = 0;
+    MGPBD_CUDA(cudaEventCreateWithFlags(&ev_, cudaEventDisableTiming));
+  }
+  MGPBD_CUDA(cudaMemcpyAsync(host_, dev, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  MGPBD_CUDA(cudaEventRecord(ev_, s));
+  pending_ = true;
+}
+
+void LazyStatus::check(const char* what) {
+  if (!pending_) return;
+  const cudaError_t e = cudaEventQuery(ev_);
+  if (e == cudaErrorNotReady) return;
+  MGPBD_CUDA(e);
+  pending_ = false;
+  if (static_cast<uint32_t>(*host_) & MGPBD_STATUS_SYNC_TIMEOUT)
+    throw Error(MGPBD_ECUDA, std::string(what) + ": a grid barrier wait timed out");
+}
+
+void LazyStatus::wait(const char* what) {
+  if (!pending_) return;
+  MGPBD_CUDA(cudaEventSynchronize(ev_));
+  check(what);
+}
+
 Xpbd::Xpbd(const mgpbd_xpbd_params& p) : p_(p) {
   require(p.dt > 0.0f, MGPBD_EINVAL, "xpbd: dt must be positive");
   require(p.method >= MGPBD_XPBD_DEFAULT && p.method <= MGPBD_XPBD_GRAPH_COLORING, MGPBD_EINVAL,
@@ -557,17 +590,10 @@ void Xpbd::preupdate() {
   MGPBD_CUDA(cudaMemsetAsync(lam_d_.p, 0, sizeof(float) * nt_, stream_));
 }
 
-void Xpbd::check_status() {
-  int32_t st = 0;
-  MGPBD_CUDA(cudaMemcpyAsync(&st, status_.p, sizeof(int32_t), cudaMemcpyDeviceToHost, stream_));
-  MGPBD_CUDA(cudaStreamSynchronize(stream_));
-  if (static_cast<uint32_t>(st) & MGPBD_STATUS_SYNC_TIMEOUT)
-    throw Error(MGPBD_ECUDA, "xpbd colour kernel: a grid barrier wait timed out");
-}
-
 void Xpbd::update(int32_t passes) {
   require(x_ != nullptr, MGPBD_ESTATE, "xpbd: set_mesh has not been called");
   require(passes >= 0, MGPBD_EINVAL, "xpbd: negative pass count");
+  lazy_.check("xpbd colour kernel");
   if (passes == 0) return;
   XArgs a;
   a.x = x_;
@@ -606,7 +632,7 @@ void Xpbd::update(int32_t passes) {
   MGPBD_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(k_xpbd_color), dim3(grid_),
                                          dim3(kLT), args, 0, s));
   MGPBD_CHECK_LAUNCH();
-  check_status();
+  lazy_.record(status_.p, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -708,16 +734,9 @@ void Vbd::update_vel() {
   MGPBD_CHECK_LAUNCH();
 }
 
-void Vbd::check_status() {
-  int32_t st = 0;
-  MGPBD_CUDA(cudaMemcpyAsync(&st, status_.p, sizeof(int32_t), cudaMemcpyDeviceToHost, stream_));
-  MGPBD_CUDA(cudaStreamSynchronize(stream_));
-  if (static_cast<uint32_t>(st) & MGPBD_STATUS_SYNC_TIMEOUT)
-    throw Error(MGPBD_ECUDA, "vbd colour kernel: a grid barrier wait timed out");
-}
-
 void Vbd::solve() {
   require(inited_, MGPBD_ESTATE, "vbd: init has not been called");
+  lazy_.check("vbd colour kernel");
   if (p_.n_iterations == 0) return;
   VArgs a;
   a.x = x_;
@@ -757,7 +776,7 @@ void Vbd::solve() {
   MGPBD_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(k_vbd_color), dim3(grid_),
                                          dim3(kLT), args, 0, s));
   MGPBD_CHECK_LAUNCH();
-  check_status();
+  lazy_.record(status_.p, s);
 }
 
 void* Vbd::field(int32_t f, int64_t* count) {

@@ -15,6 +15,26 @@
 
 namespace mgpbd {
 
+// Status word of the cooperative colour kernels, read without stalling the
+// stream: each launch queues a copy into pinned host memory and an event;
+// the next call checks the copy if the event has completed (a grid barrier
+// that gave up is reported then, as MGPBD_ECUDA).
+class LazyStatus {
+ public:
+  LazyStatus() = default;
+  LazyStatus(const LazyStatus&) = delete;
+  LazyStatus& operator=(const LazyStatus&) = delete;
+  ~LazyStatus();
+  void record(const int32_t* dev, cudaStream_t s);
+  void check(const char* what);
+  void wait(const char* what);
+
+ private:
+  int32_t* host_ = nullptr;
+  cudaEvent_t ev_ = nullptr;
+  bool pending_ = false;
+};
+
 class Xpbd {
  public:
   explicit Xpbd(const mgpbd_xpbd_params& p);
@@ -23,13 +43,14 @@ class Xpbd {
                 const float* t_m, int32_t nv, int32_t nt);
   void preupdate();
   void update(int32_t passes);
+  void synchronize() { lazy_.wait("xpbd colour kernel"); }
   float* lambda_h() const { return lam_h_.p; }
   float* lambda_d() const { return lam_d_.p; }
   int32_t n_colors() const { return n_colors_; }
 
  private:
-  void check_status();
   mgpbd_xpbd_params p_;
+  LazyStatus lazy_;
   cudaStream_t stream_ = nullptr;
   float* x_ = nullptr;
   const float* invm_ = nullptr;
@@ -53,6 +74,7 @@ class Vbd {
   void make_prediction();
   void solve();
   void update_vel();
+  void synchronize() { lazy_.wait("vbd colour kernel"); }
   void step() {
     make_prediction();
     solve();
@@ -65,8 +87,8 @@ class Vbd {
   float lam() const { return lam_; }
 
  private:
-  void check_status();
   mgpbd_vbd_params p_;
+  LazyStatus lazy_;
   float mu_ = 0.0f, lam_ = 0.0f;
   std::vector<float> omegas_;
   cudaStream_t stream_ = nullptr;

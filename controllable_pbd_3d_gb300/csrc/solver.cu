@@ -5,6 +5,7 @@
 #include "zone.cuh"
 
 #include <algorithm>
+#include <limits>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -107,8 +108,11 @@ Solver::Solver(const mgpbd_params& p) : p_(p) {
   require(p.n_smooth >= 0 && p.maxiter >= 0 && p.maxiter_cg >= 0, MGPBD_EINVAL,
           "iteration counts must be non-negative");
   require(p.mode == MGPBD_MODE_PARITY || p.mode == MGPBD_MODE_FAST, MGPBD_EINVAL, "unknown mode");
-  require(p.precond == MGPBD_PRECOND_VCYCLE || p.precond == MGPBD_PRECOND_CHEB, MGPBD_EINVAL,
-          "unknown preconditioner");
+  require(p.precond == MGPBD_PRECOND_VCYCLE || p.precond == MGPBD_PRECOND_CHEB ||
+              p.precond == MGPBD_PRECOND_LEARNED,
+          MGPBD_EINVAL, "unknown preconditioner");
+  if (p.precond == MGPBD_PRECOND_LEARNED)
+    require(!p.cg_alias, MGPBD_EINVAL, "cg_alias does not combine with the learned coarse correction");
   if (p.precond == MGPBD_PRECOND_CHEB) {
     require(p.mode == MGPBD_MODE_FAST, MGPBD_EINVAL, "the Chebyshev preconditioner needs FAST mode");
     require(p.cheb_degree >= 1 && p.cheb_degree < kMaxCheb, MGPBD_EINVAL,
@@ -879,12 +883,89 @@ void Solver::vcycle(int32_t l, const float* b, const CgState* guard) {
     float* res = (l == 0 && p_.cg_alias) ? cg_r_.p : L.r.p;
     launch_residual_g(guard, L.view(), b, cur, res, stream_);
     launch_restrict_g(guard, L.mem_ptr.p, L.mem_rows.p, res, C.n, C.b.p, stream_);
-    vcycle(l + 1, C.b.p, guard);
+    if (l == 0)
+      coarse_correction(guard);
+    else
+      vcycle(l + 1, C.b.p, guard);
     launch_prolong_add_g(guard, L.agg.p, C.xa.p, L.n, cur, stream_);
     smooth_level(l, b, cur, nxt, p_.n_smooth, false, guard);
   }
   if (cur != L.xa.p)
     MGPBD_CUDA(cudaMemcpyAsync(L.xa.p, cur, sizeof(float) * L.n, cudaMemcpyDeviceToDevice, stream_));
+}
+
+// The coarse correction of the level-0 V-cycle: the recursion (the
+// reference's), the learned weights, or -- on the first V-cycle of a learned
+// solve -- both, the plain one judging the learned one by coarse energy.
+void Solver::coarse_correction(const CgState* guard) {
+  Level& C = levels_[1];
+  cudaStream_t s = stream_;
+  if (judge_pending_) {
+    judge_pending_ = false;
+    apply_coarse_weights(C.n, net_w_.p, C.diag_inv.p, C.b.p, net_e_.p, s);
+    vcycle(1, C.b.p, guard);
+    double el = coarse_energy(net_e_.p, C.b.p);
+    double ep = coarse_energy(C.xa.p, C.b.p);
+    stats_.coarse_energy_learned += el;
+    stats_.coarse_energy_plain += ep;
+    net_active_ = std::isfinite(el) && el <= static_cast<double>(p_.learned_accept) * ep;
+    if (net_active_)
+      MGPBD_CUDA(cudaMemcpyAsync(C.xa.p, net_e_.p, sizeof(float) * C.n, cudaMemcpyDeviceToDevice, s));
+    else
+      stats_.learned_rejected += 1;
+    return;
+  }
+  if (net_active_) {
+    apply_coarse_weights(C.n, net_w_.p, C.diag_inv.p, C.b.p, C.xa.p, s);
+    return;
+  }
+  vcycle(1, C.b.p, guard);
+  if (rec_count_ < rec_cap_) {
+    if (rec_calls_ % rec_every_ == 0) {
+      const int64_t off = static_cast<int64_t>(rec_count_) * C.n;
+      MGPBD_CUDA(cudaMemcpyAsync(rec_rc_ + off, C.b.p, sizeof(float) * C.n, cudaMemcpyDeviceToDevice, s));
+      MGPBD_CUDA(cudaMemcpyAsync(rec_ec_ + off, C.xa.p, sizeof(float) * C.n, cudaMemcpyDeviceToDevice, s));
+      ++rec_count_;
+    }
+    ++rec_calls_;
+  }
+}
+
+NetGraph Solver::net_graph() const {
+  const Level& C = levels_[1];
+  NetGraph g;
+  g.n = C.n;
+  g.nnz = C.nnz;
+  g.indptr = C.indptr.p;
+  g.indices = C.indices.p;
+  g.data = C.data.p;
+  g.diag_inv = C.diag_inv.p;
+  return g;
+}
+
+double Solver::coarse_energy(const float* e, const float* r) {
+  Level& C = levels_[1];
+  cudaStream_t s = stream_;
+  int blocks = reduce_blocks(C.n);
+  launch_spmv(C.view(), e, net_t_.p, s);
+  launch_dot_partials(e, net_t_.p, C.n, partials_.p, s);
+  launch_dot_partials(e, r, C.n, partials_.p + blocks, s);
+  launch_finalize(partials_.p, blocks, 2, scalars_.p + 48, s);
+  sync_read(h_buf_ + 48, scalars_.p + 48, 2 * sizeof(double));
+  return 0.5 * h_buf_[48] - h_buf_[49];
+}
+
+void Solver::record_coarse(float* rc, float* ec, int32_t capacity, int32_t every) {
+  require_init();
+  require(n_levels() >= 2, MGPBD_ESTATE, "record_coarse: the hierarchy has one level");
+  require(capacity >= 0 && every >= 1, MGPBD_EINVAL, "record_coarse: capacity < 0 or every < 1");
+  require(capacity == 0 || (rc && ec), MGPBD_EINVAL, "record_coarse: null buffer");
+  rec_rc_ = rc;
+  rec_ec_ = ec;
+  rec_cap_ = capacity;
+  rec_every_ = every;
+  rec_count_ = 0;
+  rec_calls_ = 0;
 }
 
 void Solver::precondition(const CgState* guard) {
@@ -923,11 +1004,86 @@ void Solver::cg_body(const float* b, float* x) {
   launch_cg_update_p(st, levels_[0].xa.p, cg_p_.p, n, s);
 }
 
+// PCG with the learned coarse correction (MGPBD_PRECOND_LEARNED): the
+// iterations of pcg(), with the network's weights computed once for the
+// solve, the judge on the first V-cycle and a restart from the current
+// iterate when the learned preconditioner stalls (the preconditioner is
+// linear and fixed between restarts, so standard CG applies).
+int32_t Solver::pcg_learned(const float* b, float* x) {
+  constexpr int32_t kStallWindow = 200;
+  require(net_ != nullptr, MGPBD_ESTATE,
+          "MGPBD_PRECOND_LEARNED: no coarse network attached (mgpbd_set_coarse_net)");
+  require(n_levels() >= 2, MGPBD_ESTATE, "MGPBD_PRECOND_LEARNED needs a level-1 aggregate graph");
+  require(!p_.cg_alias, MGPBD_ENOTSUP, "MGPBD_PRECOND_LEARNED does not combine with cg_alias");
+  cudaStream_t s = stream_;
+  int64_t n = nt_;
+  int blocks = reduce_blocks(n);
+  const int32_t n1 = levels_[1].n;
+  if (net_e_.n < n1) {
+    net_e_.alloc(n1);
+    net_t_.alloc(n1);
+    net_w_.alloc(n1);
+  }
+  // the network's weights for this solve's level-1 matrix
+  net_->weights(net_graph(), net_w_.p, s);
+  const size_t vb = sizeof(float) * n;
+  float* z = levels_[0].xa.p;
+  MGPBD_CUDA(cudaMemsetAsync(x, 0, vb, s));
+  MGPBD_CUDA(cudaMemcpyAsync(cg_r_.p, b, vb, cudaMemcpyDeviceToDevice, s));
+  judge_pending_ = true;
+  precondition(nullptr);
+  judge_pending_ = false;
+  MGPBD_CUDA(cudaMemcpyAsync(cg_p_.p, z, vb, cudaMemcpyDeviceToDevice, s));
+  MGPBD_CUDA(cudaMemcpyAsync(cg_z_.p, z, vb, cudaMemcpyDeviceToDevice, s));
+  launch_dot_partials(cg_r_.p, z, n, partials_.p, s);
+  launch_dot_partials(b, b, n, partials_.p + blocks, s);
+  launch_cg_init(cg_state_.p, partials_.p, blocks, p_.tol_cg, p_.rel_tol_cg, p_.maxiter_cg, s);
+  double best = std::numeric_limits<double>::infinity();
+  int32_t best_at = 0;
+  const uint32_t broken = MGPBD_STATUS_NAN | MGPBD_STATUS_PAP_NONPOS;
+  for (int32_t k = 0; k < p_.maxiter_cg; ++k) {
+    cg_body(b, x);
+    sync_read(h_state_, cg_state_.p, sizeof(CgState));
+    const bool bad = net_active_ && (static_cast<uint32_t>(h_state_->status) & broken);
+    if (h_state_->done && !bad) break;
+    if (!net_active_) continue;
+    if (h_state_->rr < best) {
+      best = h_state_->rr;
+      best_at = h_state_->iters;
+    }
+    if (bad || h_state_->iters - best_at >= kStallWindow) {
+      // fall back to the plain V-cycle from the current iterate
+      net_active_ = false;
+      stats_.learned_fallbacks += 1;
+      if (static_cast<uint32_t>(h_state_->status) & MGPBD_STATUS_NAN) {
+        MGPBD_CUDA(cudaMemsetAsync(x, 0, vb, s));
+        MGPBD_CUDA(cudaMemcpyAsync(cg_r_.p, b, vb, cudaMemcpyDeviceToDevice, s));
+      } else {
+        launch_residual(levels_[0].view(), b, x, cg_r_.p, s);
+      }
+      precondition(nullptr);
+      MGPBD_CUDA(cudaMemcpyAsync(cg_p_.p, z, vb, cudaMemcpyDeviceToDevice, s));
+      MGPBD_CUDA(cudaMemcpyAsync(cg_z_.p, z, vb, cudaMemcpyDeviceToDevice, s));
+      launch_dot_partials(cg_r_.p, z, n, partials_.p, s);
+      launch_cg_restart(cg_state_.p, partials_.p, blocks, static_cast<int32_t>(broken), s);
+      sync_read(h_state_, cg_state_.p, sizeof(CgState));
+      if (h_state_->done) break;
+    }
+  }
+  sync_read(h_state_, cg_state_.p, sizeof(CgState));
+  if (net_active_) stats_.learned_solves += 1;
+  net_active_ = false;
+  status_ |= static_cast<uint32_t>(h_state_->status);
+  return h_state_->iters;
+}
+
 // GPUMultigridSolver.solve (cons/mgpcg_gpu.py:261-329)
 int32_t Solver::pcg(const float* b, float* x) {
   require_init();
   if (cheb()) return pcg_cheb(b, x);
-  if (p_.mode == MGPBD_MODE_FAST && p_.use_graph && b == rhs_.p && x == dlam_.p)
+  if (learned()) return pcg_learned(b, x);
+  if (p_.mode == MGPBD_MODE_FAST && p_.use_graph && b == rhs_.p && x == dlam_.p &&
+      rec_count_ >= rec_cap_)
     return pcg_graph(b, x);
   cudaStream_t s = stream_;
   int64_t n = nt_;
@@ -1097,6 +1253,11 @@ void Solver::solve(int32_t frame) {
   stats_.ms_dual = 0.0;
   stats_.warm_amp = 0.0;
   stats_.warm_declined = 0;
+  stats_.learned_fallbacks = 0;
+  stats_.learned_rejected = 0;
+  stats_.learned_solves = 0;
+  stats_.coarse_energy_learned = 0.0;
+  stats_.coarse_energy_plain = 0.0;
   log_.clear();
   auto now = [] {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();

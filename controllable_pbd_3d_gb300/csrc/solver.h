@@ -11,6 +11,7 @@
 #include "common.h"
 #include "jform.cuh"
 #include "kernels.cuh"
+#include "mpnn.cuh"
 #include "structure.h"
 
 namespace mgpbd {
@@ -80,6 +81,11 @@ class Solver {
   void level_sweep(int32_t level, int32_t op, const float* x, const float* b, float* y,
                    float omega);
 
+  // learned coarse correction (MGPBD_PRECOND_LEARNED)
+  void set_coarse_net(CoarseNet* net) { net_ = net; }
+  void record_coarse(float* rc, float* ec, int32_t capacity, int32_t every);
+  int32_t record_count() const { return rec_count_; }
+
   const mgpbd_stats& stats() const { return stats_; }
   // rows of (iteration, residual, cg_iters, omega, host seconds) of the last
   // solve, one per call the reference makes to benchmark.record_iteration
@@ -105,6 +111,15 @@ class Solver {
   // z = V-cycle(r) for the CG residual r (level-0 result left in xa)
   void precondition(const CgState* guard);
   int32_t pcg_graph(const float* b, float* x);
+  // PCG with the learned coarse correction, judged and backed up by the
+  // plain V-cycle
+  bool learned() const { return p_.precond == MGPBD_PRECOND_LEARNED; }
+  int32_t pcg_learned(const float* b, float* x);
+  // coarse correction of the level-0 V-cycle into levels_[1].xa
+  void coarse_correction(const CgState* guard);
+  NetGraph net_graph() const;
+  // 1/2 e^T A_1 e - e^T r on level 1 (host sync)
+  double coarse_energy(const float* e, const float* r);
   // FAST mode with the Chebyshev preconditioner (matrix-free A)
   bool cheb() const { return p_.precond == MGPBD_PRECOND_CHEB; }
   JView jview();
@@ -170,6 +185,15 @@ class Solver {
   float* jcg_x_ = nullptr;
   long long jgraph_init_launches_ = 0;
   long long jgraph_body_launches_ = 0;
+
+  CoarseNet* net_ = nullptr;
+  bool net_active_ = false;   // the current solve uses the network
+  bool judge_pending_ = false;
+  DevBuf<float> net_e_, net_t_, net_w_;
+  float* rec_rc_ = nullptr;
+  float* rec_ec_ = nullptr;
+  int32_t rec_cap_ = 0, rec_every_ = 1, rec_count_ = 0;
+  int64_t rec_calls_ = 0;
 
   mgpbd_stats stats_{};
   uint32_t status_ = 0;

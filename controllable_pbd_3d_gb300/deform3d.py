@@ -95,6 +95,11 @@ class Deform3D:
     self._stream()
     N.check(self._lib.mgpbd_xpbd_preupdate(self._h), 'mgpbd_xpbd_preupdate')
 
+  def synchronize(self):
+    """Wait for the queued passes and raise if a colour kernel's grid
+    barrier gave up (passes are asynchronous on the current stream)."""
+    N.check(self._lib.mgpbd_xpbd_synchronize(self._h), 'mgpbd_xpbd_synchronize')
+
   # cons/deform3d.py:44-52
   def update_cons(self, n_passes: int = 1):
     self._stream()

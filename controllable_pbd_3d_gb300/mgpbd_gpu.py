@@ -86,7 +86,12 @@ class MGPBDSolverGPU:
     compliance     > 0: alpha~ = compliance / dt^2 for every tet;
     precond        'vcycle' (reference) or 'cheb' (FAST only: Chebyshev
                    polynomial of degree cheb_degree on [lmax*cheb_lo, lmax],
-                   matrix-free operator, no CSR assembly);
+                   matrix-free operator, no CSR assembly) or 'learned' (the
+                   V-cycle with its coarse sweeps replaced by the linear
+                   correction w * r / diag(A_c), w from a trained CoarseNet
+                   attached with set_coarse_net; the plain V-cycle judges it
+                   on each solve's first V-cycle -- threshold learned_accept,
+                   see include/mgpbd.h -- and takes over on stalls);
     use_graph      FAST: one CUDA graph with a device-side loop per CG solve
                    (False: the same kernels from a host loop);
     persistent     FAST + 'cheb': each CG solve is one cooperative persistent
@@ -103,7 +108,8 @@ class MGPBDSolverGPU:
                coarse_solver='jacobi', smoother='jacobi', max_levels=0, max_coarse=400,
                kinematic_pins=False, coarse_sweeps=0, cg_alias=False, compliance=0.0,
                precond='vcycle', cheb_degree=8, cheb_lo=0.01, use_graph=True,
-               persistent=True, primal=False, primal_tol=1e-2, check_finite=True):
+               persistent=True, primal=False, primal_tol=1e-2, learned_accept=0.1,
+               check_finite=True):
     if aggregation != 'tet':
       raise NotImplementedError(
           "aggregation='pyamg' needs PyAMG's smoothed-aggregation setup, which this "
@@ -165,13 +171,14 @@ class MGPBDSolverGPU:
     p.coarse_sweeps = int(coarse_sweeps)
     p.cg_alias = int(bool(cg_alias))
     p.compliance = float(compliance)
-    p.precond = {'vcycle': 0, 'cheb': 1}[precond]
+    p.precond = {'vcycle': 0, 'cheb': 1, 'learned': 2}[precond]
     p.cheb_degree = int(cheb_degree)
     p.cheb_lo = float(cheb_lo)
     p.use_graph = int(bool(use_graph))
     p.persistent = int(bool(persistent))
     p.primal = int(bool(primal))
     p.primal_tol = float(primal_tol)
+    p.learned_accept = float(learned_accept)
     self.params = p
     h = C.c_void_p()
     N.check(self._lib.mgpbd_create(C.byref(p), C.byref(h)), 'mgpbd_create')
@@ -263,8 +270,47 @@ class MGPBDSolverGPU:
         'cg_path': ('kernels', 'persistent', 'staged', 'primal', 'primal-staged')[s.cg_path],
         'cg_grid': s.cg_grid, 'cg_iters_warm': s.cg_iters_warm, 'cg_launches': s.cg_launches,
         'ms_warm': s.ms_warm, 'ms_dual': s.ms_dual, 'warm_amp': s.warm_amp,
-        'warm_declined': s.warm_declined,
+        'warm_declined': s.warm_declined, 'learned_fallbacks': s.learned_fallbacks,
+        'learned_rejected': s.learned_rejected, 'learned_solves': s.learned_solves,
+        'coarse_energy_learned': s.coarse_energy_learned,
+        'coarse_energy_plain': s.coarse_energy_plain,
     }
+
+  # ---- learned coarse correction (no reference counterpart) ----------- #
+  def set_coarse_net(self, net):
+    """Attach a trained `CoarseNet` (or None) for precond='learned'; the
+    solver keeps a reference so the network outlives its use."""
+    self._coarse_net = net
+    N.check(self._lib.mgpbd_set_coarse_net(self._h, net._h if net is not None else None),
+            'mgpbd_set_coarse_net')
+
+  def record_coarse(self, capacity, every=1):
+    """Start recording (restricted residual, plain coarse correction) pairs
+    of level 1 from the plain V-cycles of the following solves; returns the
+    two (capacity, n1) device buffers being filled."""
+    n1 = int(self.stats()['rows'][1]) if self._inited else 0
+    if n1 == 0:
+      raise RuntimeError('record_coarse needs init() and a two-level hierarchy')
+    rc = torch.zeros((capacity, n1), dtype=torch.float32, device=self.v_p.device)
+    ec = torch.zeros_like(rc)
+    self._rec = (rc, ec)
+    N.check(self._lib.mgpbd_record_coarse(self._h, rc.data_ptr(), ec.data_ptr(), int(capacity),
+                                          int(every)), 'mgpbd_record_coarse')
+    return rc, ec
+
+  def recorded_coarse(self):
+    """The pairs stored so far: (rc[:k], ec[:k]); stops the recording."""
+    k = C.c_int32()
+    N.check(self._lib.mgpbd_record_count(self._h, C.byref(k)), 'mgpbd_record_count')
+    N.check(self._lib.mgpbd_record_coarse(self._h, None, None, 0, 1), 'mgpbd_record_coarse')
+    rc, ec = self._rec
+    return rc[:k.value], ec[:k.value]
+
+  def coarse_graph(self):
+    """The level-1 aggregate graph (CSR + 1/diag, device tensors) that the
+    learned coarse correction runs on."""
+    from .learned import CoarseGraph
+    return CoarseGraph.from_solver(self, 1)
 
   def newton_log(self):
     n = C.c_int32()

@@ -125,6 +125,11 @@ class VBDSolver:
         self.benchmark.record_iteration(n, 0.0, omega=om)
       self.benchmark.end_frame()
 
+  def synchronize(self):
+    """Wait for the queued solve and raise if the colour kernel's grid
+    barrier gave up."""
+    N.check(self._lib.mgpbd_vbd_synchronize(self._h), 'mgpbd_vbd_synchronize')
+
   def update_vel(self):
     self._stream()
     N.check(self._lib.mgpbd_vbd_update_vel(self._h), 'mgpbd_vbd_update_vel')

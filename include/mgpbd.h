@@ -134,10 +134,32 @@ typedef struct mgpbd_params {
    * CG on A only. */
   int32_t primal;
   float primal_tol;  /* relative dual residual of the hand-over (1e-2)     */
+  /* MGPBD_PRECOND_LEARNED: the judged first V-cycle of a solve keeps the
+   * network iff E_net <= learned_accept * E_plain, E = 1/2 e^T A_c e -
+   * e^T r_c of the two coarse corrections (both negative when they help):
+   * 0.1 (default) keeps a network that achieves at least a tenth of the
+   * coarse-energy decrease of the reference's sweeps (the coarse level is
+   * a small part of this system's convergence, so the test only has to
+   * catch a network that does not correct at all); 1 demands as much. */
+  float learned_accept;
 } mgpbd_params;
 
 #define MGPBD_PRECOND_VCYCLE 0
 #define MGPBD_PRECOND_CHEB 1
+/* The V-cycle with its coarse correction (the recursion below level 0,
+ * min(50, n) Jacobi sweeps on the reference's two-level hierarchy,
+ * cons/mgpcg_gpu.py:216-224) replaced by the learned linear correction
+ * e_c = w * r_c / diag(A_c), w from a trained network on the
+ * level-1 graph (mgpbd_net_*, attached with mgpbd_set_coarse_net), computed
+ * once per solve (a fixed linear preconditioner, so standard CG applies),
+ * host-checked every iteration.  The plain
+ * V-cycle stays as judge and fallback: the first V-cycle of every solve
+ * computes both coarse corrections and keeps the network only if its
+ * coarse energy 1/2 e^T A_c e - e^T r_c (lower = closer to A_c^-1 r_c in
+ * the energy norm) passes the test set by learned_accept; a solve whose residual
+ * makes no new minimum for 200 iterations (or meets p.Ap <= 0 / NaN) falls
+ * back to the plain V-cycle, restarting CG from its current iterate. */
+#define MGPBD_PRECOND_LEARNED 2
 
 typedef struct mgpbd_stats {
   int32_t newton_iters;     /* Newton iterations run in the last solve        */
@@ -158,7 +180,13 @@ typedef struct mgpbd_stats {
   double ms_dual;           /* of the dual persistent kernels, last solve     */
   double warm_amp;          /* dual residual / |b| of the primal start (last) */
   int32_t warm_declined;    /* Newton iterations whose warm start declined    */
-  int32_t pad;
+  /* MGPBD_PRECOND_LEARNED, last solve: */
+  int32_t learned_fallbacks; /* solves that fell back to the plain V-cycle     */
+  int32_t learned_rejected;  /* solves whose first coarse correction the plain
+                                V-cycle judged better (network not used)      */
+  int32_t learned_solves;    /* solves that kept the network to the end       */
+  double coarse_energy_learned; /* coarse energies of the judged first        */
+  double coarse_energy_plain;   /* V-cycle, summed over the solves            */
 } mgpbd_stats;
 
 #define MGPBD_CGPATH_KERNELS 0      /* one kernel (or graph node) per operation */
@@ -258,6 +286,91 @@ int mgpbd_level_csr(mgpbd_handle h, int32_t level, int32_t* n_rows, int64_t* nnz
 int mgpbd_level_count(mgpbd_handle h, int32_t* n_levels);
 /* Aggregate id of each row of `level` (device, length n_rows(level)). */
 int mgpbd_level_agg(mgpbd_handle h, int32_t level, int32_t** agg_ids);
+
+/* ---- learned coarse correction (no counterpart in the reference) ---------
+ * The reference's V-cycle corrects with min(50, n) Jacobi sweeps on its
+ * coarsest level (cons/mgpcg_gpu.py:216-224).  The learned correction is
+ * linear in the residual: e_c = w * r_c / diag(A_c), with one weight per
+ * aggregate computed from the level-1 matrix A_c by a 3-layer
+ * message-passing network (hidden width 64) over its graph and bounded,
+ * w_i = c_i sigmoid(y_i) with c_i = 1.9 / sum_j |Ah_ij| (below
+ * 2 / sum_j |Ah_ij| no mode is over-corrected, so the V-cycle stays
+ * positive definite; 1 / sum_j |Ah_ij| is the l1-Jacobi weight).  With
+ * s_i = (1/A_ii)^1/2 and Ah = S A_c S, the network on a node field r is
+ *   sigma = rms(S r), u = S r / sigma, a1 = Ah u
+ *   H1 = relu(u w1s + a1 w1n + b1)
+ *   H2 = relu([H1, Ah H1] W2 + b2), H3 = relu([H2, Ah H2] W3 + b3)
+ *   y = H3 wo + bo, e = sigma S y            (mgpbd_net_forward)
+ * and y is taken on the field r = sqrt(diag A_c) (mgpbd_net_weights).
+ * Parameters: one float32 vector of MGPBD_NET_PARAMS values laid out
+ *   w1s[64] w1n[64] b1[64] | W2[128][64] b2[64] | W3[128][64] b3[64] |
+ *   wo[64] bo.
+ * The dense layers run on the tensor cores with bf16 weights and
+ * activations (float32 accumulation).  Training (the library's own backward
+ * kernels and Adam) minimises the scaled coarse energy over a batch of
+ * restricted residuals r_s (u_s = S r_s / sigma_s):
+ *   MGPBD_NET_LOSS_WEIGHTS: v_s = w * u_s, L = mean_s (1/2 v_s^T Ah v_s -
+ *                           v_s^T u_s) / n  (the correction the solver uses)
+ *   MGPBD_NET_LOSS_FIELD:   L = mean_s (1/2 y_s^T Ah y_s - y_s^T u_s) / n
+ *                           with y_s the network on r_s
+ * Both are minimised by e = A_c^-1 r.  A CSR graph passed to these calls is
+ * (n, nnz, indptr[n+1], indices[nnz], data[nnz], diag_inv[n]): device
+ * arrays, column indices in [0, n), indptr[n] == nnz (not checked on the
+ * device). */
+#define MGPBD_NET_PARAMS 16769
+#define MGPBD_NET_LOSS_WEIGHTS 0
+#define MGPBD_NET_LOSS_FIELD 1
+typedef struct mgpbd_net* mgpbd_net_handle;
+/* Glorot-uniform weights from `seed` (splitmix64), zero biases. */
+int mgpbd_net_create(uint64_t seed, mgpbd_net_handle* out);
+void mgpbd_net_destroy(mgpbd_net_handle net);
+/* Device pointers of the parameter and gradient vectors (MGPBD_NET_PARAMS
+ * floats each).  After writing the parameters, call mgpbd_net_sync_params. */
+int mgpbd_net_params(mgpbd_net_handle net, float** params, float** grad);
+int mgpbd_net_sync_params(mgpbd_net_handle net, void* stream);
+/* w = per-aggregate weights of the graph (device vector of n). */
+int mgpbd_net_weights(mgpbd_net_handle net, int32_t n, int64_t nnz, const int32_t* indptr,
+                      const int32_t* indices, const float* data, const float* diag_inv,
+                      float* w, void* stream);
+/* e = max(w, 0) * diag_inv * r (device vectors of n; weights from
+ * mgpbd_net_weights are already positive). */
+int mgpbd_net_apply(int32_t n, const float* w, const float* diag_inv, const float* r, float* e,
+                    void* stream);
+/* e = the network on the field r (device vectors of n). */
+int mgpbd_net_forward(mgpbd_net_handle net, int32_t n, int64_t nnz, const int32_t* indptr,
+                      const int32_t* indices, const float* data, const float* diag_inv,
+                      const float* r, float* e, void* stream);
+/* Loss (MGPBD_NET_LOSS_*) and gradient (into the gradient vector) of the
+ * batch of n_samples residuals stored back to back (device, n_samples * n
+ * floats); *loss is host memory, the call returns after it is copied back. */
+int mgpbd_net_loss_grad(mgpbd_net_handle net, int32_t n, int64_t nnz, const int32_t* indptr,
+                        const int32_t* indices, const float* data, const float* diag_inv,
+                        const float* samples, int32_t n_samples, int32_t mode, double* loss,
+                        void* stream);
+/* One bias-corrected Adam step from the gradient vector. */
+int mgpbd_net_adam(mgpbd_net_handle net, float lr, float beta1, float beta2, float eps,
+                   void* stream);
+/* `steps` Adam steps of the MGPBD_NET_LOSS_WEIGHTS loss on batches of
+ * `batch` samples taken cyclically from the n_samples residuals (step k
+ * uses samples (k*batch + i) mod n_samples); losses (host, `steps` doubles)
+ * receives each step's loss; one host sync. */
+int mgpbd_net_train(mgpbd_net_handle net, int32_t n, int64_t nnz, const int32_t* indptr,
+                    const int32_t* indices, const float* data, const float* diag_inv,
+                    const float* samples, int32_t n_samples, int32_t batch, int32_t steps,
+                    float lr, double* losses, void* stream);
+
+/* Attach a network (or NULL) for MGPBD_PRECOND_LEARNED; the caller keeps it
+ * alive while the solver may use it.  Its coarse graph is level 1. */
+int mgpbd_set_coarse_net(mgpbd_handle h, mgpbd_net_handle net);
+/* Training data from the plain solver: while capacity > 0, every `every`-th
+ * plain V-cycle (counting from this call) stores its restricted level-1
+ * residual r_c into rc[k * n1 ...] and the plain coarse correction (the
+ * reference's coarsest-level sweeps) into ec[k * n1 ...] (device buffers
+ * of capacity * n1 floats, n1 = rows of level 1), k = 0 .. capacity-1.
+ * CG solves run from a host loop (not a CUDA graph) while recording.
+ * capacity 0 stops; mgpbd_record_count gives the pairs stored. */
+int mgpbd_record_coarse(mgpbd_handle h, float* rc, float* ec, int32_t capacity, int32_t every);
+int mgpbd_record_count(mgpbd_handle h, int32_t* count);
 
 /* ---- per-stage calls (the reference's separately callable kernels) ------ */
 /* _compute_C_and_gradC (cons/mgpbd_gpu.py:225-247) at the bound positions */

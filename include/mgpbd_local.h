@@ -77,8 +77,12 @@ int mgpbd_xpbd_set_mesh(mgpbd_xpbd_handle h, float* x, const float* x_ref, const
                         const int32_t* t_i, const float* t_m, int32_t nv, int32_t nt);
 /* preupdate_cons (:40-42): both multipliers to zero */
 int mgpbd_xpbd_preupdate(mgpbd_xpbd_handle h);
-/* update_cons (:44-52), n_passes times */
+/* update_cons (:44-52), n_passes times.  Asynchronous on the handle's
+ * stream; a grid barrier of the colour kernel that gave up is reported by a
+ * later call, or by mgpbd_xpbd_synchronize. */
 int mgpbd_xpbd_update(mgpbd_xpbd_handle h, int32_t n_passes);
+/* waits for the last update and reports its status */
+int mgpbd_xpbd_synchronize(mgpbd_xpbd_handle h);
 /* device pointers of hydro_lambda / devia_lambda (nt each) */
 int mgpbd_xpbd_lambdas(mgpbd_xpbd_handle h, float** hydro, float** devia);
 /* colours of the graph colouring method (0 for the other methods) */
@@ -118,6 +122,9 @@ int mgpbd_vbd_make_prediction(mgpbd_vbd_handle h); /* :125-132 */
 int mgpbd_vbd_solve(mgpbd_vbd_handle h);           /* :134-160 */
 int mgpbd_vbd_update_vel(mgpbd_vbd_handle h);      /* :161-166 */
 int mgpbd_vbd_step(mgpbd_vbd_handle h);            /* :168-172 */
+/* waits for the last solve and reports its status (solve, like update
+ * above, is asynchronous on the handle's stream) */
+int mgpbd_vbd_synchronize(mgpbd_vbd_handle h);
 /* the omega of each iteration of solve (n_iterations values, 1 where the
  * Chebyshev step is off), as the reference records it */
 int mgpbd_vbd_omegas(mgpbd_vbd_handle h, float* omegas);

@@ -91,3 +91,19 @@ def test_step_before_init_is_a_state_error():
     assert L.mgpbd_init(h) == -4  # no mesh bound
   finally:
     L.mgpbd_destroy(h)
+
+
+def test_stats_struct_layout_matches_the_header(tmp_path):
+  """ctypes' mgpbd_stats has the C compiler's size and field offsets."""
+  src = tmp_path / 'lay.c'
+  fields = [f for f, _ in N.Stats._fields_]
+  body = '\n'.join(f'  printf("%s %zu\\n", "{f}", offsetof(mgpbd_stats, {f}));' for f in fields)
+  src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "mgpbd.h"\nint main(void) {\n'
+                 f'  printf("size %zu\\n", sizeof(mgpbd_stats));\n{body}\n  return 0;\n}}\n')
+  exe = tmp_path / 'lay'
+  subprocess.run(['gcc', '-I', os.path.join(ROOT, 'include'), str(src), '-o', str(exe)], check=True)
+  out = dict(ln.split() for ln in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                  check=True).stdout.splitlines())
+  assert int(out['size']) == C.sizeof(N.Stats)
+  for f in fields:
+    assert int(out[f]) == getattr(N.Stats, f).offset, f

@@ -1,0 +1,351 @@
+"""Learned coarse correction (CoarseNet): the oracle's gradient against finite
+differences (CPU), the CUDA forward, backward and Adam against the oracle
+(GPU), and the network inside the solver: trained on pairs the plain solver
+records, judged by the plain V-cycle, and what it gains over the plain
+V-cycle PCG on the same Newton systems.
+
+Tolerances.  The CUDA kernels store W2, W3 and the activations H1, G1, H2, G2
+in bfloat16 (the oracle's `device=True` rounds at the same points) but sum in
+float32 in another order, so an activation near a rounding boundary can land
+one bf16 step (2^-8 relative) away from the oracle's; outputs and gradients
+are compared in relative L2 norm:
+  forward e_c          |e - e_ref| <= 1e-2 |e_ref|
+  loss                 relative 1e-3
+  gradient             |g - g_ref| <= 2e-2 |g_ref|, cosine >= 0.999
+  Adam step            float32 rounding (1e-6 relative)
+"""
+
+import time
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from oracle import mpnn_oracle as MO
+
+
+def rel_l2(a, b):
+  a = np.asarray(a, np.float64)
+  b = np.asarray(b, np.float64)
+  return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def random_spd(n, seed):
+  B = sp.random(n, n, density=0.15, random_state=seed) + sp.eye(n)
+  A = (B @ B.T + 0.5 * sp.eye(n)).tocsr()
+  A.sort_indices()
+  return A
+
+
+@pytest.mark.parametrize('mode', ['weights', 'field'])
+def test_oracle_gradient_matches_finite_differences(mode):
+  A = random_spd(30, 1)
+  g = MO.Graph(A.indptr, A.indices, A.data, 1.0 / A.diagonal())
+  p = MO.init_params(3).astype(np.float64)
+  p[MO.OFF_B1:MO.OFF_B1 + 64] = 0.1
+  p[MO.OFF_B2:MO.OFF_B2 + 64] = 0.05
+  p[MO.OFF_B3:MO.OFF_B3 + 64] = 0.05
+  rng = np.random.default_rng(0)
+  S = [rng.standard_normal(30) for _ in range(3)]
+  _, G = MO.loss_and_grad(p, g, S, device=False, mode=mode)
+  idx = np.concatenate([rng.choice(MO.N_PARAMS, 60, replace=False),
+                        [MO.OFF_BO, MO.OFF_W1S, MO.OFF_W1N + 5, MO.OFF_B1 + 3, MO.OFF_WO + 7]])
+  h = 1e-6
+  for k in idx:
+    pp, pm = p.copy(), p.copy()
+    pp[k] += h
+    pm[k] -= h
+    fd = (MO.loss_and_grad(pp, g, S, device=False, mode=mode)[0] -
+          MO.loss_and_grad(pm, g, S, device=False, mode=mode)[0]) / (2 * h)
+    assert abs(fd - G[k]) <= 1e-7 * max(1.0, abs(G[k])), k
+
+
+def test_oracle_energy_minimiser_is_the_coarse_solve():
+  """The loss is minimised by e = A^-1 r: the scaled energy of the exact
+  solve is below that of any perturbation of it."""
+  A = random_spd(25, 2)
+  g = MO.Graph(A.indptr, A.indices, A.data, 1.0 / A.diagonal())
+  r = np.random.default_rng(1).standard_normal(25)
+  e = sp.linalg.spsolve(A.tocsc(), r)
+  E0 = MO.energy(g, r, e)
+  for k in range(5):
+    d = np.random.default_rng(10 + k).standard_normal(25) * 1e-2
+    assert MO.energy(g, r, e + d) > E0
+
+
+def test_bf16_rounding_is_nearest_even():
+  x = np.array([1.0, 1.0 + 2 ** -8, 1.0 + 3 * 2 ** -8, 1.0 + 2 ** -9, -2.5, 0.0], np.float32)
+  y = MO.bf16(x)
+  assert y[0] == 1.0 and y[1] == 1.0          # tie -> even
+  assert y[2] == 1.0 + 4 * 2 ** -8            # tie -> even (up)
+  assert y[3] == 1.0 and y[4] == -2.5 and y[5] == 0.0
+
+
+# ---------------------------------------------------------------------------
+# GPU
+
+
+def cube_solver(torch, n=8, seed=3, **kw):
+  from controllable_pbd_3d_gb300 import meshgen
+  from controllable_pbd_3d_gb300.mgpbd_gpu import MGPBDSolverGPU
+  xr, t = meshgen.hex_grid_tets(n, n, n, h=1.0 / n)
+  x0, _ = meshgen.hex_grid_tets(n, n, n, h=1.0 / n, jitter=0.05, seed=seed)
+  invm = np.ones(len(xr), np.float32)
+  invm[meshgen.grid_face_vertices(n, n, n, axis=1, side='max')] = 0.0
+  x = torch.tensor(x0, device='cuda')
+  args = dict(mu=1e6, maxiter=3, rtol=1e-9, atol=0.0, maxiter_cg=4000, tol_cg=0.0,
+              rel_tol_cg=1e-6, smoother='safe', kinematic_pins=True, compliance=1.5e-6)
+  args.update(kw)
+  s = MGPBDSolverGPU(x, torch.tensor(xr, device='cuda'), torch.tensor(invm, device='cuda'),
+                     torch.tensor(t, device='cuda'), None, [0.0, -9.8, 0.0], 1.0 / 300, **args)
+  s.init()
+  return s, x
+
+
+def filled_graph(torch, s):
+  s._compute_C_and_gradC()
+  s._fill_A_and_update_gpu()
+  torch.cuda.synchronize()
+  g = s.coarse_graph().snapshot()
+  og = MO.Graph(g.indptr.cpu().numpy(), g.indices.cpu().numpy(), g.data.cpu().numpy(),
+                g.diag_inv.cpu().numpy())
+  return g, og
+
+
+def random_params(seed):
+  p = MO.init_params(seed)
+  rng = np.random.default_rng(seed + 100)
+  for off in (MO.OFF_B1, MO.OFF_B2, MO.OFF_B3):
+    p[off:off + 64] = rng.uniform(-0.1, 0.1, 64)
+  p[MO.OFF_BO] = 0.02
+  return p.astype(np.float32)
+
+
+@pytest.mark.gpu
+def test_gpu_forward_matches_oracle(cuda):
+  torch = cuda
+  from controllable_pbd_3d_gb300.learned import CoarseNet
+  s, _ = cube_solver(torch)
+  g, og = filled_graph(torch, s)
+  net = CoarseNet(seed=5)
+  p = random_params(5)
+  net.load_params(p)
+  rng = np.random.default_rng(7)
+  for k in range(3):
+    r = rng.standard_normal(g.n).astype(np.float32) * 10.0 ** (k - 1)
+    e = net.forward(g, torch.tensor(r, device='cuda')).cpu().numpy()
+    e_ref, _ = MO.forward(p, og, r, device=True)
+    assert rel_l2(e, e_ref) < 1e-2, k
+  # a zero residual gives a zero correction
+  z = net.forward(g, torch.zeros(g.n, device='cuda')).cpu().numpy()
+  assert np.all(z == 0.0)
+
+
+@pytest.mark.gpu
+def test_gpu_weights_and_correction_match_oracle(cuda):
+  torch = cuda
+  from controllable_pbd_3d_gb300.learned import CoarseNet
+  s, _ = cube_solver(torch)
+  g, og = filled_graph(torch, s)
+  net = CoarseNet(seed=4)
+  p = random_params(4)
+  net.load_params(p)
+  w = net.weights(g).cpu().numpy()
+  w_ref, _ = MO.weights(p, og, device=True)
+  assert rel_l2(w, w_ref) < 1e-2
+  r = np.random.default_rng(2).standard_normal(g.n).astype(np.float32)
+  e = net.correction(g, torch.tensor(r, device='cuda'), torch.tensor(w, device='cuda'))
+  assert rel_l2(e.cpu().numpy(), MO.apply_weights(og, w, r)) < 1e-6
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('mode', ['weights', 'field'])
+def test_gpu_gradient_matches_oracle(cuda, mode):
+  torch = cuda
+  from controllable_pbd_3d_gb300.learned import CoarseNet
+  s, _ = cube_solver(torch)
+  g, og = filled_graph(torch, s)
+  net = CoarseNet(seed=6)
+  p = random_params(6)
+  net.load_params(p)
+  rng = np.random.default_rng(8)
+  R = rng.standard_normal((4, g.n)).astype(np.float32)
+  loss = net.loss_grad(g, torch.tensor(R, device='cuda'), mode=mode)
+  grad = net.grad.cpu().numpy()
+  loss_ref, grad_ref = MO.loss_and_grad(p, og, list(R), device=True, mode=mode)
+  assert abs(loss - loss_ref) <= 1e-3 * abs(loss_ref)
+  assert rel_l2(grad, grad_ref) < 2e-2
+  cos = float(grad @ grad_ref / (np.linalg.norm(grad) * np.linalg.norm(grad_ref)))
+  assert cos > 0.999
+  # every parameter block receives its share
+  for lo, hi in ((MO.OFF_W1S, MO.OFF_W2), (MO.OFF_W2, MO.OFF_W3), (MO.OFF_W3, MO.OFF_WO),
+                 (MO.OFF_WO, MO.N_PARAMS)):
+    assert rel_l2(grad[lo:hi], grad_ref[lo:hi]) < 5e-2, (lo, hi)
+
+
+@pytest.mark.gpu
+def test_gpu_adam_step_matches_oracle(cuda):
+  torch = cuda
+  from controllable_pbd_3d_gb300.learned import CoarseNet
+  s, _ = cube_solver(torch, n=6)
+  g, _ = filled_graph(torch, s)
+  net = CoarseNet(seed=9)
+  p0 = net.state().astype(np.float64)
+  R = torch.randn((2, g.n), device='cuda')
+  m = np.zeros(MO.N_PARAMS)
+  v = np.zeros(MO.N_PARAMS)
+  p = p0
+  for t in (1, 2):
+    net.loss_grad(g, R)
+    gr = net.grad.cpu().numpy().astype(np.float64)
+    net.adam_step(lr=1e-2)
+    p, m, v = MO.adam(p, gr, m, v, t, 1e-2)
+    got = net.state().astype(np.float64)
+    assert np.abs(got - p).max() <= 1e-5 * max(1.0, np.abs(p).max())
+
+
+def record_and_train(torch, n=12, capacity=192, every=3, steps=400):
+  """Pairs from one Newton iteration of the plain solver (so every pair
+  belongs to the level-1 matrix the graph snapshot holds), then training."""
+  from controllable_pbd_3d_gb300.learned import CoarseNet
+  s, x = cube_solver(torch, n=n, maxiter=1)
+  rc, ec = s.record_coarse(capacity, every)
+  s.step(0)
+  rc, ec = s.recorded_coarse()
+  g = s.coarse_graph().snapshot()
+  net = CoarseNet(seed=1)
+  losses = net.fit(g, rc, steps=steps, batch=8, lr=2e-3)
+  return s, x, net, g, rc, ec, losses
+
+
+@pytest.mark.gpu
+def test_training_on_plain_solver_pairs_lowers_the_coarse_energy(cuda):
+  """The plain solver records (r_c, e_c) pairs; training lowers the loss,
+  and the trained correction's coarse energy is compared with the plain
+  correction's on the same residuals (lower = smaller energy-norm error)."""
+  torch = cuda
+  from controllable_pbd_3d_gb300.learned import coarse_energy
+  s, _, net, g, rc, ec, losses = record_and_train(torch)
+  assert rc.shape[0] >= 64
+  assert np.isfinite(losses).all()
+  assert losses[-20:].mean() < 0.5 * losses[:10].mean()
+  held = slice(rc.shape[0] - 32, rc.shape[0])
+  e_net = net.correction(g, rc[held])
+  E_net = coarse_energy(g, rc[held], e_net).cpu().numpy()
+  E_plain = coarse_energy(g, rc[held], ec[held]).cpu().numpy()
+  print(f'\ncoarse energy, mean over 32 recorded residuals: network {E_net.mean():.4e}, '
+        f'plain {E_plain.mean():.4e}; loss {losses[:10].mean():.4e} -> {losses[-20:].mean():.4e}')
+  assert (E_net < 0).all()  # better than no correction at all
+
+
+def newton_system(torch, precond, net=None):
+  """A solver at the first Newton system of substep 0 (A, b filled)."""
+  s, x = cube_solver(torch, n=12, precond=precond)
+  if net is not None:
+    s.set_coarse_net(net)
+  s.make_prediction()
+  s._compute_C_and_gradC()
+  s._residual_norm_gpu()
+  s._fill_A_and_update_gpu()
+  torch.cuda.synchronize()
+  return s
+
+
+@pytest.mark.gpu
+def test_learned_pcg_solution_matches_direct_solve(cuda):
+  """One Newton system solved to relative residual 1e-6 by the plain
+  V-cycle PCG and by the learned one: both solutions within 1e-4 (relative
+  max norm) of a float64 sparse direct solve of the same A and b."""
+  torch = cuda
+  from scipy.sparse.linalg import spsolve
+  _, _, net, _, _, _, _ = record_and_train(torch)
+  out = {}
+  for precond in ('vcycle', 'learned'):
+    s = newton_system(torch, precond, net if precond == 'learned' else None)
+    A0 = s._gpu_solver._gpu_As[0]
+    b = s._b_gpu.clone()
+    x = torch.zeros_like(b)
+    it = s._gpu_solver.solve(b, x)
+    torch.cuda.synchronize()
+    A = sp.csr_matrix((A0.data.cpu().numpy().astype(np.float64), A0.indices.cpu().numpy(),
+                       A0.indptr.cpu().numpy()), shape=(A0.n_rows, A0.n_rows))
+    xd = spsolve(A.tocsc(), b.cpu().numpy().astype(np.float64))
+    out[precond] = (float(np.abs(x.cpu().numpy() - xd).max() / np.abs(xd).max()), it,
+                    s.stats())
+  print(f"\nrelative error vs a float64 direct solve: plain {out['vcycle'][0]:.2e} "
+        f"({out['vcycle'][1]} CG iterations), learned {out['learned'][0]:.2e} "
+        f"({out['learned'][1]} CG iterations)")
+  assert out['vcycle'][0] < 1e-4 and out['learned'][0] < 1e-4
+
+
+@pytest.mark.gpu
+def test_learned_pcg_reports_the_gain(cuda):
+  """Same Newton steps solved by the plain V-cycle PCG (the reference's
+  min(50, n) coarse sweeps) and by the learned one (network weights judged
+  by the plain V-cycle on each solve's first V-cycle): the network is kept
+  on every solve, no solve falls back or hits maxiter_cg, the Newton
+  iterations match, and the gain in solve time over the plain V-cycle is
+  reported (asserted to be a speed-up)."""
+  torch = cuda
+  _, _, net, _, _, _, _ = record_and_train(torch)
+
+  def run(precond):
+    s2, x2 = cube_solver(torch, n=12, precond=precond)
+    if precond == 'learned':
+      s2.set_coarse_net(net)
+    s2.make_prediction()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s2.solve(0)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    return x2.cpu().numpy(), s2.stats(), dt
+
+  xp, sp_, tp = run('vcycle')
+  xl, sl, tl = run('learned')
+  assert sl['newton_iters'] == sp_['newton_iters']
+  assert sl['learned_solves'] == sl['newton_iters'] and sl['learned_fallbacks'] == 0
+  assert not (sl['status'] & 4)  # no CG solve hit maxiter_cg
+  assert np.isfinite(xl).all()
+  print(f"\nplain V-cycle PCG: {sp_['cg_iters_total']} CG iterations, {tp * 1e3:.1f} ms; "
+        f"learned: {sl['cg_iters_total']} CG iterations, {tl * 1e3:.1f} ms "
+        f"({tp / tl:.2f}x); coarse energy of the first V-cycles: network "
+        f"{sl['coarse_energy_learned']:.3e}, plain {sl['coarse_energy_plain']:.3e}")
+  assert tl < 0.8 * tp
+
+
+@pytest.mark.gpu
+def test_judge_rejects_a_worse_network(cuda):
+  """A network whose weights vanish (output bias -30: w = c sigmoid(-30))
+  gives no coarse correction to speak of; the plain V-cycle's energy test
+  rejects it on every solve, and the solve is then the plain one, bit for
+  bit."""
+  torch = cuda
+  from controllable_pbd_3d_gb300.learned import CoarseNet
+  s, x, net, g, rc, ec, _ = record_and_train(torch, steps=50)
+  bad = CoarseNet(seed=2)
+  p = net.state()
+  p[MO.OFF_WO:MO.OFF_BO] = 0.0
+  p[MO.OFF_BO] = -30.0
+  bad.load_params(p)
+  assert float(bad.weights(g).max()) < 1e-12
+  s2, x2 = cube_solver(torch, n=12, precond='learned')
+  s2.set_coarse_net(bad)
+  s2.step(0)
+  st = s2.stats()
+  assert st['learned_rejected'] == st['newton_iters'] and st['learned_solves'] == 0
+  assert st['coarse_energy_plain'] < 0.0
+  assert abs(st['coarse_energy_learned']) < 1e-9 * abs(st['coarse_energy_plain'])
+  s3, x3 = cube_solver(torch, n=12)
+  s3.step(0)
+  assert s3.stats()['cg_iters_total'] == st['cg_iters_total']
+  assert np.array_equal(x2.cpu().numpy(), x3.cpu().numpy())
+
+
+@pytest.mark.gpu
+def test_learned_precond_needs_a_network(cuda):
+  torch = cuda
+  from controllable_pbd_3d_gb300._native import MGPBDError
+  s, _ = cube_solver(torch, n=6, precond='learned')
+  with pytest.raises(MGPBDError):
+    s.step(0)

@@ -195,6 +195,7 @@ def gpu_xpbd(torch, d, method=None):
   for _ in range(int(d['substeps'])):
     fw.step(int(d['passes']))
     traj.append(x.cpu().numpy())
+  c.synchronize()  # raises if a colour kernel's grid barrier gave up
   return np.stack(traj), c, fw
 
 
@@ -210,6 +211,7 @@ def gpu_vbd(torch, d, **over):
   for k in range(int(d['substeps'])):
     s.step(k)
     traj.append(x.cpu().numpy())
+  s.synchronize()
   return np.stack(traj), s
 
 
