@@ -447,7 +447,7 @@ def learned_leg(torch, args, hbm, kind):
                    'w = c sigmoid(y), c = 1.9 / row sums of |Ah|, y from the 3-layer '
                    'message-passing network (hidden 64, bf16 tensor-core layers) on the '
                    'level-1 graph, computed once per Newton iteration; judge threshold 0.1 of '
-                   'the plain coarse-energy decrease',
+                   'the plain coarse-energy decrease, stall window 1000 CG iterations',
          'train': {'pairs': int(rc.shape[0]), 'adam_steps': 600, 'batch': 8,
                    'seconds': round(t_train, 3), 'loss_first10': float(losses[:10].mean()),
                    'loss_last20': float(losses[-20:].mean()),
@@ -605,6 +605,31 @@ def run_profile_solve(args):
                     'status': s.stats()['status']}), flush=True)
 
 
+def run_profile_net(args):
+  """The coarse network's weights pass on the level-1 graph of a
+  `--size`^3 cube (pairs from one plain Newton iteration, 100 Adam steps),
+  repeated --profile-reps times, for profilers; one JSON line."""
+  import torch
+  torch.cuda.set_device(0)
+  from controllable_pbd_3d_gb300.learned import CoarseNet
+  kwr = dict(SOLVER_KW)
+  kwr.update(PLAIN_KW)
+  kwr['maxiter'] = 1
+  sr, _, _ = make_solver(torch, args.size, kwr)
+  sr.record_coarse(64, 8)
+  sr.step(0)
+  rc, _ = sr.recorded_coarse()
+  g = sr.coarse_graph().snapshot()
+  net = CoarseNet(seed=1)
+  net.fit(g, rc, steps=100, batch=8, lr=2e-3)
+  torch.cuda.synchronize()
+  for _ in range(args.profile_reps):
+    w = net.weights(g)
+  torch.cuda.synchronize()
+  print(json.dumps({'profile_net': args.size, 'n1': g.n, 'nnz1': g.nnz,
+                    'weights_mean': float(w.mean()), 'reps': args.profile_reps}))
+
+
 def run_reference(args):
   """The reference algorithm on the host cores: the OpenMP CPU port of the
   plain step (the reference itself needs Taichi, which is not available).
@@ -662,8 +687,13 @@ def main():
   ap.add_argument('--primal', type=int, default=None, choices=[0, 1])
   # Chebyshev solve as one persistent kernel, or one kernel per phase
   ap.add_argument('--profile-path', default='persistent', choices=['persistent', 'kernels'])
+  # the coarse network's weights pass alone (for ncu)
+  ap.add_argument('--profile-net', action='store_true')
+  ap.add_argument('--profile-reps', type=int, default=5)
   args = ap.parse_args()
-  if args.profile_solve:
+  if args.profile_net:
+    run_profile_net(args)
+  elif args.profile_solve:
     run_profile_solve(args)
   elif args.impl == 'reference':
     run_reference(args)

@@ -111,8 +111,10 @@ Solver::Solver(const mgpbd_params& p) : p_(p) {
   require(p.precond == MGPBD_PRECOND_VCYCLE || p.precond == MGPBD_PRECOND_CHEB ||
               p.precond == MGPBD_PRECOND_LEARNED,
           MGPBD_EINVAL, "unknown preconditioner");
-  if (p.precond == MGPBD_PRECOND_LEARNED)
+  if (p.precond == MGPBD_PRECOND_LEARNED) {
     require(!p.cg_alias, MGPBD_EINVAL, "cg_alias does not combine with the learned coarse correction");
+    require(p.learned_stall >= 0, MGPBD_EINVAL, "learned_stall must be non-negative");
+  }
   if (p.precond == MGPBD_PRECOND_CHEB) {
     require(p.mode == MGPBD_MODE_FAST, MGPBD_EINVAL, "the Chebyshev preconditioner needs FAST mode");
     require(p.cheb_degree >= 1 && p.cheb_degree < kMaxCheb, MGPBD_EINVAL,
@@ -1010,7 +1012,6 @@ void Solver::cg_body(const float* b, float* x) {
 // iterate when the learned preconditioner stalls (the preconditioner is
 // linear and fixed between restarts, so standard CG applies).
 int32_t Solver::pcg_learned(const float* b, float* x) {
-  constexpr int32_t kStallWindow = 200;
   require(net_ != nullptr, MGPBD_ESTATE,
           "MGPBD_PRECOND_LEARNED: no coarse network attached (mgpbd_set_coarse_net)");
   require(n_levels() >= 2, MGPBD_ESTATE, "MGPBD_PRECOND_LEARNED needs a level-1 aggregate graph");
@@ -1051,7 +1052,7 @@ int32_t Solver::pcg_learned(const float* b, float* x) {
       best = h_state_->rr;
       best_at = h_state_->iters;
     }
-    if (bad || h_state_->iters - best_at >= kStallWindow) {
+    if (bad || (p_.learned_stall > 0 && h_state_->iters - best_at >= p_.learned_stall)) {
       // fall back to the plain V-cycle from the current iterate
       net_active_ = false;
       stats_.learned_fallbacks += 1;

@@ -108,7 +108,7 @@ class MGPBDSolverGPU:
                coarse_solver='jacobi', smoother='jacobi', max_levels=0, max_coarse=400,
                kinematic_pins=False, coarse_sweeps=0, cg_alias=False, compliance=0.0,
                precond='vcycle', cheb_degree=8, cheb_lo=0.01, use_graph=True,
-               persistent=True, primal=False, primal_tol=1e-2, learned_accept=0.1,
+               persistent=True, primal=False, primal_tol=1e-2, learned_accept=0.1, learned_stall=1000,
                check_finite=True):
     if aggregation != 'tet':
       raise NotImplementedError(
@@ -179,6 +179,7 @@ class MGPBDSolverGPU:
     p.primal = int(bool(primal))
     p.primal_tol = float(primal_tol)
     p.learned_accept = float(learned_accept)
+    p.learned_stall = int(learned_stall)
     self.params = p
     h = C.c_void_p()
     N.check(self._lib.mgpbd_create(C.byref(p), C.byref(h)), 'mgpbd_create')

@@ -142,6 +142,12 @@ typedef struct mgpbd_params {
    * a small part of this system's convergence, so the test only has to
    * catch a network that does not correct at all); 1 demands as much. */
   float learned_accept;
+  /* MGPBD_PRECOND_LEARNED: a solve whose CG residual makes no new minimum
+   * for this many iterations (default 1000) falls back to the plain
+   * V-cycle (restarting CG from its iterate); 0 disables the test (p.Ap <= 0
+   * and NaN still fall back).  CG residual norms plateau for a few hundred
+   * iterations in ordinary solves of stiff bodies. */
+  int32_t learned_stall;
 } mgpbd_params;
 
 #define MGPBD_PRECOND_VCYCLE 0
@@ -156,9 +162,10 @@ typedef struct mgpbd_params {
  * V-cycle stays as judge and fallback: the first V-cycle of every solve
  * computes both coarse corrections and keeps the network only if its
  * coarse energy 1/2 e^T A_c e - e^T r_c (lower = closer to A_c^-1 r_c in
- * the energy norm) passes the test set by learned_accept; a solve whose residual
- * makes no new minimum for 200 iterations (or meets p.Ap <= 0 / NaN) falls
- * back to the plain V-cycle, restarting CG from its current iterate. */
+ * the energy norm) passes the test set by learned_accept; a solve whose
+ * residual makes no new minimum for learned_stall iterations (or meets
+ * p.Ap <= 0 / NaN) falls back to the plain V-cycle, restarting CG from its
+ * current iterate. */
 #define MGPBD_PRECOND_LEARNED 2
 
 typedef struct mgpbd_stats {
