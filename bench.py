@@ -333,9 +333,11 @@ def roofline_csr(torch, s, hbm_peak, peak_kind, reps=40):
                  'frac': round(achieved / hbm_peak, 4), 'peak_kind': peak_kind,
                  'algorithmic_bytes_per_launch': bytes_, 'launch_us': round(dt * 1e6, 2),
                  'traffic': None}
+  code = s.row_shape(0) or 406
+  g, u = divmod(code, 100)
   roof = dict(out['jacobi'])
-  roof['kernel'] = 'k_csr_rows_vec<4,6,kJacobi> (level-0 weighted Jacobi sweep, CSR)'
-  roof['spmv'] = dict(out['spmv'], kernel='k_csr_rows_vec<4,6,kSpmv> (level-0 SpMV, CSR)')
+  roof['kernel'] = f'k_csr_rows_vec<{g},{u},kJacobi> (level-0 weighted Jacobi sweep, CSR)'
+  roof['spmv'] = dict(out['spmv'], kernel=f'k_csr_rows_vec<{g},{u},kSpmv> (level-0 SpMV, CSR)')
   return roof
 
 
@@ -435,11 +437,13 @@ def learned_leg(torch, args, hbm, kind):
   kwl['precond'] = 'learned'
   sl, _, _ = make_solver(torch, args.size, kwl)
   sl.set_coarse_net(net)
+  shapes = sl.autotune(reps=5)
   k = max(1, min(args.steps, args.plain_steps))
   tl, stl = time_steps(torch, sl, k, 0)
   out = {'value': round(k / tl, 4), 'unit': UNIT, 'steps': k,
          'newton_iters_per_step': sum(x['newton_iters'] for x in stl) / k,
          'cg_iters_per_step': sum(x['cg_iters_total'] for x in stl) / k,
+         'row_shapes': {str(l): c for l, c in shapes.items()},
          'learned_solves': sum(x['learned_solves'] for x in stl),
          'fallbacks': sum(x['learned_fallbacks'] for x in stl),
          'rejected': sum(x['learned_rejected'] for x in stl),
@@ -520,6 +524,8 @@ def run_ours(args):
     kwp = dict(SOLVER_KW)
     kwp.update(PLAIN_KW)
     sp_, xp, _ = make_solver(torch, args.size, kwp)
+    # the row-kernel tile shape of each level, picked by timing (autotuner)
+    shapes = sp_.autotune(reps=5)
     # no warm-up step: the plain path captures nothing and each substep
     # takes ~40 s; its first substep is timed
     k_plain = max(1, min(args.steps, args.plain_steps))
@@ -530,6 +536,8 @@ def run_ours(args):
              'cg_iters_per_step': sum(x['cg_iters_total'] for x in stp) / k_plain,
              'config': 'parity-mode CSR V-cycle (2-level tet aggregation, 50 coarse Jacobi '
                        'sweeps, smoother weight min(2/3, 4/(3 lambda_max))), host-checked loops',
+             'row_shapes': {str(l): c for l, c in shapes.items()},
+             'row_shape_us': {str(l): round(t, 2) for l, (_, t) in sp_.last_tuning.items()},
              'roofline': roof_csr}
     del sp_
     torch.cuda.empty_cache()

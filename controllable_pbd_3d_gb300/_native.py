@@ -161,6 +161,10 @@ _SIGS = {
     'mgpbd_net_adam': (C.c_int, [vp, f32, f32, f32, f32, vp]),
     'mgpbd_net_train': (C.c_int, [vp, i32, i64, vp, vp, vp, vp, vp, i32, i32, i32, f32, vp, vp]),
     'mgpbd_set_coarse_net': (C.c_int, [vp, vp]),
+    'mgpbd_row_shapes': (C.c_int, [vp, P_i32]),
+    'mgpbd_autotune_rows': (C.c_int, [vp, i32, vp, vp]),
+    'mgpbd_level_row_shape': (C.c_int, [vp, i32, P_i32]),
+    'mgpbd_set_level_row_shape': (C.c_int, [vp, i32, i32]),
     'mgpbd_record_coarse': (C.c_int, [vp, vp, vp, i32, i32]),
     'mgpbd_record_count': (C.c_int, [vp, P_i32]),
     'mgpbd_host_pattern': (C.c_int, [vp, i32, P_i64, vp, vp]),

@@ -378,6 +378,30 @@ int mgpbd_net_train(mgpbd_net_handle net, int32_t n, int64_t nnz, const int32_t*
   });
 }
 
+int mgpbd_autotune_rows(mgpbd_handle h, int32_t reps, int32_t* codes, float* us_per_sweep) {
+  if (!h || reps < 1) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.autotune_rows(reps, codes, us_per_sweep); });
+}
+
+int mgpbd_level_row_shape(mgpbd_handle h, int32_t level, int32_t* code) {
+  if (!h || !code) return MGPBD_EINVAL;
+  return guarded([&] { *code = h->impl.level_row_shape(level); });
+}
+
+int mgpbd_set_level_row_shape(mgpbd_handle h, int32_t level, int32_t code) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.set_level_row_shape(level, code); });
+}
+
+int mgpbd_row_shapes(int32_t* codes, int32_t* count) {
+  if (!count) return MGPBD_EINVAL;
+  return guarded([&] {
+    if (codes)
+      for (int i = 0; i < mgpbd::kNumRowShapes; ++i) codes[i] = mgpbd::row_shape_code(i);
+    *count = mgpbd::kNumRowShapes;
+  });
+}
+
 int mgpbd_set_coarse_net(mgpbd_handle h, mgpbd_net_handle net) {
   if (!h) return MGPBD_EINVAL;
   h->impl.set_coarse_net(net ? &net->impl : nullptr);

@@ -497,25 +497,50 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// Tile shapes of the vectorised row kernel: G lanes per row, each loading U
+// float4 (value) + int4 (column) pairs per pass, so one pass covers 4*G*U
+// nonzeros of a row.  Index 0 is the default for long rows (4 x 6: the
+// ~81-nonzero rows of the level-0 ARAP matrix, SpMV 5.0 TB/s on GB300 at
+// 40^3 against 4.3 for 8 x 4 and 4.8 for 4 x 8), index 1 for shorter rows;
+// tune_row_shape picks among all of them by timing.
+constexpr int kRowShapeG[kNumRowShapes] = {4, 4, 4, 2, 2, 4, 8, 8};
+constexpr int kRowShapeU[kNumRowShapes] = {6, 4, 8, 4, 8, 2, 2, 4};
+
+template <int OP>
+void launch_vec_shape(int idx, const CsrView& a, const float* x, const float* b, float* y,
+                      float w, double* partials, const CgState* st, cudaStream_t s,
+                      const float* wp) {
+  const int G = kRowShapeG[idx];
+  const int grid = OP == kSpmvDot ? reduce_blocks(a.n) : grid_for(a.n, kThreads / G);
+  switch (idx) {
+#define MGPBD_VEC_CASE(I, GG, UU)                                                            \
+  case I:                                                                                    \
+    k_csr_rows_vec<GG, UU, OP><<<grid, kThreads, 0, s>>>(a.n, a.indptr, a.indices, a.data, x, \
+                                                         b, a.diag_inv, y, w, wp, partials, st); \
+    break;
+    MGPBD_VEC_CASE(0, 4, 6)
+    MGPBD_VEC_CASE(1, 4, 4)
+    MGPBD_VEC_CASE(2, 4, 8)
+    MGPBD_VEC_CASE(3, 2, 4)
+    MGPBD_VEC_CASE(4, 2, 8)
+    MGPBD_VEC_CASE(5, 4, 2)
+    MGPBD_VEC_CASE(6, 8, 2)
+    MGPBD_VEC_CASE(7, 8, 4)
+#undef MGPBD_VEC_CASE
+    default:
+      throw Error(MGPBD_EINVAL, "unknown row-kernel shape");
+  }
+  MGPBD_CHECK_LAUNCH();
+}
+
 template <int OP>
 void rows_dispatch(const CsrView& a, const float* x, const float* b, float* y, float w,
                    double* partials, const CgState* st, cudaStream_t s, const float* wp = nullptr) {
   if (a.n <= 0) return;
   double avg = a.n ? (double)a.nnz / a.n : 0.0;
   if (a.padded && OP != kJacobiZero) {
-    // one pass of G lanes x U float4 covers 4*G*U elements of a row; 4 lanes
-    // x 6 float4 (96 elements) suits the ~81-nonzero rows of the level-0
-    // ARAP matrix: measured on GB300 at 40^3 (207 MB matrix), SpMV 5.0 TB/s
-    // against 4.3 TB/s for 8 x 4 and 4.8 TB/s for 4 x 8
-    const int G = 4;
-    int grid = OP == kSpmvDot ? reduce_blocks(a.n) : grid_for(a.n, kThreads / G);
-    if (avg >= 40)
-      k_csr_rows_vec<4, 6, OP><<<grid, kThreads, 0, s>>>(a.n, a.indptr, a.indices, a.data, x, b,
-                                                          a.diag_inv, y, w, wp, partials, st);
-    else
-      k_csr_rows_vec<4, 4, OP><<<grid, kThreads, 0, s>>>(a.n, a.indptr, a.indices, a.data, x, b,
-                                                          a.diag_inv, y, w, wp, partials, st);
-    MGPBD_CHECK_LAUNCH();
+    const int idx = a.shape >= 0 ? a.shape : (avg >= 40 ? 0 : 1);
+    launch_vec_shape<OP>(idx, a, x, b, y, w, partials, st, s, wp);
     return;
   }
   int G = avg >= 48 ? 32 : (avg >= 20 ? 16 : (avg >= 8 ? 8 : 4));
@@ -1012,6 +1037,52 @@ void launch_dense_chol_solve(const CgState* st, const double* L, int32_t n, cons
                              cudaStream_t s) {
   k_chol_solve<<<1, 256, sizeof(double) * n, s>>>(st, L, n, b, x);
   MGPBD_CHECK_LAUNCH();
+}
+
+int row_shape_code(int idx) {
+  require(idx >= 0 && idx < kNumRowShapes, MGPBD_EINVAL, "row shape index out of range");
+  return 100 * kRowShapeG[idx] + kRowShapeU[idx];
+}
+
+int row_shape_index(int code) {
+  for (int i = 0; i < kNumRowShapes; ++i)
+    if (100 * kRowShapeG[i] + kRowShapeU[i] == code) return i;
+  throw Error(MGPBD_EINVAL, "unknown row-kernel shape code (G * 100 + U)");
+}
+
+int tune_row_shape(const CsrView& a, const float* x, const float* b, float* y, int reps,
+                   cudaStream_t s, float* best_us) {
+  require(a.padded, MGPBD_EINVAL, "tune_row_shape needs a padded (library) CSR matrix");
+  require(reps >= 1, MGPBD_EINVAL, "tune_row_shape: reps must be positive");
+  cudaEvent_t e0, e1;
+  MGPBD_CUDA(cudaEventCreate(&e0));
+  MGPBD_CUDA(cudaEventCreate(&e1));
+  int best = 0;
+  float best_ms = 0.f;
+  try {
+    for (int i = 0; i < kNumRowShapes; ++i) {
+      launch_vec_shape<kJacobi>(i, a, x, b, y, 0.5f, nullptr, nullptr, s, nullptr);
+      MGPBD_CUDA(cudaEventRecord(e0, s));
+      for (int r = 0; r < reps; ++r)
+        launch_vec_shape<kJacobi>(i, a, x, b, y, 0.5f, nullptr, nullptr, s, nullptr);
+      MGPBD_CUDA(cudaEventRecord(e1, s));
+      MGPBD_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      MGPBD_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (i == 0 || ms < best_ms) {
+        best_ms = ms;
+        best = i;
+      }
+    }
+  } catch (...) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    throw;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (best_us) *best_us = 1e3f * best_ms / reps;
+  return best;
 }
 
 }  // namespace mgpbd

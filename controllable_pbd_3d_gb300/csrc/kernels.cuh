@@ -68,7 +68,20 @@ struct CsrView {
   // indices/data are 16-byte aligned and padded by >= 4 elements, so the
   // vectorised row kernel may be used
   bool padded = false;
+  // tile shape of the vectorised row kernel (index into the candidate
+  // list), -1: chosen from the mean row length
+  int shape = -1;
 };
+// candidate tile shapes of the vectorised row kernel (G lanes x U float4)
+constexpr int kNumRowShapes = 8;
+// shape index <-> code G * 100 + U (e.g. 406 = 4 lanes x 6 float4)
+int row_shape_code(int idx);
+int row_shape_index(int code);
+// times every candidate shape on `a` (reps Jacobi sweeps y = x + 0.5 D^-1
+// (b - A x) each, CUDA events on s, synchronising) and returns the fastest
+// shape's index; *best_us gets its time per sweep
+int tune_row_shape(const CsrView& a, const float* x, const float* b, float* y, int reps,
+                   cudaStream_t s, float* best_us);
 // padding (elements) the library allocates after every CSR value/index array
 constexpr int64_t kCsrPad = 8;
 // y = A x

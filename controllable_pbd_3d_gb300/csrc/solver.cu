@@ -933,6 +933,44 @@ void Solver::coarse_correction(const CgState* guard) {
   }
 }
 
+void Solver::autotune_rows(int32_t reps, int32_t* codes, float* us) {
+  require_init();
+  for (int32_t l = 0; l < n_levels(); ++l) {
+    Level& L = levels_[l];
+    MGPBD_CUDA(cudaMemsetAsync(L.xa.p, 0, sizeof(float) * L.n, stream_));
+    MGPBD_CUDA(cudaMemsetAsync(L.b.p, 0, sizeof(float) * L.n, stream_));
+    float t = 0.f;
+    CsrView v = L.view();
+    L.shape = tune_row_shape(v, L.xa.p, L.b.p, L.xb.p, reps, stream_, &t);
+    if (codes) codes[l] = row_shape_code(L.shape);
+    if (us) us[l] = t;
+  }
+  // a captured CG loop holds the old shapes
+  if (cg_exec_) {
+    cudaGraphExecDestroy(cg_exec_);
+    cg_exec_ = nullptr;
+    cg_graph_b_ = nullptr;
+    cg_graph_x_ = nullptr;
+  }
+}
+
+int32_t Solver::level_row_shape(int32_t l) const {
+  const Level& L = level(l);
+  return L.shape < 0 ? 0 : row_shape_code(L.shape);
+}
+
+void Solver::set_level_row_shape(int32_t l, int32_t code) {
+  require_init();
+  require(l >= 0 && l < n_levels(), MGPBD_EINVAL, "level out of range");
+  levels_[l].shape = code == 0 ? -1 : row_shape_index(code);
+  if (cg_exec_) {
+    cudaGraphExecDestroy(cg_exec_);
+    cg_exec_ = nullptr;
+    cg_graph_b_ = nullptr;
+    cg_graph_x_ = nullptr;
+  }
+}
+
 NetGraph Solver::net_graph() const {
   const Level& C = levels_[1];
   NetGraph g;

@@ -31,6 +31,9 @@ struct Level {
   DevBuf<float> omega;
   // host copies of the structure (kept for the level below)
   Csr host;
+  // tile shape of the vectorised row kernel on this level (-1: from the
+  // mean row length; set by the autotuner or the caller)
+  int shape = -1;
   CsrView view() const {
     CsrView v;
     v.n = n;
@@ -40,6 +43,7 @@ struct Level {
     v.data = data.p;
     v.diag_inv = diag_inv.p;
     v.padded = true;
+    v.shape = shape;
     return v;
   }
 };
@@ -80,6 +84,12 @@ class Solver {
   void restore_alpha(const float* saved);
   void level_sweep(int32_t level, int32_t op, const float* x, const float* b, float* y,
                    float omega);
+
+  // row-kernel tile shapes per level: tune all levels (codes G*100+U and
+  // the best time per Jacobi sweep), or read / set one level's
+  void autotune_rows(int32_t reps, int32_t* codes, float* us);
+  int32_t level_row_shape(int32_t l) const;
+  void set_level_row_shape(int32_t l, int32_t code);
 
   // learned coarse correction (MGPBD_PRECOND_LEARNED)
   void set_coarse_net(CoarseNet* net) { net_ = net; }

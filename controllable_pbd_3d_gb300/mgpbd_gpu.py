@@ -277,6 +277,54 @@ class MGPBDSolverGPU:
         'coarse_energy_plain': s.coarse_energy_plain,
     }
 
+  # ---- row-kernel autotuner (no reference counterpart) ---------------- #
+  def autotune(self, reps=5, cache=None):
+    """Pick the CSR row-kernel tile shape (G lanes x U float4, code
+    G*100+U) of every multigrid level by timing all candidates on the
+    level's matrix.  With `cache` (a JSON file path) levels are keyed by GPU
+    name, rows and nonzeros: when every level is found the cached shapes are
+    set without timing; otherwise all levels are tuned and the file updated.
+    Returns {level: code}."""
+    import json
+    import os
+    st = self.stats()
+    nl = st['n_levels']
+    gpu = torch.cuda.get_device_name(self.v_p.device)
+    keys = [f"{gpu}|{st['rows'][l]}|{st['nnz'][l]}" for l in range(nl)]
+    table = {}
+    if cache is not None and os.path.exists(cache):
+      with open(cache) as f:
+        table = json.load(f)
+    if cache is not None and all(k in table for k in keys):
+      for l, k in enumerate(keys):
+        N.check(self._lib.mgpbd_set_level_row_shape(self._h, l, int(table[k]['code'])),
+                'mgpbd_set_level_row_shape')
+      return {l: int(table[k]['code']) for l, k in enumerate(keys)}
+    self._stream()
+    codes = (C.c_int32 * nl)()
+    us = (C.c_float * nl)()
+    N.check(self._lib.mgpbd_autotune_rows(self._h, int(reps), codes, us), 'mgpbd_autotune_rows')
+    self.last_tuning = {l: (int(codes[l]), float(us[l])) for l in range(nl)}
+    if cache is not None:
+      for l, k in enumerate(keys):
+        table[k] = {'code': int(codes[l]), 'us_per_sweep': float(us[l])}
+      tmp = cache + '.tmp'
+      with open(tmp, 'w') as f:
+        json.dump(table, f, indent=1, sort_keys=True)
+      os.replace(tmp, cache)
+    return {l: int(codes[l]) for l in range(nl)}
+
+  def row_shape(self, level):
+    """The row-kernel shape code of a level (0: from the mean row length)."""
+    c = C.c_int32()
+    N.check(self._lib.mgpbd_level_row_shape(self._h, int(level), C.byref(c)),
+            'mgpbd_level_row_shape')
+    return c.value
+
+  def set_row_shape(self, level, code):
+    N.check(self._lib.mgpbd_set_level_row_shape(self._h, int(level), int(code)),
+            'mgpbd_set_level_row_shape')
+
   # ---- learned coarse correction (no reference counterpart) ----------- #
   def set_coarse_net(self, net):
     """Attach a trained `CoarseNet` (or None) for precond='learned'; the

@@ -379,6 +379,27 @@ int mgpbd_set_coarse_net(mgpbd_handle h, mgpbd_net_handle net);
 int mgpbd_record_coarse(mgpbd_handle h, float* rc, float* ec, int32_t capacity, int32_t every);
 int mgpbd_record_count(mgpbd_handle h, int32_t* count);
 
+/* ---- row-kernel autotuner (no counterpart in the reference) ---------------
+ * The CSR kernels of the V-cycle (SpMV, Jacobi sweep, residual) process a
+ * row with G lanes, each loading U float4 values and int4 columns per pass.
+ * The library picks (G, U) from the mean row length; the autotuner times
+ * every candidate shape on each multigrid level's own matrix instead.
+ * Shapes are named by the code G * 100 + U (e.g. 406).  A shape changes the
+ * summation order inside a row, so results can differ in the last bits
+ * between shapes; a fixed shape repeats bit for bit. */
+/* Candidate codes (codes: room for *count entries; NULL to query *count). */
+int mgpbd_row_shapes(int32_t* codes, int32_t* count);
+/* After mgpbd_init: time each candidate (reps Jacobi sweeps, CUDA events on
+ * the handle's stream, synchronising) on every level and keep the fastest;
+ * codes[l] and us_per_sweep[l] (host, n_levels entries, either may be NULL)
+ * receive the choice and its time per sweep.  Values of the level vectors
+ * are overwritten. */
+int mgpbd_autotune_rows(mgpbd_handle h, int32_t reps, int32_t* codes, float* us_per_sweep);
+/* Current shape code of a level (0: chosen from the mean row length), or set
+ * one (a code from mgpbd_row_shapes, or 0), e.g. from a cached tuning. */
+int mgpbd_level_row_shape(mgpbd_handle h, int32_t level, int32_t* code);
+int mgpbd_set_level_row_shape(mgpbd_handle h, int32_t level, int32_t code);
+
 /* ---- per-stage calls (the reference's separately callable kernels) ------ */
 /* _compute_C_and_gradC (cons/mgpbd_gpu.py:225-247) at the bound positions */
 int mgpbd_compute_constraints(mgpbd_handle h);
