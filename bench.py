@@ -264,7 +264,14 @@ def primal_iteration_bytes(nt, nv, degree):
   return degree * (140 * nt + 24 * nv) + (degree - 1) * 112 * nv + (32 + 64 + 192) * nv
 
 
-def roofline_from_steps(st, nt, nv, degree, hbm_peak, peak_kind):
+# DRAM bytes (read + write) of one launch of each persistent kernel on the
+# 40^3 workload, from one ncu capture each of `bench.py --profile-solve
+# --size 40` (dram__bytes_read.sum + dram__bytes_write.sum): almost all of it
+# is the first read of the operator data, staged on chip for the solve
+TRAFFIC_40 = {'k_pcg': 44874752, 'k_jcg': 46275840}
+
+
+def roofline_from_steps(st, nt, nv, degree, hbm_peak, peak_kind, size=40):
   """Roofline of the two persistent kernels over the timed steps, from the
   CUDA events the library records around each launch on its stream (stats
   ms_warm / ms_dual) and the iterations each ran.  The one with more GPU
@@ -295,7 +302,8 @@ def roofline_from_steps(st, nt, nv, degree, hbm_peak, peak_kind):
                 'bytes_per_cg_iteration': per_it, 'launches': n,
                 'cg_iterations_per_launch': round(its / n, 1), 'launch_us': round(dt * 1e6, 1),
                 'us_per_cg_iteration': round(ms * 1e3 / max(its, 1), 2),
-                'share_of_step_gpu_time': None, 'traffic': None})
+                'share_of_step_gpu_time': None,
+                'traffic': TRAFFIC_40[name[:5]] if size == 40 else None})
   out.sort(key=lambda r: -r['launch_us'] * r['launches'])
   total = sum(r['launch_us'] * r['launches'] for r in out)
   for r in out:
@@ -303,6 +311,9 @@ def roofline_from_steps(st, nt, nv, degree, hbm_peak, peak_kind):
     del r['share_of_step_gpu_time']
   roof = dict(out[0])
   roof['cg_path'] = path
+  if roof['traffic'] is not None:
+    roof['traffic_source'] = ('ncu dram__bytes_read.sum + dram__bytes_write.sum of one '
+                              'launch of bench.py --profile-solve --size 40 (same workload)')
   roof['working_set_note'] = ('operator data staged in shared memory / resident in L2 across '
                               'each solve: the rate is on-chip, not HBM')
   if len(out) > 1:
@@ -511,7 +522,8 @@ def run_ours(args):
   e2e = {'value': round(ws * args.steps / t_e2e, 3), 'unit': UNIT,
          'h2d_bytes_per_step': 2 * x.numel() * 4, 'd2h_bytes_per_step': 2 * x.numel() * 4}
 
-  roof = roofline_from_steps(st, s.n_tets, s.n_verts, FAST_KW['cheb_degree'], hbm, kind)
+  roof = roofline_from_steps(st, s.n_tets, s.n_verts, FAST_KW['cheb_degree'], hbm, kind,
+                             args.size)
   roof['matrix_free_apply'] = roofline_matrix_free(torch, s, hbm, kind)
   st0 = st[-1]
   n_verts, n_tets = s.n_verts, s.n_tets

@@ -16,9 +16,10 @@ from .learned import CoarseGraph, CoarseNet  # noqa: F401
 from .graph_coloring import ColoringResult, color_edges, color_elements, color_vertices  # noqa: F401
 from .mgpbd_gpu import MGPBDSolverGPU  # noqa: F401
 from .solver_benchmark import SolverBenchmark  # noqa: F401
+from .tet_data import TetData, load_tets  # noqa: F401
 from .vbd import VBDSolver  # noqa: F401
 
 __all__ = ['MGPBDSolverGPU', 'SolverBenchmark', 'MGPBDConstraint', 'PbdFramework', 'Body',
            'BodyBatch', 'AdaptiveZone', 'MGPBDAdaptiveSolver', 'Deform3D', 'VBDSolver',
            'ColoringResult', 'color_edges', 'color_elements', 'color_vertices', 'CoarseNet',
-           'CoarseGraph']
+           'CoarseGraph', 'TetData', 'load_tets']

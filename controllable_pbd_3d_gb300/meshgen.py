@@ -154,8 +154,9 @@ def cube_body(n: int, jitter: float = 0.01, seed: int = 0, pin_top: bool = True,
   return x, t_i, invm
 
 
-def parse_medit_mesh(path: str):
-  """Minimal MEDIT `.mesh` reader: returns `(verts, tets, tris)`, 0-based.
+def parse_medit_mesh(path: str, dtype=np.float32):
+  """Minimal MEDIT `.mesh` reader: returns `(verts, tets, tris)`, 0-based,
+  vertices in `dtype` (meshio, which the reference uses, gives float64).
 
   Replaces meshio for the reference's `load_tet` (`utils/io.py:11-19`).
   """
@@ -174,7 +175,7 @@ def parse_medit_mesh(path: str):
       i += 2 + n * width
     else:
       i += 1
-  verts = out['Vertices'][:, :3].astype(np.float32)
+  verts = out['Vertices'][:, :3].astype(dtype)
   tets = (out['Tetrahedra'][:, :4].astype(np.int64) - 1).reshape(-1).astype(np.int32)
   tris = (out.get('Triangles', np.zeros((0, 4)))[:, :3].astype(np.int64) - 1)
   return verts, tets, tris.reshape(-1).astype(np.int32)

@@ -46,3 +46,10 @@ def cuda():
   from controllable_pbd_3d_gb300 import _native
   _native.lib()
   return torch
+
+
+@pytest.fixture(scope='session')
+def cuda_or_cpu():
+  """'cuda' where a GPU is visible, else 'cpu' (host-only code paths)."""
+  torch = pytest.importorskip('torch')
+  return 'cuda' if torch.cuda.is_available() else 'cpu'
