@@ -33,6 +33,9 @@ MGPBD_SMOOTH_JACOBI_SAFE = 1
 MGPBD_PRECOND_VCYCLE = 0
 MGPBD_PRECOND_CHEB = 1
 MGPBD_PRECOND_LEARNED = 2
+MGPBD_CONS_ARAP = 0
+MGPBD_CONS_LENGTH = 1
+MGPBD_CONS_VOLUME = 2
 MGPBD_NET_PARAMS = 16769
 MGPBD_NET_LOSS_WEIGHTS = 0
 MGPBD_NET_LOSS_FIELD = 1
@@ -161,6 +164,7 @@ _SIGS = {
     'mgpbd_net_adam': (C.c_int, [vp, f32, f32, f32, f32, vp]),
     'mgpbd_net_train': (C.c_int, [vp, i32, i64, vp, vp, vp, vp, vp, i32, i32, i32, f32, vp, vp]),
     'mgpbd_set_coarse_net': (C.c_int, [vp, vp]),
+    'mgpbd_set_constraint_types': (C.c_int, [vp, vp]),
     'mgpbd_row_shapes': (C.c_int, [vp, P_i32]),
     'mgpbd_autotune_rows': (C.c_int, [vp, i32, vp, vp]),
     'mgpbd_level_row_shape': (C.c_int, [vp, i32, P_i32]),

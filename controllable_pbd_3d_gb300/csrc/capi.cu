@@ -402,6 +402,11 @@ int mgpbd_row_shapes(int32_t* codes, int32_t* count) {
   });
 }
 
+int mgpbd_set_constraint_types(mgpbd_handle h, const int32_t* types) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.set_constraint_types(types); });
+}
+
 int mgpbd_set_coarse_net(mgpbd_handle h, mgpbd_net_handle net) {
   if (!h) return MGPBD_EINVAL;
   h->impl.set_coarse_net(net ? &net->impl : nullptr);

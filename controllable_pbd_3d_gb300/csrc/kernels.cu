@@ -65,12 +65,24 @@ __device__ __forceinline__ void st3(float* p, int64_t i, float3 v) {
 // ---------------------------------------------------------------------------
 // _precompute_rest_shape (cons/mgpbd_gpu.py:136-151)
 __global__ void k_rest_shape(const float* __restrict__ x_ref, const int4* __restrict__ t_i,
-                             int32_t nt, float mu, float dt, float* __restrict__ dm_inv,
-                             float* __restrict__ rest_vol, float* __restrict__ alpha) {
+                             const int32_t* __restrict__ ctype, int32_t nt, float mu, float dt,
+                             float* __restrict__ dm_inv, float* __restrict__ rest_vol,
+                             float* __restrict__ alpha) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt;
        t += (int64_t)gridDim.x * blockDim.x) {
     int4 q = t_i[t];
-    float3 r0 = ld3(x_ref, q.x), r1 = ld3(x_ref, q.y), r2 = ld3(x_ref, q.z), r3 = ld3(x_ref, q.w);
+    float3 r0 = ld3(x_ref, q.x), r1 = ld3(x_ref, q.y);
+    if (ctype && ctype[t] == MGPBD_CONS_LENGTH) {
+      // rest length of the edge (slots 0, 1); no Dm^-1
+      const float dx = r0.x - r1.x, dy = r0.y - r1.y, dz = r0.z - r1.z;
+      const float len = sqrtf(dx * dx + dy * dy + dz * dz);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) dm_inv[9 * t + k] = 0.0f;
+      rest_vol[t] = len;
+      alpha[t] = mu < 0.0f ? (-mu) / (dt * dt) : 1.0f / (mu * dt * dt * len);
+      continue;
+    }
+    float3 r2 = ld3(x_ref, q.z), r3 = ld3(x_ref, q.w);
     float D[3][3] = {{r1.x - r0.x, r2.x - r0.x, r3.x - r0.x},
                      {r1.y - r0.y, r2.y - r0.y, r3.y - r0.y},
                      {r1.z - r0.z, r2.z - r0.z, r3.z - r0.z}};
@@ -158,22 +170,88 @@ __device__ __forceinline__ float arap_c(const float (&s)[3]) {
 
 // _compute_C_and_gradC (cons/mgpbd_gpu.py:225-247) with _arap_gradient
 // (cons/mgpbd.py:35-68): G = U diag((S-1)/C) V^T Dm^-T, g0 = -(g1+g2+g3)
+// Edge length constraint (cons/length.py:65-90): C = |x_a - x_b| - L0 on
+// slots 0 and 1 at positions x (+ omega * dpos); gradients +-n on the two
+// slots, 0 on slots 2 and 3 (which repeat the edge's vertices).
+__device__ __forceinline__ float length_c(const float* __restrict__ x, const float* dpos,
+                                          float omega, int4 q, float rest, float3* n) {
+  float3 a = ld3(x, q.x), b = ld3(x, q.y);
+  if (dpos) {
+    float3 da = ld3(dpos, q.x), db = ld3(dpos, q.y);
+    a = make_float3(a.x + omega * da.x, a.y + omega * da.y, a.z + omega * da.z);
+    b = make_float3(b.x + omega * db.x, b.y + omega * db.y, b.z + omega * db.z);
+  }
+  const float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+  const float len = sqrtf(dx * dx + dy * dy + dz * dz);
+  if (n) *n = len > 1e-12f ? make_float3(dx / len, dy / len, dz / len) : make_float3(0.f, 0.f, 0.f);
+  return len - rest;
+}
+
+// Volume constraint (the hydrostatic constraint of cons/deform3d.py:81-83):
+// C = det F - 1; P = d(det F)/dF = [f2 x f3, f3 x f1, f1 x f2] (columns).
+__device__ __forceinline__ float volume_c(const float (&F)[3][3], float (&P)[3][3]) {
+  const float f1[3] = {F[0][0], F[1][0], F[2][0]};
+  const float f2[3] = {F[0][1], F[1][1], F[2][1]};
+  const float f3[3] = {F[0][2], F[1][2], F[2][2]};
+  const float c23[3] = {f2[1] * f3[2] - f2[2] * f3[1], f2[2] * f3[0] - f2[0] * f3[2],
+                        f2[0] * f3[1] - f2[1] * f3[0]};
+  const float c31[3] = {f3[1] * f1[2] - f3[2] * f1[1], f3[2] * f1[0] - f3[0] * f1[2],
+                        f3[0] * f1[1] - f3[1] * f1[0]};
+  const float c12[3] = {f1[1] * f2[2] - f1[2] * f2[1], f1[2] * f2[0] - f1[0] * f2[2],
+                        f1[0] * f2[1] - f1[1] * f2[0]};
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    P[r][0] = c23[r];
+    P[r][1] = c31[r];
+    P[r][2] = c12[r];
+  }
+  return f1[0] * c23[0] + f1[1] * c23[1] + f1[2] * c23[2] - 1.0f;
+}
+
 __global__ void k_constraints(const float* __restrict__ x, const int4* __restrict__ t_i,
-                              const float* __restrict__ dm_inv, int32_t nt, float* __restrict__ C,
+                              const int32_t* __restrict__ ctype, const float* __restrict__ dm_inv,
+                              const float* __restrict__ rest, int32_t nt, float* __restrict__ C,
                               float4* __restrict__ gradC) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt;
        t += (int64_t)gridDim.x * blockDim.x) {
     int4 q = t_i[t];
+    const int ty = ctype ? ctype[t] : MGPBD_CONS_ARAP;
+    float g[4][3];
+    if (ty == MGPBD_CONS_LENGTH) {
+      float3 n;
+      C[t] = length_c(x, nullptr, 0.0f, q, rest[t], &n);
+      float4* o = gradC + 3 * t;
+      o[0] = make_float4(n.x, n.y, n.z, -n.x);
+      o[1] = make_float4(-n.y, -n.z, 0.0f, 0.0f);
+      o[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      continue;
+    }
     float B[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) B[k] = dm_inv[9 * t + k];
     float F[3][3];
     deformation(x, nullptr, 0.0f, q, B, F);
+    if (ty == MGPBD_CONS_VOLUME) {
+      float P[3][3];
+      C[t] = volume_c(F, P);
+#pragma unroll
+      for (int k = 1; k < 4; ++k)
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+          g[k][r] = B[(k - 1) * 3 + 0] * P[r][0] + B[(k - 1) * 3 + 1] * P[r][1] +
+                    B[(k - 1) * 3 + 2] * P[r][2];
+#pragma unroll
+      for (int r = 0; r < 3; ++r) g[0][r] = -g[1][r] - g[2][r] - g[3][r];
+      float4* o = gradC + 3 * t;
+      o[0] = make_float4(g[0][0], g[0][1], g[0][2], g[1][0]);
+      o[1] = make_float4(g[1][1], g[1][2], g[2][0], g[2][1]);
+      o[2] = make_float4(g[2][2], g[3][0], g[3][1], g[3][2]);
+      continue;
+    }
     float U[3][3], s[3], V[3][3];
     svd3_rv(F, U, s, V);
     float c = arap_c(s);
     C[t] = c;
-    float g[4][3];
     if (c > 1e-6f) {
       float d[3] = {(s[0] - 1.0f) / c, (s[1] - 1.0f) / c, (s[2] - 1.0f) / c};
       float P[3][3];
@@ -220,7 +298,8 @@ __global__ void k_rhs(const float* __restrict__ C, const float* __restrict__ alp
 // several omega_k in one pass
 __global__ void k_dual_trial(const float* __restrict__ x, const float* __restrict__ dpos,
                              const double* __restrict__ omegas, int n_omega,
-                             const int4* __restrict__ t_i, const float* __restrict__ dm_inv,
+                             const int4* __restrict__ t_i, const int32_t* __restrict__ ctype,
+                             const float* __restrict__ dm_inv, const float* __restrict__ rest,
                              const float* __restrict__ alpha, const float* __restrict__ lambda,
                              int32_t nt, double* __restrict__ partials) {
   constexpr int kMaxOmega = 16;
@@ -230,17 +309,34 @@ __global__ void k_dual_trial(const float* __restrict__ x, const float* __restric
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt;
        t += (int64_t)gridDim.x * blockDim.x) {
     int4 q = t_i[t];
+    const int ty = ctype ? ctype[t] : MGPBD_CONS_ARAP;
+    float al = alpha[t] * lambda[t];
+    if (ty == MGPBD_CONS_LENGTH) {
+      const float L0 = rest[t];
+#pragma unroll 1
+      for (int k = 0; k < n_omega; ++k) {
+        float r = -(length_c(x, dpos, (float)omegas[k], q, L0, nullptr) + al);
+        acc[k] += (double)r * (double)r;
+      }
+      continue;
+    }
     float B[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) B[k] = dm_inv[9 * t + k];
-    float al = alpha[t] * lambda[t];
 #pragma unroll 1
     for (int k = 0; k < n_omega; ++k) {
       float F[3][3];
       deformation(x, dpos, (float)omegas[k], q, B, F);
-      float U[3][3], s[3], V[3][3];
-      svd3_rv(F, U, s, V);
-      float r = -(arap_c(s) + al);
+      float c;
+      if (ty == MGPBD_CONS_VOLUME) {
+        float P[3][3];
+        c = volume_c(F, P);
+      } else {
+        float U[3][3], s[3], V[3][3];
+        svd3_rv(F, U, s, V);
+        c = arap_c(s);
+      }
+      float r = -(c + al);
       acc[k] += (double)r * (double)r;
     }
   }
@@ -812,14 +908,23 @@ __global__ void k_chol_solve(const CgState* __restrict__ st, const double* __res
 // ===========================================================================
 int reduce_blocks(int64_t n) { return grid_for(n, kThreads * 4); }
 
-void launch_rest_shape(const float* x_ref, const int32_t* t_i, int32_t nt, float mu, float dt,
-                       float* dm_inv, float* rest_vol, float* alpha, cudaStream_t s) {
+void launch_rest_shape(const float* x_ref, const int32_t* t_i, const int32_t* ctype, int32_t nt,
+                       float mu, float dt, float* dm_inv, float* rest_vol, float* alpha,
+                       cudaStream_t s) {
   if (nt <= 0) return;
-  k_rest_shape<<<grid_for(nt, kThreads), kThreads, 0, s>>>(x_ref, reinterpret_cast<const int4*>(t_i),
-                                                          nt, mu, dt, dm_inv, rest_vol, alpha);
+  k_rest_shape<<<grid_for(nt, kThreads), kThreads, 0, s>>>(
+      x_ref, reinterpret_cast<const int4*>(t_i), ctype, nt, mu, dt, dm_inv, rest_vol, alpha);
   MGPBD_CHECK_LAUNCH();
 }
-
+void launch_constraints(const float* x, const int32_t* t_i, const int32_t* ctype,
+                        const float* dm_inv, const float* rest, int32_t nt, float* C,
+                        float* gradC, cudaStream_t s) {
+  if (nt <= 0) return;
+  k_constraints<<<ceil_div(nt, 128), 128, 0, s>>>(x, reinterpret_cast<const int4*>(t_i), ctype,
+                                                  dm_inv, rest, nt, C,
+                                                  reinterpret_cast<float4*>(gradC));
+  MGPBD_CHECK_LAUNCH();
+}
 void launch_predict(float* x, float* v, float* x_old, float* x_pred, const float* invm, int32_t nv,
                     float dt, const float* g, float damp, int kinematic, cudaStream_t s) {
   if (nv <= 0) return;
@@ -832,14 +937,6 @@ void launch_update_vel(const float* x, const float* x_old, float* v, int32_t nv,
                        cudaStream_t s) {
   if (nv <= 0) return;
   k_update_vel<<<grid_for(nv, kThreads), kThreads, 0, s>>>(x, x_old, v, nv, dt, damp);
-  MGPBD_CHECK_LAUNCH();
-}
-
-void launch_constraints(const float* x, const int32_t* t_i, const float* dm_inv, int32_t nt, float* C,
-                        float* gradC, cudaStream_t s) {
-  if (nt <= 0) return;
-  k_constraints<<<ceil_div(nt, 128), 128, 0, s>>>(x, reinterpret_cast<const int4*>(t_i), dm_inv, nt, C,
-                                                  reinterpret_cast<float4*>(gradC));
   MGPBD_CHECK_LAUNCH();
 }
 
@@ -856,12 +953,13 @@ void launch_dual_sq(const float* C, const float* alpha, const float* lambda, int
 }
 
 void launch_dual_trial(const float* x, const float* dpos, const double* omegas, int n_omega,
-                       const int32_t* t_i, const float* dm_inv, const float* alpha,
-                       const float* lambda, int32_t nt, double* partials, cudaStream_t s) {
+                       const int32_t* t_i, const int32_t* ctype, const float* dm_inv,
+                       const float* rest, const float* alpha, const float* lambda, int32_t nt,
+                       double* partials, cudaStream_t s) {
   require(n_omega >= 1 && n_omega <= 16, MGPBD_EINVAL, "n_omega out of range");
   k_dual_trial<<<reduce_blocks(nt), kThreads, 0, s>>>(x, dpos, omegas, n_omega,
-                                                      reinterpret_cast<const int4*>(t_i), dm_inv,
-                                                      alpha, lambda, nt, partials);
+                                                      reinterpret_cast<const int4*>(t_i), ctype,
+                                                      dm_inv, rest, alpha, lambda, nt, partials);
   MGPBD_CHECK_LAUNCH();
 }
 

@@ -14,15 +14,19 @@ constexpr int kReduceThreads = 256;
 constexpr int kMaxReduceBlocks = 1216;  // 8 x 152 SMs
 
 // ---- per-vertex / per-tet stages (cons/mgpbd_gpu.py) ---------------------
-void launch_rest_shape(const float* x_ref, const int32_t* t_i, int32_t nt, float mu, float dt,
-                       float* dm_inv, float* rest_vol, float* alpha, cudaStream_t s);
+// ctype (nullable: all MGPBD_CONS_ARAP) selects each constraint's type; a
+// length constraint's rest length goes to rest_vol
+void launch_rest_shape(const float* x_ref, const int32_t* t_i, const int32_t* ctype, int32_t nt,
+                       float mu, float dt, float* dm_inv, float* rest_vol, float* alpha,
+                       cudaStream_t s);
 void launch_predict(float* x, float* v, float* x_old, float* x_pred, const float* invm,
                     int32_t nv, float dt, const float* g, float damp, int kinematic,
                     cudaStream_t s);
 void launch_update_vel(const float* x, const float* x_old, float* v, int32_t nv, float dt,
                        float damp, cudaStream_t s);
-void launch_constraints(const float* x, const int32_t* t_i, const float* dm_inv, int32_t nt,
-                        float* C, float* gradC, cudaStream_t s);
+void launch_constraints(const float* x, const int32_t* t_i, const int32_t* ctype,
+                        const float* dm_inv, const float* rest, int32_t nt, float* C,
+                        float* gradC, cudaStream_t s);
 // b = -(C + alpha*lambda); partials of |b|^2 (float64)
 void launch_rhs(const float* C, const float* alpha, const float* lambda, int32_t nt, float* b,
                 double* partials, cudaStream_t s);
@@ -32,8 +36,9 @@ void launch_dual_sq(const float* C, const float* alpha, const float* lambda, int
 // dual residual at x + omega_k * dpos for n_omega step sizes; partials laid
 // out [k * blocks + block]
 void launch_dual_trial(const float* x, const float* dpos, const double* omegas, int n_omega,
-                       const int32_t* t_i, const float* dm_inv, const float* alpha,
-                       const float* lambda, int32_t nt, double* partials, cudaStream_t s);
+                       const int32_t* t_i, const int32_t* ctype, const float* dm_inv,
+                       const float* rest, const float* alpha, const float* lambda, int32_t nt,
+                       double* partials, cudaStream_t s);
 // lambda += dlam; dpos[v] = sum over incident (t,l) ascending of
 // w_v * dlam_t * gradC[t,l]
 void launch_lambda_update(float* lambda, const float* dlam, int32_t nt, cudaStream_t s);

@@ -152,6 +152,16 @@ void Solver::require_init() const {
 // the built-in tet aggregation): level_sizes[0] = nt, and for each level l
 // the level_sizes[l] entries of agg_ids from offset sum(level_sizes[0..l))
 // map level-l rows onto [0, level_sizes[l+1]), every coarse row used.
+void Solver::set_constraint_types(const int32_t* types) {
+  require(t_i_ != nullptr, MGPBD_ESTATE, "mgpbd_set_mesh has not been called");
+  if (!types) {
+    ctype_host_.clear();
+  } else {
+    ctype_host_.assign(types, types + nt_);
+  }
+  inited_ = false;
+}
+
 void Solver::set_hierarchy(const int32_t* agg_ids, int32_t n_levels, const int32_t* level_sizes) {
   require(x_ && t_i_, MGPBD_ESTATE, "mgpbd_set_mesh must come before mgpbd_set_hierarchy");
   require(n_levels >= 2 && n_levels <= 8, MGPBD_EINVAL, "n_levels must be in [2, 8]");
@@ -193,6 +203,7 @@ void Solver::set_mesh(const float* x_ref, const float* invm, const int32_t* t_i,
   inited_ = false;
   user_sizes_.clear();
   user_aggs_.clear();
+  ctype_host_.clear();
   if (cg_exec_) {
     cudaGraphExecDestroy(cg_exec_);
     cg_exec_ = nullptr;
@@ -254,8 +265,33 @@ void Solver::init() {
   require((reinterpret_cast<uintptr_t>(t_i_) & 15) == 0 && (reinterpret_cast<uintptr_t>(x_) & 3) == 0,
           MGPBD_EINVAL, "t_i must be 16-byte aligned (read as int4)");
 
-  launch_rest_shape(x_ref_, t_i_, nt_, p_.compliance > 0.0f ? -p_.compliance : p_.mu, p_.dt,
-                    dm_inv_.p, rest_vol_.p, alpha_.p, s);
+  // constraint types (mgpbd_set_constraint_types): a length constraint lists
+  // its edge twice (a, b, a, b) and needs compliance-based alpha~
+  ctype_.release();
+  if (!ctype_host_.empty()) {
+    require(static_cast<int64_t>(ctype_host_.size()) == nt_, MGPBD_EINVAL,
+            "constraint types: one per constraint (nt)");
+    bool generic = false;
+    for (int32_t c = 0; c < nt_; ++c) {
+      const int32_t ty = ctype_host_[c];
+      require(ty == MGPBD_CONS_ARAP || ty == MGPBD_CONS_LENGTH || ty == MGPBD_CONS_VOLUME,
+              MGPBD_EINVAL, "unknown constraint type");
+      generic |= ty != MGPBD_CONS_ARAP;
+      if (ty == MGPBD_CONS_LENGTH) {
+        const int32_t* q = t_host.data() + 4LL * c;
+        require(q[2] == q[0] && q[3] == q[1] && q[0] != q[1], MGPBD_EINVAL,
+                "a length constraint must list its two vertices twice: (a, b, a, b)");
+      }
+    }
+    require(!generic || p_.compliance > 0.0f, MGPBD_EINVAL,
+            "length and volume constraints take alpha~ = compliance / dt^2: set compliance > 0");
+    ctype_.alloc(nt_);
+    MGPBD_CUDA(cudaMemcpyAsync(ctype_.p, ctype_host_.data(), sizeof(int32_t) * nt_,
+                               cudaMemcpyHostToDevice, s));
+  }
+  launch_rest_shape(x_ref_, t_i_, ctype_.p, nt_,
+                    p_.compliance > 0.0f ? -p_.compliance : p_.mu, p_.dt, dm_inv_.p, rest_vol_.p,
+                    alpha_.p, s);
 
   // level-0 pattern (cons/mgpbd_gpu.py:153-194)
   levels_.clear();
@@ -290,7 +326,7 @@ void Solver::init() {
   }
 
   // first A at the current positions (cons/mgpbd_gpu.py:98-100)
-  launch_constraints(x_, t_i_, dm_inv_.p, nt_, C_.p, gradC_.p, s);
+  launch_constraints(x_, t_i_, ctype_.p, dm_inv_.p, rest_vol_.p, nt_, C_.p, gradC_.p, s);
   launch_fill_A(L0.indptr.p, L0.indices.p, t_i_, invm_, gradC_.p, alpha_.p, nt_, L0.data.p,
                 L0.diag_inv.p, s);
   std::vector<float> a0(L0.nnz);
@@ -781,7 +817,7 @@ void Solver::step(int32_t frame) {
 
 void Solver::compute_constraints() {
   require_init();
-  launch_constraints(x_, t_i_, dm_inv_.p, nt_, C_.p, gradC_.p, stream_);
+  launch_constraints(x_, t_i_, ctype_.p, dm_inv_.p, rest_vol_.p, nt_, C_.p, gradC_.p, stream_);
 }
 
 // _fill_A_and_update_gpu (cons/mgpbd_gpu.py:320-324)
@@ -1250,7 +1286,7 @@ double Solver::line_search() {
   h_buf_[0] = 1.0;
   MGPBD_CUDA(cudaMemcpyAsync(omegas_.p, h_buf_, sizeof(double), cudaMemcpyHostToDevice, s));
   launch_dual_sq(C_.p, alpha_.p, lambda_.p, nt_, partials_.p, s);
-  launch_dual_trial(x_, dpos_.p, omegas_.p, 1, t_i_, dm_inv_.p, alpha_.p, lambda_.p, nt_,
+  launch_dual_trial(x_, dpos_.p, omegas_.p, 1, t_i_, ctype_.p, dm_inv_.p, rest_vol_.p, alpha_.p, lambda_.p, nt_,
                     partials_.p + blocks, s);
   launch_finalize(partials_.p, blocks, 2, scalars_.p, s);
   sync_read(h_buf_, scalars_.p, 2 * sizeof(double));
@@ -1261,7 +1297,7 @@ double Solver::line_search() {
   for (int k = 0; k < 9; ++k) om[k] = std::ldexp(1.0, -(k + 1));
   std::memcpy(h_buf_, om, sizeof(om));
   MGPBD_CUDA(cudaMemcpyAsync(omegas_.p, h_buf_, sizeof(om), cudaMemcpyHostToDevice, s));
-  launch_dual_trial(x_, dpos_.p, omegas_.p, 9, t_i_, dm_inv_.p, alpha_.p, lambda_.p, nt_,
+  launch_dual_trial(x_, dpos_.p, omegas_.p, 9, t_i_, ctype_.p, dm_inv_.p, rest_vol_.p, alpha_.p, lambda_.p, nt_,
                     partials_.p, s);
   launch_finalize(partials_.p, blocks, 9, scalars_.p, s);
   sync_read(h_buf_, scalars_.p, 9 * sizeof(double));

@@ -57,6 +57,8 @@ class Solver {
   void set_mesh(const float* x_ref, const float* invm, const int32_t* t_i, int32_t nv, int32_t nt,
                 float* x, float* v);
   void set_hierarchy(const int32_t* agg_ids, int32_t n_levels, const int32_t* level_sizes);
+  // per-constraint MGPBD_CONS_* types (host array of nt; nullptr: all ARAP)
+  void set_constraint_types(const int32_t* types);
   void init();
   void step(int32_t frame);
   void make_prediction();
@@ -152,6 +154,8 @@ class Solver {
   DevBuf<float> x_old_, x_pred_, dpos_;
   DevBuf<float> dm_inv_, rest_vol_, alpha_, lambda_, C_, gradC_, rhs_, dlam_;
   DevBuf<int32_t> inc_ptr_, inc_ent_;
+  DevBuf<int32_t> ctype_;              // constraint types (absent: all ARAP)
+  std::vector<int32_t> ctype_host_;
   std::vector<Level> levels_;
 
   DevBuf<float> cg_r_, cg_z_, cg_p_, cg_ap_;

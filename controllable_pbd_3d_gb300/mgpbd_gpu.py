@@ -94,6 +94,11 @@ class MGPBDSolverGPU:
                    see include/mgpbd.h -- and takes over on stalls);
     use_graph      FAST: one CUDA graph with a device-side loop per CG solve
                    (False: the same kernels from a host loop);
+    constraints    'arap' (the reference: one ARAP constraint per tet) or
+                   'edge_volume' (one length constraint per unique tet edge
+                   and one volume constraint det F - 1 per tet, alpha~ =
+                   compliance / dt^2; n_tets then counts constraints, the
+                   mesh's tets are in mesh_t_i / n_mesh_tets);
     persistent     FAST + 'cheb': each CG solve is one cooperative persistent
                    kernel (False: one kernel per phase, per use_graph);
     primal         FAST + 'cheb' + persistent: warm-start each solve through
@@ -109,7 +114,7 @@ class MGPBDSolverGPU:
                kinematic_pins=False, coarse_sweeps=0, cg_alias=False, compliance=0.0,
                precond='vcycle', cheb_degree=8, cheb_lo=0.01, use_graph=True,
                persistent=True, primal=False, primal_tol=1e-2, learned_accept=0.1, learned_stall=1000,
-               check_finite=True):
+               constraints='arap', check_finite=True):
     if aggregation != 'tet':
       raise NotImplementedError(
           "aggregation='pyamg' needs PyAMG's smoothed-aggregation setup, which this "
@@ -128,6 +133,26 @@ class MGPBDSolverGPU:
       raise ValueError('v_p, v_p_ref and v_invm must have the same number of vertices')
     if self.t_i.shape[0] != 4 * self.n_tets:
       raise ValueError('t_i must hold 4 indices per tet')
+    # the constraint set: one ARAP constraint per tet (the reference's), or
+    # one volume constraint per tet plus one length constraint per edge
+    if constraints not in ('arap', 'edge_volume'):
+      raise ValueError("constraints must be 'arap' or 'edge_volume'")
+    self.constraint_kind = constraints
+    self.mesh_t_i = self.t_i
+    self.n_mesh_tets = self.n_tets
+    self.constraint_types = None
+    agg0 = None
+    if constraints == 'edge_volume':
+      if not compliance > 0:
+        raise ValueError("constraints='edge_volume' takes alpha~ = compliance / dt^2: "
+                         'pass compliance > 0')
+      from .edge_volume import edge_volume_hierarchy, edge_volume_system
+      t_host = self.t_i.cpu().numpy()
+      c_i, types, self.edges, _ = edge_volume_system(t_host)
+      self.constraint_types = types
+      self.t_i = torch.tensor(c_i, device=self.v_p.device)
+      self.n_tets = len(types)  # constraints (the fields below have this length)
+      agg0 = edge_volume_hierarchy(t_host, max_coarse=int(max_coarse))
     self.gravity = [float(g) for g in (gravity.to_numpy() if hasattr(gravity, 'to_numpy') else gravity)]
     self.dt = float(dt)
     self.mu = float(mu)
@@ -187,6 +212,11 @@ class MGPBDSolverGPU:
     N.check(self._lib.mgpbd_set_mesh(h, self.v_p_ref.data_ptr(), self.v_invm.data_ptr(),
                                      self.t_i.data_ptr(), self.n_verts, self.n_tets,
                                      self.v_p.data_ptr(), self.v_v.data_ptr()), 'mgpbd_set_mesh')
+    if self.constraint_types is not None:
+      N.check(self._lib.mgpbd_set_constraint_types(h, self.constraint_types.ctypes.data),
+              'mgpbd_set_constraint_types')
+      if agg0 is not None:
+        self.set_hierarchy([agg0])
     self._inited = False
     self._gpu_solver = None
 

@@ -244,6 +244,26 @@ int mgpbd_set_mesh(mgpbd_handle h, const float* x_ref, const float* invm,
 int mgpbd_set_hierarchy(mgpbd_handle h, const int32_t* agg_ids, int32_t n_levels,
                         const int32_t* level_sizes);
 
+/* Constraint types.  The reference's step has one ARAP constraint per tet
+ * (C = |S - I|_F, cons/mgpbd_gpu.py:226-247).  The library also takes, per
+ * constraint, the two blocks of a length + volume discretisation:
+ *   MGPBD_CONS_LENGTH: C = |x_a - x_b| - L0 (cons/length.py:65-90); the
+ *     constraint lists its edge twice in t_i, (a, b, a, b);
+ *   MGPBD_CONS_VOLUME: C = det F - 1, F = D_s Dm^-1 (the hydrostatic
+ *     constraint of cons/deform3d.py:81-83) on a tet's four vertices.
+ * Every constraint keeps 4 slots in t_i, so the assembly, the multigrid
+ * hierarchy, the CG kernels and the scatter are shared (a repeated vertex
+ * carries a zero gradient).  Length and volume constraints take
+ * alpha~ = compliance / dt^2 (compliance > 0 required); a length
+ * constraint's rest length is reported in MGPBD_FIELD_REST_VOL. */
+#define MGPBD_CONS_ARAP 0
+#define MGPBD_CONS_LENGTH 1
+#define MGPBD_CONS_VOLUME 2
+/* Between mgpbd_set_mesh and mgpbd_init: types (host array of nt
+ * MGPBD_CONS_* values), or NULL for all ARAP.  mgpbd_set_mesh clears it;
+ * mgpbd_init validates it.  No counterpart in the reference. */
+int mgpbd_set_constraint_types(mgpbd_handle h, const int32_t* types);
+
 /* Replaces MGPBDSolverGPU.init (cons/mgpbd_gpu.py:92-114): rest shape,
  * sparsity pattern, first A, tet hierarchy, multigrid setup. */
 int mgpbd_init(mgpbd_handle h);

@@ -46,7 +46,7 @@ def lib():
     vp, i32, f32, f64 = C.c_void_p, C.c_int32, C.c_float, C.c_double
     L.cpu_create.restype = vp
     L.cpu_create.argtypes = [i32, i32, vp, vp, vp, vp, f32, f32, f32, f32, vp, i32, f64, f64, i32,
-                             f64, f64, i32, f64, i32]
+                             f64, f64, i32, f64, i32, vp]
     L.cpu_destroy.argtypes = [vp]
     L.cpu_add_level.argtypes = [vp, i32, vp, vp, C.c_int64, vp, vp, vp]
     L.cpu_predict.argtypes = [vp]
@@ -68,7 +68,11 @@ class CpuPort:
 
   def __init__(self, x0, x_ref, invm, t_i, gravity, dt, mu=1e6, compliance=0.0, damp=1.0,
                maxiter=20, atol=1e-4, rtol=1e-2, maxiter_cg=100, tol_cg=1e-5, rel_tol_cg=0.0,
-               n_smooth=2, omega_jacobi=2.0 / 3.0, kinematic_pins=False):
+               n_smooth=2, omega_jacobi=2.0 / 3.0, kinematic_pins=False, ctype=None,
+               hierarchy=None):
+    """ctype: per-constraint types (0 ARAP, 1 length (a, b, a, b), 2
+    volume), None for all ARAP; hierarchy: level-0 aggregate ids to use
+    instead of the tet aggregation."""
     L = lib()
     self.maxiter = maxiter
     self.maxiter_cg = maxiter_cg
@@ -77,17 +81,22 @@ class CpuPort:
     xr, x, w, t, g = self._keep
     self.nv = len(xr)
     self.nt = len(t) // 4
+    ct = None if ctype is None else _c(ctype, np.int32)
+    self._keep.append(ct)
     self.h = L.cpu_create(self.nv, self.nt, xr.ctypes.data, x.ctypes.data, w.ctypes.data,
                           t.ctypes.data, dt, mu, compliance, damp, g.ctypes.data, maxiter, atol,
                           rtol, maxiter_cg, tol_cg, rel_tol_cg, n_smooth, omega_jacobi,
-                          int(bool(kinematic_pins)))
+                          int(bool(kinematic_pins)), None if ct is None else ct.ctypes.data)
     # structure from the oracle restatement
     ip, ix = orc.sparsity_pattern(t, self.nt)
     L.cpu_add_level(self.h, self.nt, ip.ctypes.data, ix.ctypes.data, len(ix), None, None, None)
-    aggs, sizes = orc.tet_hierarchy(t, self.nt)
+    if hierarchy is not None:
+      aggs, sizes = [np.asarray(hierarchy)], [self.nt, int(np.max(hierarchy)) + 1]
+    else:
+      aggs, sizes = orc.tet_hierarchy(t, self.nt)
     if aggs:
-      dm, _, al = orc.rest_shape(xr, t, mu, dt, np.float32, compliance)
-      C0, g0 = orc.constraints(x, t, dm, np.float32)
+      dm, rest, al = orc.rest_shape(xr, t, mu, dt, np.float32, compliance, ct)
+      C0, g0 = orc.constraints(x, t, dm, np.float32, ct, rest)
       a0 = orc.fill_A(ip, ix, t, w, g0, al, np.float32)
       ci, cx, cidx, coff, _ = orc.galerkin(ip, ix, a0, aggs[0], sizes[1])
       agg = _c(aggs[0], np.int32)

@@ -42,6 +42,8 @@ struct Cpu {
   std::vector<float> xref, x, v, xold, invm, dpos;
   std::vector<int32_t> t;
   std::vector<float> dminv, alpha, C, g, lam, rhs, dlam;
+  std::vector<int32_t> ctype;  // 0 ARAP, 1 length, 2 volume (empty: all ARAP)
+  std::vector<float> rest;     // rest length of a length constraint
   std::vector<Lvl> L;
   float dt, mu, compliance, damp, gravity[3];
   int maxiter, maxiter_cg, n_smooth, kinematic;
@@ -156,9 +158,84 @@ float arap_c(const Cpu& c, int e, const float* x, const float* dp, float om, dou
   return cc;
 }
 
+int ctype_of(const Cpu& c, int e) { return c.ctype.empty() ? 0 : c.ctype[e]; }
+
+// length constraint |x_a - x_b| - L0 (slots 0, 1) and its unit vector a - b
+float length_c(const Cpu& c, int e, const float* x, const float* dp, float om, float n[3]) {
+  const int32_t* q = &c.t[4 * e];
+  float d[3];
+  for (int k = 0; k < 3; ++k)
+    d[k] = (x[3 * q[0] + k] + (dp ? om * dp[3 * q[0] + k] : 0.0f)) -
+           (x[3 * q[1] + k] + (dp ? om * dp[3 * q[1] + k] : 0.0f));
+  float len = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  if (n)
+    for (int k = 0; k < 3; ++k) n[k] = len > 1e-12f ? d[k] / len : 0.0f;
+  return len - c.rest[e];
+}
+
+// volume constraint det F - 1 and d(det F)/dF (columns f2 x f3, f3 x f1, f1 x f2)
+float volume_c(const Cpu& c, int e, const float* x, const float* dp, float om, float P[3][3]) {
+  const int32_t* q = &c.t[4 * e];
+  float p[4][3];
+  for (int l = 0; l < 4; ++l)
+    for (int k = 0; k < 3; ++k) p[l][k] = x[3 * q[l] + k] + (dp ? om * dp[3 * q[l] + k] : 0.0f);
+  float F[3][3];
+  const float* B = &c.dminv[9 * e];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      float f = 0;
+      for (int k = 0; k < 3; ++k) f += (p[k + 1][i] - p[0][i]) * B[3 * k + j];
+      F[i][j] = f;
+    }
+  const float* f1c[3] = {&F[0][0], &F[1][0], &F[2][0]};
+  float f1[3] = {F[0][0], F[1][0], F[2][0]}, f2[3] = {F[0][1], F[1][1], F[2][1]},
+        f3[3] = {F[0][2], F[1][2], F[2][2]};
+  (void)f1c;
+  float c23[3] = {f2[1] * f3[2] - f2[2] * f3[1], f2[2] * f3[0] - f2[0] * f3[2], f2[0] * f3[1] - f2[1] * f3[0]};
+  float c31[3] = {f3[1] * f1[2] - f3[2] * f1[1], f3[2] * f1[0] - f3[0] * f1[2], f3[0] * f1[1] - f3[1] * f1[0]};
+  float c12[3] = {f1[1] * f2[2] - f1[2] * f2[1], f1[2] * f2[0] - f1[0] * f2[2], f1[0] * f2[1] - f1[1] * f2[0]};
+  if (P)
+    for (int r = 0; r < 3; ++r) {
+      P[r][0] = c23[r];
+      P[r][1] = c31[r];
+      P[r][2] = c12[r];
+    }
+  return f1[0] * c23[0] + f1[1] * c23[1] + f1[2] * c23[2] - 1.0f;
+}
+
+float cons_c(const Cpu& c, int e, const float* x, const float* dp, float om) {
+  const int ty = ctype_of(c, e);
+  if (ty == 1) return length_c(c, e, x, dp, om, nullptr);
+  if (ty == 2) return volume_c(c, e, x, dp, om, nullptr);
+  return arap_c(c, e, x, dp, om);
+}
+
 void constraints(Cpu& c) {
 #pragma omp parallel for schedule(static)
   for (int e = 0; e < c.nt; ++e) {
+    const int ty = ctype_of(c, e);
+    if (ty == 1) {
+      float n[3];
+      c.C[e] = length_c(c, e, c.x.data(), nullptr, 0.0f, n);
+      float* g = &c.g[12 * e];
+      std::fill(g, g + 12, 0.0f);
+      for (int k = 0; k < 3; ++k) {
+        g[k] = n[k];
+        g[3 + k] = -n[k];
+      }
+      continue;
+    }
+    if (ty == 2) {
+      float P[3][3];
+      c.C[e] = volume_c(c, e, c.x.data(), nullptr, 0.0f, P);
+      float* g = &c.g[12 * e];
+      const float* B = &c.dminv[9 * e];
+      for (int l = 1; l < 4; ++l)
+        for (int r = 0; r < 3; ++r)
+          g[3 * l + r] = B[3 * (l - 1)] * P[r][0] + B[3 * (l - 1) + 1] * P[r][1] + B[3 * (l - 1) + 2] * P[r][2];
+      for (int r = 0; r < 3; ++r) g[r] = -(g[3 + r] + g[6 + r] + g[9 + r]);
+      continue;
+    }
     double U[3][3], s[3], V[3][3];
     float cc = arap_c(c, e, c.x.data(), nullptr, 0.0f, &U[0][0], s, &V[0][0]);
     c.C[e] = cc;
@@ -343,7 +420,7 @@ double dual_norm(Cpu& c, const float* dp, float om) {
   double s = 0;
 #pragma omp parallel for reduction(+ : s) schedule(static)
   for (int e = 0; e < c.nt; ++e) {
-    float cc = dp ? arap_c(c, e, c.x.data(), dp, om) : c.C[e];
+    float cc = dp ? cons_c(c, e, c.x.data(), dp, om) : c.C[e];
     double r = -(cc + c.alpha[e] * c.lam[e]);
     s += r * r;
   }
@@ -357,7 +434,8 @@ extern "C" {
 void* cpu_create(int nv, int nt, const float* xref, const float* x0, const float* invm,
                  const int32_t* t, float dt, float mu, float compliance, float damp,
                  const float* gravity, int maxiter, double atol, double rtol, int maxiter_cg,
-                 double tol_cg, double rel_tol_cg, int n_smooth, double omega, int kinematic) {
+                 double tol_cg, double rel_tol_cg, int n_smooth, double omega, int kinematic,
+                 const int32_t* ctype) {
   Cpu* c = new Cpu();
   c->nv = nv;
   c->nt = nt;
@@ -393,8 +471,18 @@ void* cpu_create(int nv, int nt, const float* xref, const float* x0, const float
   c->cz.resize(nt);
   c->cp.resize(nt);
   c->cap.resize(nt);
+  if (ctype) c->ctype.assign(ctype, ctype + nt);
+  c->rest.assign(nt, 0.0f);
   for (int e = 0; e < nt; ++e) {
     const int32_t* q = &t[4 * e];
+    if (ctype && ctype[e] == 1) {  // length: rest length, no Dm^-1
+      float d[3];
+      for (int k = 0; k < 3; ++k) d[k] = xref[3 * q[0] + k] - xref[3 * q[1] + k];
+      c->rest[e] = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+      std::fill(&c->dminv[9 * e], &c->dminv[9 * e] + 9, 0.0f);
+      c->alpha[e] = compliance > 0 ? compliance / (dt * dt) : 1.0f / (mu * dt * dt * c->rest[e]);
+      continue;
+    }
     double D[3][3];
     for (int i = 0; i < 3; ++i)
       for (int k = 0; k < 3; ++k) D[i][k] = double(xref[3 * q[k + 1] + i]) - xref[3 * q[0] + i];

@@ -241,18 +241,50 @@ def graph_aggregate(indptr, indices, max_agg_size=8):
 # ----------------------------------------------------------------------------
 
 
-def rest_shape(x_ref, t_i, mu, dt, dtype=np.float32, compliance=0.0):
-  """cons/mgpbd_gpu.py:136-151 (compliance > 0: alpha~ = compliance / dt^2)."""
+CONS_ARAP, CONS_LENGTH, CONS_VOLUME = 0, 1, 2
+
+
+def rest_shape(x_ref, t_i, mu, dt, dtype=np.float32, compliance=0.0, ctype=None):
+  """cons/mgpbd_gpu.py:136-151 (compliance > 0: alpha~ = compliance / dt^2).
+
+  With constraint types (the library's MGPBD_CONS_*), a length constraint
+  (slots a, b, a, b) gets its rest length in the volume's place and no
+  Dm^-1 (zeros)."""
   t = np.asarray(t_i, np.int64).reshape(-1, 4)
   x = np.asarray(x_ref, dtype)
+  nt = len(t)
+  is_len = np.zeros(nt, bool) if ctype is None else np.asarray(ctype) == CONS_LENGTH
   Dm = np.stack([x[t[:, 1]] - x[t[:, 0]], x[t[:, 2]] - x[t[:, 0]], x[t[:, 3]] - x[t[:, 0]]], axis=2)
-  dm_inv = np.linalg.inv(Dm.astype(np.float64)).astype(dtype)
-  vol = (np.abs(np.linalg.det(Dm.astype(np.float64))) / 6.0).astype(dtype)
+  dm_inv = np.zeros((nt, 3, 3), dtype)
+  vol = np.zeros(nt, dtype)
+  tt = ~is_len
+  dm_inv[tt] = np.linalg.inv(Dm[tt].astype(np.float64)).astype(dtype)
+  vol[tt] = (np.abs(np.linalg.det(Dm[tt].astype(np.float64))) / 6.0).astype(dtype)
+  d = (x[t[is_len, 0]] - x[t[is_len, 1]]).astype(np.float64)
+  vol[is_len] = np.sqrt((d * d).sum(axis=1)).astype(dtype)
   if compliance > 0:
-    alpha = np.full(len(t), dtype(compliance) / (dtype(dt) * dtype(dt)), dtype)
+    alpha = np.full(nt, dtype(compliance) / (dtype(dt) * dtype(dt)), dtype)
   else:
     alpha = (dtype(1.0) / (dtype(mu) * dtype(dt) * dtype(dt) * vol)).astype(dtype)
   return dm_inv, vol, alpha
+
+
+def volume_values(F):
+  """det F - 1 and d(det F)/dF (columns f2 x f3, f3 x f1, f1 x f2): the
+  hydrostatic constraint of cons/deform3d.py:81-83."""
+  f1, f2, f3 = F[:, :, 0], F[:, :, 1], F[:, :, 2]
+  P = np.stack([np.cross(f2, f3), np.cross(f3, f1), np.cross(f1, f2)], axis=2)
+  return (f1 * P[:, :, 0]).sum(axis=1) - 1.0, P
+
+
+def length_values(x, t_i, rest, dtype):
+  """|x_a - x_b| - L0 and the unit vector a - b (cons/length.py:65-90)."""
+  t = np.asarray(t_i, np.int64).reshape(-1, 4)
+  x = np.asarray(x, dtype)
+  d = x[t[:, 0]] - x[t[:, 1]]
+  ln = np.sqrt((d.astype(np.float64) ** 2).sum(axis=1))
+  n = np.where(ln[:, None] > 1e-12, d / np.where(ln > 0, ln, 1.0)[:, None], 0.0)
+  return (ln - np.asarray(rest, np.float64)).astype(dtype), n.astype(dtype)
 
 
 def svd_rv(F):
@@ -279,18 +311,28 @@ def deformation(x, t_i, dm_inv, dtype):
   return Ds @ np.asarray(dm_inv, dtype)
 
 
-def constraint_values(x, t_i, dm_inv, dtype=np.float32):
+def constraint_values(x, t_i, dm_inv, dtype=np.float32, ctype=None, rest=None):
   F = deformation(x, t_i, dm_inv, dtype)
   _, s, _ = svd_rv(F)
   s = s.astype(dtype)
-  return np.sqrt(((s - dtype(1.0)) ** 2).sum(axis=1)).astype(dtype)
+  c = np.sqrt(((s - dtype(1.0)) ** 2).sum(axis=1)).astype(dtype)
+  if ctype is not None:
+    ct = np.asarray(ctype)
+    vol, _ = volume_values(F.astype(np.float64))
+    c = np.where(ct == CONS_VOLUME, vol.astype(dtype), c)
+    ln, _ = length_values(x, t_i, rest, dtype)
+    c = np.where(ct == CONS_LENGTH, ln, c).astype(dtype)
+  return c
 
 
-def constraints(x, t_i, dm_inv, dtype=np.float32):
+def constraints(x, t_i, dm_inv, dtype=np.float32, ctype=None, rest=None):
   """cons/mgpbd_gpu.py:225-247 + _arap_gradient (cons/mgpbd.py:35-68).
 
   Returns C (nt,) and gradC (nt, 4, 3): g_k = U diag((S-1)/C) V^T Dm^-T
-  column k-1 for k = 1..3, g_0 = -(g_1 + g_2 + g_3), zero when C <= 1e-6."""
+  column k-1 for k = 1..3, g_0 = -(g_1 + g_2 + g_3), zero when C <= 1e-6.
+  With constraint types: volume rows use C = det F - 1 with P = d(det F)/dF
+  in place of U diag((S-1)/C) V^T; length rows C = |x_a - x_b| - L0 with
+  gradients n, -n on slots 0, 1 (rest: the rest lengths)."""
   F = deformation(x, t_i, dm_inv, dtype)
   u, s, v = svd_rv(F)
   u, s, v = u.astype(dtype), s.astype(dtype), v.astype(dtype)
@@ -299,11 +341,25 @@ def constraints(x, t_i, dm_inv, dtype=np.float32):
   Cs = np.where(ok, C, dtype(1.0))
   d = (s - dtype(1.0)) / Cs[:, None]
   P = np.einsum('nrm,nm,ncm->nrc', u, d, v).astype(dtype)
+  if ctype is not None:
+    ct = np.asarray(ctype)
+    vol, Pv = volume_values(F.astype(np.float64))
+    isv = ct == CONS_VOLUME
+    P[isv] = Pv[isv].astype(dtype)
+    C[isv] = vol[isv].astype(dtype)
+    ok = ok | isv
   G = P @ np.swapaxes(np.asarray(dm_inv, dtype), 1, 2)
   g = np.zeros((len(C), 4, 3), dtype)
   g[:, 1:, :] = np.swapaxes(G, 1, 2)
   g[:, 0, :] = -(g[:, 1, :] + g[:, 2, :] + g[:, 3, :])
   g[~ok] = 0
+  if ctype is not None:
+    isl = np.asarray(ctype) == CONS_LENGTH
+    ln, n = length_values(x, t_i, rest, dtype)
+    C[isl] = ln[isl]
+    g[isl] = 0
+    g[isl, 0] = n[isl]
+    g[isl, 1] = -n[isl]
   return C, g
 
 
@@ -379,7 +435,7 @@ class MGPBDOracle:
                rtol=1e-2, maxiter_cg=100, tol_cg=1e-5, n_smooth=2, omega_jacobi=2.0 / 3.0,
                use_line_search=True, dtype=np.float32, kinematic_pins=False, rel_tol_cg=0.0,
                smoother='jacobi', coarse='jacobi', extra_levels=0, max_coarse=400,
-               coarse_sweeps=0, hierarchy=None, cg_alias=False, compliance=0.0):
+               coarse_sweeps=0, hierarchy=None, cg_alias=False, compliance=0.0, ctype=None):
     self.dtype = dtype
     f = dtype
     self.x = np.array(x0, f).reshape(-1, 3)
@@ -410,6 +466,7 @@ class MGPBDOracle:
     self._hierarchy = hierarchy
     self.cg_alias = cg_alias
     self.compliance = compliance
+    self.ctype = None if ctype is None else np.asarray(ctype, np.int32)
     self._vres = None
     self.v = np.zeros_like(self.x)
     self.x_old = np.zeros_like(self.x)
@@ -419,12 +476,12 @@ class MGPBDOracle:
   def init(self):
     f = self.dtype
     self.dm_inv, self.rest_vol, self.alpha = rest_shape(self.x_ref, self.t_i, self.mu, float(self.dt), f,
-                                                        self.compliance)
+                                                        self.compliance, self.ctype)
     ip, ix = sparsity_pattern(self.t_i, self.nt)
     L0 = Level(ip, ix, f)
     self.levels = [L0]
     self.lam = np.zeros(self.nt, f)
-    self.C, self.gradC = constraints(self.x, self.t_i, self.dm_inv, f)
+    self.C, self.gradC = constraints(self.x, self.t_i, self.dm_inv, f, self.ctype, self.rest_vol)
     L0.data = fill_A(ip, ix, self.t_i, self.invm, self.gradC, self.alpha, f)
     if self._hierarchy is None:
       aggs, sizes = tet_hierarchy(self.t_i, self.nt, self.max_coarse)
@@ -602,7 +659,7 @@ class MGPBDOracle:
 
   def dual_norm_at(self, pos):
     f = self.dtype
-    c = constraint_values(pos, self.t_i, self.dm_inv, f)
+    c = constraint_values(pos, self.t_i, self.dm_inv, f, self.ctype, self.rest_vol)
     r = (-(c + self.alpha * self.lam)).astype(np.float64)
     return float(np.sqrt(np.dot(r, r)))
 
@@ -630,7 +687,8 @@ class MGPBDOracle:
     r0 = 0.0
     self.log = []
     for ite in range(self.maxiter):
-      self.C, self.gradC = constraints(self.x, self.t_i, self.dm_inv, f)
+      self.C, self.gradC = constraints(self.x, self.t_i, self.dm_inv, f, self.ctype,
+                                       self.rest_vol)
       b, r = self.residual()
       if ite == 0:
         r0 = r

@@ -1,0 +1,186 @@
+"""Length + volume constraint discretisation (one length constraint per
+unique tet edge, one volume constraint det F - 1 per tet): the system
+builder and its hierarchy (CPU), the oracle's gradients against finite
+differences (CPU), and the CUDA step against the float64 oracle on the same
+constraints (GPU, per stage and per substep, plain V-cycle and FAST paths).
+
+These blocks have no reference counterpart in the MGPBD step (the reference
+uses one ARAP constraint per tet); their definitions follow cons/length.py
+(C = |x_a - x_b| - L0) and the hydrostatic constraint of cons/deform3d.py
+(C = det F - 1), and the oracle is this project's float64 restatement.
+Tolerances as in test_gpu_parity: per-stage 1e-4 relative (C 1e-5),
+positions 1e-5 relative.
+"""
+
+import numpy as np
+import pytest
+
+from controllable_pbd_3d_gb300 import _native as N
+from controllable_pbd_3d_gb300 import meshgen
+from controllable_pbd_3d_gb300.edge_volume import (edge_volume_hierarchy, edge_volume_system,
+                                                   tet_edges)
+from oracle import mgpbd_oracle as MO
+
+
+def body(n=5, jitter=0.03, seed=2):
+  xr, t = meshgen.hex_grid_tets(n, n, n, h=1.0 / n)
+  x0, _ = meshgen.hex_grid_tets(n, n, n, h=1.0 / n, jitter=jitter, seed=seed)
+  invm = np.ones(len(xr), np.float32)
+  invm[meshgen.grid_face_vertices(n, n, n, axis=1, side='max')] = 0.0
+  return xr, x0, t, invm
+
+
+def test_system_builder():
+  _, _, t, _ = body(6)
+  q = t.reshape(-1, 4)
+  c, types, edges, owner = edge_volume_system(t)
+  nt = len(q)
+  assert len(types) == nt + len(edges) and len(c) == 4 * len(types)
+  assert (types[:nt] == N.MGPBD_CONS_VOLUME).all() and (types[nt:] == N.MGPBD_CONS_LENGTH).all()
+  cc = c.reshape(-1, 4)
+  assert np.array_equal(cc[:nt], q)
+  assert np.array_equal(cc[nt:, :2], edges) and np.array_equal(cc[nt:, 2:], edges)
+  # every tet edge exactly once, sorted, owned by the first tet that has it
+  allk = set()
+  for ti, tt in enumerate(q):
+    for a in range(4):
+      for b in range(a + 1, 4):
+        allk.add(tuple(sorted((int(tt[a]), int(tt[b])))))
+  assert len(allk) == len(edges) and (edges[:, 0] < edges[:, 1]).all()
+  assert [tuple(e) for e in edges] == sorted(allk)
+  assert edge_volume_hierarchy(meshgen.hex_grid_tets(4, 4, 4)[1]) is None  # 320 tets: one level
+  for (a, b), o in zip(edges[:50], owner[:50]):
+    has = [i for i, tt in enumerate(q) if a in tt and b in tt]
+    assert o == min(has)
+  agg = edge_volume_hierarchy(t)
+  from controllable_pbd_3d_gb300.tet_aggregation import build_tet_hierarchy
+  Ps, sizes = build_tet_hierarchy(t, None, nt)
+  assert np.array_equal(agg[:nt], Ps[0].indices)
+  assert np.array_equal(agg[nt:], Ps[0].indices[owner])
+  assert set(np.unique(agg)) == set(range(sizes[1]))
+
+
+def test_oracle_gradients_match_finite_differences():
+  xr, x0, t, _ = body(3, 0.08, 5)
+  c, types, _, _ = edge_volume_system(t)
+  dm, rest, _ = MO.rest_shape(xr, c, 1.0, 1.0, np.float64, 1e-6, types)
+  C, g = MO.constraints(x0, c, dm, np.float64, types, rest)
+  x = x0.astype(np.float64)
+  cc = c.reshape(-1, 4)
+  rng = np.random.default_rng(0)
+  h = 1e-7
+  for k in rng.choice(len(types), 40, replace=False):
+    # a vertex listed twice (length constraints: a, b, a, b) gets the sum of
+    # its slots' gradients (the repeated slots carry zero)
+    for v in sorted(set(int(q) for q in cc[k])):
+      for d in range(3):
+        xp = x.copy()
+        xp[v, d] += h
+        xm = x.copy()
+        xm[v, d] -= h
+        one = cc[k:k + 1].reshape(-1)
+        fd = (MO.constraint_values(xp, one, dm[k:k + 1], np.float64, types[k:k + 1],
+                                   rest[k:k + 1])[0] -
+              MO.constraint_values(xm, one, dm[k:k + 1], np.float64, types[k:k + 1],
+                                   rest[k:k + 1])[0]) / (2 * h)
+        want = sum(g[k, s2, d] for s2 in range(4) if cc[k, s2] == v)
+        assert abs(fd - want) <= 1e-5 * max(1.0, abs(want)), (k, v, d, fd, want)
+    if types[k] == N.MGPBD_CONS_LENGTH:
+      assert np.all(g[k, 2:] == 0)
+  # rest state: zero constraint values
+  C0, _ = MO.constraints(xr, c, dm, np.float64, types, rest)
+  assert np.abs(C0).max() < 1e-6
+
+
+def test_oracle_step_converges():
+  xr, x0, t, invm = body(5)
+  c, types, _, _ = edge_volume_system(t)
+  agg = edge_volume_hierarchy(t)
+  o = MO.MGPBDOracle(x0, xr, invm, c, [0, -9.8, 0], 1 / 300, dtype=np.float64, compliance=1e-6,
+                     ctype=types, hierarchy=([agg], [len(types), int(agg.max()) + 1]),
+                     kinematic_pins=True, maxiter=5, maxiter_cg=2000, rel_tol_cg=1e-8,
+                     tol_cg=1e-14, smoother='safe')
+  o.init()
+  o.step(0)
+  assert np.isfinite(o.x).all()
+  b, r = o.residual()
+  assert r < o.log[0][1]
+
+
+def gpu_solver(torch, xr, x0, t, invm, **kw):
+  from controllable_pbd_3d_gb300.mgpbd_gpu import MGPBDSolverGPU
+  x = torch.tensor(x0, device='cuda')
+  s = MGPBDSolverGPU(x, torch.tensor(xr, device='cuda'), torch.tensor(invm, device='cuda'),
+                     torch.tensor(t, device='cuda'), None, [0.0, -9.8, 0.0], 1.0 / 300,
+                     constraints='edge_volume', compliance=1e-6, kinematic_pins=True, **kw)
+  s.init()
+  return s, x
+
+
+def oracle(xr, x0, t, invm, **kw):
+  c, types, _, _ = edge_volume_system(t)
+  agg = edge_volume_hierarchy(t)
+  o = MO.MGPBDOracle(x0, xr, invm, c, [0, -9.8, 0], 1 / 300, compliance=1e-6, ctype=types,
+                     hierarchy=([agg], [len(types), int(agg.max()) + 1]), kinematic_pins=True,
+                     **kw)
+  o.init()
+  return o
+
+
+@pytest.mark.gpu
+def test_gpu_stages_match_oracle(cuda):
+  torch = cuda
+  xr, x0, t, invm = body(6)
+  s, x = gpu_solver(torch, xr, x0, t, invm)
+  o = oracle(xr, x0, t, invm, dtype=np.float32)
+  assert np.allclose(s.rest_vol.cpu().numpy(), o.rest_vol, rtol=1e-5)
+  assert np.allclose(s.alpha_tilde.cpu().numpy(), o.alpha, rtol=1e-6)
+  s._compute_C_and_gradC()
+  C = s.constraints.cpu().numpy()
+  g = s.gradC.cpu().numpy()
+  Co, go = MO.constraints(x0, o.t_i, o.dm_inv, np.float32, o.ctype, o.rest_vol)
+  assert np.abs(C - Co).max() <= 1e-5 * max(np.abs(Co).max(), 1e-3)
+  assert np.abs(g - go).max() <= 1e-4 * np.abs(go).max()
+  s._residual_norm_gpu()
+  s._fill_A_and_update_gpu()
+  A = s._gpu_solver._gpu_As[0].data.cpu().numpy()
+  Ao = MO.fill_A(o.levels[0].indptr, o.levels[0].indices, o.t_i, o.invm, go, o.alpha,
+                 np.float32)
+  assert np.abs(A - Ao).max() <= 1e-4 * np.abs(Ao).max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('variant', ['vcycle', 'fast-primal'])
+def test_gpu_substeps_match_float64_oracle(cuda, variant):
+  torch = cuda
+  xr, x0, t, invm = body(6)
+  kw = dict(damp=0.993, maxiter=5, rtol=1e-6, atol=1e-9, maxiter_cg=4000, tol_cg=1e-12,
+            rel_tol_cg=1e-7)
+  o = oracle(xr, x0, t, invm, dtype=np.float64, smoother='safe', **kw)
+  extra = dict(smoother='safe') if variant == 'vcycle' else dict(
+      mode='fast', precond='cheb', cheb_lo=1e-3, primal=True, primal_tol=1e-2)
+  s, x = gpu_solver(torch, xr, x0, t, invm, **kw, **extra)
+  for k in range(2):
+    o.step(k)
+    s.step(k)
+  err = float(np.abs(x.cpu().numpy() - o.x).max())
+  assert err <= 1e-5 * float(np.abs(o.x).max()), err
+  assert s.stats()['newton_iters'] >= 1
+
+
+@pytest.mark.gpu
+def test_gpu_rejects_a_bad_length_constraint(cuda):
+  torch = cuda
+  from controllable_pbd_3d_gb300.mgpbd_gpu import MGPBDSolverGPU
+  from controllable_pbd_3d_gb300._native import MGPBDError
+  xr, x0, t, invm = body(3)
+  c, types, _, _ = edge_volume_system(t)
+  c = c.copy()
+  c[4 * (len(types) - 1) + 2] = c[4 * (len(types) - 1) + 1]  # (a, b, b, b)
+  s = MGPBDSolverGPU(torch.tensor(x0, device='cuda'), torch.tensor(xr, device='cuda'),
+                     torch.tensor(invm, device='cuda'), torch.tensor(c, device='cuda'), None,
+                     [0.0, -9.8, 0.0], 1.0 / 300, compliance=1e-6)
+  import ctypes as C
+  N.check(s._lib.mgpbd_set_constraint_types(s._h, types.ctypes.data), 'types')
+  with pytest.raises(MGPBDError):
+    s.init()
