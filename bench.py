@@ -3,13 +3,16 @@
 
 Workload (one "step" = one MGPBD substep = prediction + Newton/PCG solve +
 velocity update): a 40x40x40 hex cube, 5 tets per hex (68,921 vertices,
-320,000 tets, 25.9M level-0 nonzeros), rest shape the regular grid, start
-positions jittered U(+-0.01 h) from seed 0, unit vertex mass, top face
-pinned (kinematic), gravity -9.8, dt = 1/60 / 5 substeps, compliance drawn
-log-uniform in [1e-9, 1e-4] from the seed (alpha~ = compliance / dt^2), PCG
-to relative residual 1e-6.  Synthetic data: the reference's experiment
-meshes are not available.  The level-0 matrix (207 MB) exceeds the 129 MB
-L2, so no L2 flush is needed between steps.
+320,000 tets), rest shape the regular grid, start positions jittered
+U(+-0.01 h) from seed 0, unit vertex mass, top face pinned (kinematic),
+gravity -9.8, dt = 1/60 / 5 substeps, compliance drawn log-uniform in
+[1e-9, 1e-4] from the seed (alpha~ = compliance / dt^2), PCG to relative
+residual 1e-6.  Constraints (--constraints): by default one length
+constraint per unique tet edge plus one volume constraint (det F - 1) per
+tet, the construction the benchmark configuration names (718,520
+constraints, 72.4M level-0 nonzeros); 'arap' is the reference step's one
+ARAP constraint per tet (25.9M nonzeros), also reported as a secondary leg.
+Synthetic data: the reference's experiment meshes are not available.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -153,13 +156,18 @@ def max_over_ranks(ws, v):
   return float(t.item())
 
 
-def make_solver(torch, n, kw):
+CONSTRAINT_NAMES = {'edge_volume': 'one length constraint per tet edge + one volume '
+                                   'constraint (det F - 1) per tet',
+                    'arap': 'one ARAP constraint per tet (the reference step)'}
+
+
+def make_solver(torch, n, kw, constraints='edge_volume'):
   from controllable_pbd_3d_gb300.mgpbd_gpu import MGPBDSolverGPU
   xr, x0, t, invm, compliance = workload(n)
   x = torch.tensor(x0, device='cuda')
   s = MGPBDSolverGPU(x, torch.tensor(xr, device='cuda'), torch.tensor(invm, device='cuda'),
                      torch.tensor(t, device='cuda'), None, [0.0, -9.8, 0.0], DT,
-                     compliance=compliance, **kw)
+                     compliance=compliance, constraints=constraints, **kw)
   s.init()
   return s, x, compliance
 
@@ -266,12 +274,13 @@ def primal_iteration_bytes(nt, nv, degree):
 
 # DRAM bytes (read + write) of one launch of each persistent kernel on the
 # 40^3 workload, from one ncu capture each of `bench.py --profile-solve
-# --size 40` (dram__bytes_read.sum + dram__bytes_write.sum): almost all of it
-# is the first read of the operator data, staged on chip for the solve
-TRAFFIC_40 = {'k_pcg': 44874752, 'k_jcg': 46275840}
+# --size 40 --constraints arap|edge_volume` (dram__bytes_read.sum +
+# dram__bytes_write.sum)
+TRAFFIC_40 = {'arap': {'k_pcg': 44874752, 'k_jcg': 46275840},
+              'edge_volume': {'k_pcg': 21536038400, 'k_jcg': 71564010240}}
 
 
-def roofline_from_steps(st, nt, nv, degree, hbm_peak, peak_kind, size=40):
+def roofline_from_steps(st, nt, nv, degree, hbm_peak, peak_kind, size=40, constraints='arap'):
   """Roofline of the two persistent kernels over the timed steps, from the
   CUDA events the library records around each launch on its stream (stats
   ms_warm / ms_dual) and the iterations each ran.  The one with more GPU
@@ -303,7 +312,8 @@ def roofline_from_steps(st, nt, nv, degree, hbm_peak, peak_kind, size=40):
                 'cg_iterations_per_launch': round(its / n, 1), 'launch_us': round(dt * 1e6, 1),
                 'us_per_cg_iteration': round(ms * 1e3 / max(its, 1), 2),
                 'share_of_step_gpu_time': None,
-                'traffic': TRAFFIC_40[name[:5]] if size == 40 else None})
+                'traffic': (TRAFFIC_40.get(constraints, {}).get(name[:5]) if size == 40
+                            else None)})
   out.sort(key=lambda r: -r['launch_us'] * r['launches'])
   total = sum(r['launch_us'] * r['launches'] for r in out)
   for r in out:
@@ -313,7 +323,8 @@ def roofline_from_steps(st, nt, nv, degree, hbm_peak, peak_kind, size=40):
   roof['cg_path'] = path
   if roof['traffic'] is not None:
     roof['traffic_source'] = ('ncu dram__bytes_read.sum + dram__bytes_write.sum of one '
-                              'launch of bench.py --profile-solve --size 40 (same workload)')
+                              'launch of bench.py --profile-solve --size 40 --constraints '
+                              f'{constraints} (same workload)')
   roof['working_set_note'] = ('operator data staged in shared memory / resident in L2 across '
                               'each solve: the rate is on-chip, not HBM')
   if len(out) > 1:
@@ -352,11 +363,14 @@ def roofline_csr(torch, s, hbm_peak, peak_kind, reps=40):
   return roof
 
 
-# CG iterations per Newton iteration the plain AMG-PCG needs on this
-# workload (GB300 run, 20 Newton iterations of one substep: 1877-2138, mean
-# 1970); the GPU arm re-measures it every run from its plain leg
-PLAIN_CG_PER_NEWTON = 1970
-NEWTON_PER_SUBSTEP = 20  # the stiff workload always runs the full 20 Newton iterations
+# Newton iterations per substep and CG iterations per Newton iteration of
+# the plain AMG-PCG on the 40^3 workload, per constraint construction
+# (GB300 runs; ARAP: every substep runs the full 20 Newton iterations at
+# 1877-2138 CG iterations, mean 1970; length + volume: 2 Newton iterations
+# at ~2577 CG iterations).  The GPU arm re-measures both every run from its
+# plain leg; the reference arm, which has no GPU, uses these.
+PLAIN_CG_PER_NEWTON = {'arap': 1970, 'edge_volume': 2577}
+NEWTON_PER_SUBSTEP = {'arap': 20, 'edge_volume': 2}
 
 
 class CpuSampler:
@@ -365,15 +379,22 @@ class CpuSampler:
   of substep 0 with its CG capped at `cg_sample` iterations: constraints,
   residual, matrix fill, Galerkin refill, smoother weights, the CG
   iterations, scatter, line search, apply.  A substep is then
-  NEWTON_PER_SUBSTEP x (non-CG time + cg_per_newton x time per CG iteration)."""
+  newton_per_substep x (non-CG time + cg_per_newton x time per CG iteration)."""
 
-  def __init__(self, n, cg_sample=20):
+  def __init__(self, n, cg_sample=20, constraints='edge_volume'):
     from oracle.cpu_port import CpuPort, threads
     xr, x0, t, invm, compliance = workload(n)
     self.cg_sample = cg_sample
+    ctype = agg = None
+    if constraints == 'edge_volume':
+      from controllable_pbd_3d_gb300.edge_volume import edge_volume_hierarchy, edge_volume_system
+      c, ctype, _, _ = edge_volume_system(t)
+      agg = edge_volume_hierarchy(t)
+      t = c
     self.port = CpuPort(x0, xr, invm, t, [0.0, -9.8, 0.0], DT, compliance=compliance,
                         maxiter=20, atol=1e-4, rtol=1e-2, maxiter_cg=cg_sample, tol_cg=1e-12,
-                        rel_tol_cg=1e-6, n_smooth=2, kinematic_pins=True)
+                        rel_tol_cg=1e-6, n_smooth=2, kinematic_pins=True, ctype=ctype,
+                        hierarchy=agg)
     self.threads = threads()
     from oracle.cpu_port import lib
     lib().cpu_predict(self.port.h)
@@ -386,8 +407,8 @@ class CpuSampler:
     t_other = out[3] + out[4] + out[6]
     return t_other, t_cg, int(out[1])
 
-  def substeps_per_s(self, t_other, t_cg, cg_per_newton):
-    return 1.0 / (NEWTON_PER_SUBSTEP * (t_other + cg_per_newton * t_cg))
+  def substeps_per_s(self, t_other, t_cg, cg_per_newton, newton_per_substep):
+    return 1.0 / (newton_per_substep * (t_other + cg_per_newton * t_cg))
 
 
 def net_forward_bytes(n, nnz):
@@ -413,7 +434,7 @@ def learned_leg(torch, args, hbm, kind):
   kwr = dict(SOLVER_KW)
   kwr.update(PLAIN_KW)
   kwr['maxiter'] = 1
-  sr, _, _ = make_solver(torch, args.size, kwr)
+  sr, _, _ = make_solver(torch, args.size, kwr, args.constraints)
   sr.record_coarse(256, 4)
   sr.step(0)
   rc, ec = sr.recorded_coarse()
@@ -446,7 +467,7 @@ def learned_leg(torch, args, hbm, kind):
   kwl = dict(SOLVER_KW)
   kwl.update(PLAIN_KW)
   kwl['precond'] = 'learned'
-  sl, _, _ = make_solver(torch, args.size, kwl)
+  sl, _, _ = make_solver(torch, args.size, kwl, args.constraints)
   sl.set_coarse_net(net)
   shapes = sl.autotune(reps=5)
   k = max(1, min(args.steps, args.plain_steps))
@@ -473,19 +494,55 @@ def learned_leg(torch, args, hbm, kind):
   return out
 
 
-def run_ours(args):
-  import torch
-  ws, rank, local = dist_init(args)
-  torch.cuda.set_device(local)
-  from controllable_pbd_3d_gb300 import _native as N
-  hbm, kind = peaks()
+def fast_kw(args):
   kw = dict(SOLVER_KW)
   kw.update(FAST_KW)
   if args.no_graph:
     kw['use_graph'] = False
   if args.primal is not None:
     kw['primal'] = bool(args.primal)
-  s, x, compliance = make_solver(torch, args.size, kw)
+  return kw
+
+
+def plain_leg(torch, args, hbm, kind, constraints):
+  """The plain float32 AMG-PCG on the same workload (fewer steps: it is
+  slow), its row-kernel tile shapes picked by the autotuner."""
+  kwp = dict(SOLVER_KW)
+  kwp.update(PLAIN_KW)
+  sp_, _, _ = make_solver(torch, args.size, kwp, constraints)
+  shapes = sp_.autotune(reps=5)
+  # the same substeps as the fast leg where that is affordable: the length +
+  # volume body needs 2 Newton iterations in substep 0 and 1 later (warm up
+  # like the fast leg, ~6 s a substep); every ARAP substep runs the full 20
+  # Newton iterations (~36 s), so ARAP times its first substep
+  warm = 0 if constraints == 'arap' else min(args.warmup, 3)
+  for i in range(warm):
+    sp_.step(i)
+  k_plain = max(1, min(args.steps, args.plain_steps))
+  tp, stp = time_steps(torch, sp_, k_plain, warm)
+  roof_csr = roofline_csr(torch, sp_, hbm, kind)
+  plain = {'value': round(k_plain / tp, 4), 'unit': UNIT, 'steps': k_plain, 'warmup': warm,
+           'newton_iters_per_step': sum(x['newton_iters'] for x in stp) / k_plain,
+           'cg_iters_per_step': sum(x['cg_iters_total'] for x in stp) / k_plain,
+           'config': 'parity-mode CSR V-cycle (2-level tet aggregation, 50 coarse Jacobi '
+                     'sweeps, smoother weight min(2/3, 4/(3 lambda_max))), host-checked loops',
+           'row_shapes': {str(l): c for l, c in shapes.items()},
+           'row_shape_us': {str(l): round(t, 2) for l, (_, t) in sp_.last_tuning.items()},
+           'roofline': roof_csr}
+  del sp_
+  torch.cuda.empty_cache()
+  return plain
+
+
+def run_ours(args):
+  import torch
+  ws, rank, local = dist_init(args)
+  torch.cuda.set_device(local)
+  from controllable_pbd_3d_gb300 import _native as N
+  hbm, kind = peaks()
+  cons = args.constraints
+  kw = fast_kw(args)
+  s, x, compliance = make_solver(torch, args.size, kw, cons)
   for i in range(args.warmup):
     s.step(i)
   torch.cuda.synchronize()
@@ -523,43 +580,23 @@ def run_ours(args):
          'h2d_bytes_per_step': 2 * x.numel() * 4, 'd2h_bytes_per_step': 2 * x.numel() * 4}
 
   roof = roofline_from_steps(st, s.n_tets, s.n_verts, FAST_KW['cheb_degree'], hbm, kind,
-                             args.size)
+                             args.size, cons)
   roof['matrix_free_apply'] = roofline_matrix_free(torch, s, hbm, kind)
   st0 = st[-1]
-  n_verts, n_tets = s.n_verts, s.n_tets
+  n_verts, n_cons = s.n_verts, s.n_tets
+  n_tets = s.n_mesh_tets
   del s
   torch.cuda.empty_cache()
 
-  # the plain float32 AMG-PCG on the same workload (fewer steps: it is slow)
-  plain = None
-  if not args.no_plain:
-    kwp = dict(SOLVER_KW)
-    kwp.update(PLAIN_KW)
-    sp_, xp, _ = make_solver(torch, args.size, kwp)
-    # the row-kernel tile shape of each level, picked by timing (autotuner)
-    shapes = sp_.autotune(reps=5)
-    # no warm-up step: the plain path captures nothing and each substep
-    # takes ~40 s; its first substep is timed
-    k_plain = max(1, min(args.steps, args.plain_steps))
-    tp, stp = time_steps(torch, sp_, k_plain, 0)
-    roof_csr = roofline_csr(torch, sp_, hbm, kind)
-    plain = {'value': round(k_plain / tp, 4), 'unit': UNIT, 'steps': k_plain,
-             'newton_iters_per_step': sum(x['newton_iters'] for x in stp) / k_plain,
-             'cg_iters_per_step': sum(x['cg_iters_total'] for x in stp) / k_plain,
-             'config': 'parity-mode CSR V-cycle (2-level tet aggregation, 50 coarse Jacobi '
-                       'sweeps, smoother weight min(2/3, 4/(3 lambda_max))), host-checked loops',
-             'row_shapes': {str(l): c for l, c in shapes.items()},
-             'row_shape_us': {str(l): round(t, 2) for l, (_, t) in sp_.last_tuning.items()},
-             'roofline': roof_csr}
-    del sp_
-    torch.cuda.empty_cache()
+  plain = None if args.no_plain else plain_leg(torch, args, hbm, kind, cons)
   out = {
       'metric': METRIC, 'value': round(value, 3), 'unit': UNIT, 'n_gpus': ws,
       'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(t_max * 1e3 / args.steps, 3),
       'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
       'data': 'synthetic (seeded hex-grid cube; reference meshes unavailable)',
       'config': {'workload': f'{args.size}^3 hex cube, 5 tets/hex', 'n_verts': n_verts,
-                 'n_tets': n_tets, 'nnz_level0': st0['nnz'][0], 'levels': st0['rows'],
+                 'n_tets': n_tets, 'constraints': CONSTRAINT_NAMES[cons],
+                 'n_constraints': n_cons, 'nnz_level0': st0['nnz'][0], 'levels': st0['rows'],
                  'compliance': compliance, 'dt': DT, 'rel_res_cg': 1e-6, 'mode': 'fast',
                  'solver': ('primal warm start + dual persistent Chebyshev-8 CG'
                             if kw.get('primal') else 'dual persistent Chebyshev-8 CG'),
@@ -577,19 +614,42 @@ def run_ours(args):
     if plain is not None:
       lrn['speedup_vs_plain'] = round(lrn['value'] / plain['value'], 3)
     out['learned_amg_pcg'] = lrn
+  if cons != 'arap' and not args.no_arap:
+    # the reference step's own constraint (one ARAP constraint per tet) on
+    # the same body: the fast step and the plain AMG-PCG
+    k = max(1, min(args.steps, 5))
+    sa, _, _ = make_solver(torch, args.size, kw, 'arap')
+    for i in range(min(args.warmup, 3)):
+      sa.step(i)
+    ta, sta = time_steps(torch, sa, k, args.warmup)
+    arap = {'constraints': CONSTRAINT_NAMES['arap'], 'value': round(k / ta, 4), 'unit': UNIT,
+            'steps': k, 'newton_iters_per_step': sum(x['newton_iters'] for x in sta) / k,
+            'cg_iters_per_step': sum(x['cg_iters_total'] for x in sta) / k,
+            'nnz_level0': sta[-1]['nnz'][0],
+            'roofline': roofline_from_steps(sta, sa.n_tets, sa.n_verts, FAST_KW['cheb_degree'],
+                                            hbm, kind, args.size, 'arap')}
+    del sa
+    torch.cuda.empty_cache()
+    if not args.no_plain:
+      arap['plain_fp32_amg_pcg'] = plain_leg(torch, args, hbm, kind, 'arap')
+      arap['speedup_vs_plain'] = round(arap['value'] / arap['plain_fp32_amg_pcg']['value'], 2)
+    out['arap'] = arap
   if rank == 0 and not args.no_cpu_baseline:
-    cpu = CpuSampler(args.size)
+    cpu = CpuSampler(args.size, constraints=cons)
     cpu.sample()  # warm-up (first-touch of the host arrays)
     t_other, t_cg, n_cg = cpu.sample()
-    cg_per_newton = (plain['cg_iters_per_step'] / max(plain['newton_iters_per_step'], 1)
-                     if plain is not None else PLAIN_CG_PER_NEWTON)
+    if plain is not None:
+      newton_ps = max(plain['newton_iters_per_step'], 1.0)
+      cg_per_newton = plain['cg_iters_per_step'] / newton_ps
+    else:
+      newton_ps, cg_per_newton = NEWTON_PER_SUBSTEP[cons], PLAIN_CG_PER_NEWTON[cons]
     out['cpu_baseline'] = {
-        'value': round(cpu.substeps_per_s(t_other, t_cg, cg_per_newton), 6), 'unit': UNIT,
-        'cores': cpu.threads, 'kind': 'port',
+        'value': round(cpu.substeps_per_s(t_other, t_cg, cg_per_newton, newton_ps), 6),
+        'unit': UNIT, 'cores': cpu.threads, 'kind': 'port',
         'sample': f'OpenMP CPU port of the plain step (oracle/cpu_step.cpp), one Newton '
                   f'iteration of substep 0 with {n_cg} CG iterations: {t_other:.2f} s outside '
                   f'CG + {t_cg * 1e3:.1f} ms per CG iteration, scaled to '
-                  f'{NEWTON_PER_SUBSTEP} x ({cg_per_newton:.0f} CG iterations + the rest) per '
+                  f'{newton_ps:g} x ({cg_per_newton:.0f} CG iterations + the rest) per '
                   'substep; setup excluded'}
   if rank == 0:
     print(json.dumps(out), flush=True)
@@ -610,7 +670,7 @@ def run_profile_solve(args):
   if args.primal is not None:
     kw['primal'] = bool(args.primal)
   kw['maxiter_cg'] = args.profile_maxiter
-  s, x, _ = make_solver(torch, args.size, kw)
+  s, x, _ = make_solver(torch, args.size, kw, args.constraints)
   s.make_prediction()
   s.lambdaf.zero_()
   s._compute_C_and_gradC()
@@ -620,7 +680,8 @@ def run_profile_solve(args):
   t0 = time.perf_counter()
   it = s._gpu_solver.solve(s._b_gpu, s._dlam_gpu)
   torch.cuda.synchronize()
-  print(json.dumps({'profile_solve': args.profile_precond, 'size': args.size, 'cg_iters': it,
+  print(json.dumps({'profile_solve': args.profile_precond, 'size': args.size,
+                    'constraints': args.constraints, 'cg_iters': it,
                     'seconds': round(time.perf_counter() - t0, 4),
                     'status': s.stats()['status']}), flush=True)
 
@@ -635,7 +696,7 @@ def run_profile_net(args):
   kwr = dict(SOLVER_KW)
   kwr.update(PLAIN_KW)
   kwr['maxiter'] = 1
-  sr, _, _ = make_solver(torch, args.size, kwr)
+  sr, _, _ = make_solver(torch, args.size, kwr, args.constraints)
   sr.record_coarse(64, 8)
   sr.step(0)
   rc, _ = sr.recorded_coarse()
@@ -658,7 +719,8 @@ def run_reference(args):
   rank = int(os.environ.get('RANK', '0'))
   if rank != 0:
     return
-  cpu = CpuSampler(args.size)
+  cons = args.constraints
+  cpu = CpuSampler(args.size, constraints=cons)
   others, cgs = [], []
   t0 = time.perf_counter()
   for i in range(args.warmup + args.steps):
@@ -668,17 +730,17 @@ def run_reference(args):
       cgs.append(t_cg)
   wall = time.perf_counter() - t0
   t_other, t_cg = float(np.mean(others)), float(np.mean(cgs))
-  value = cpu.substeps_per_s(t_other, t_cg, PLAIN_CG_PER_NEWTON)
+  value = cpu.substeps_per_s(t_other, t_cg, PLAIN_CG_PER_NEWTON[cons], NEWTON_PER_SUBSTEP[cons])
   sample = (f'per step: one Newton iteration of substep 0 with {n_cg} CG iterations '
             f'({t_other:.2f} s outside CG + {t_cg * 1e3:.1f} ms per CG iteration); value scaled '
-            f'to {NEWTON_PER_SUBSTEP} x ({PLAIN_CG_PER_NEWTON} CG iterations + the rest) per '
-            'substep; OpenMP CPU port of the plain step, all host threads')
+            f'to {NEWTON_PER_SUBSTEP[cons]} x ({PLAIN_CG_PER_NEWTON[cons]} CG iterations + the '
+            'rest) per substep; OpenMP CPU port of the plain step, all host threads')
   out = {'metric': METRIC, 'value': round(value, 6), 'unit': UNIT, 'n_gpus': ws,
          'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(1e3 / value, 1),
          'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
          'data': 'synthetic (seeded hex-grid cube)', 'impl': 'reference',
          'config': {'workload': f'{args.size}^3 hex cube, 5 tets/hex', 'rel_res_cg': 1e-6,
-                    'sample_wall_s': round(wall, 1)},
+                    'constraints': CONSTRAINT_NAMES[cons], 'sample_wall_s': round(wall, 1)},
          'cpu_baseline': {'value': round(value, 6), 'unit': UNIT, 'cores': cpu.threads,
                           'kind': 'port', 'sample': sample},
          'e2e': {'value': round(value, 6), 'unit': UNIT, 'h2d_bytes_per_step': 0,
@@ -697,6 +759,9 @@ def main():
   ap.add_argument('--no-plain', action='store_true')
   ap.add_argument('--plain-steps', type=int, default=1)
   ap.add_argument('--no-learned', action='store_true')
+  ap.add_argument('--no-arap', action='store_true')
+  # the constraint construction of the headline workload
+  ap.add_argument('--constraints', default='edge_volume', choices=['edge_volume', 'arap'])
   # same kernels launched from a host loop instead of one CUDA graph per
   # CG solve (ncu cannot profile kernels inside conditional graphs)
   ap.add_argument('--no-graph', action='store_true')

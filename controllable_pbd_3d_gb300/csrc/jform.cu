@@ -21,12 +21,13 @@ using namespace jdev;
 constexpr int kT = 256;  // threads per block
 
 // ---------------------------------------------------------------------------
-__global__ void k_jprep(const int32_t* __restrict__ inc_ent, const float* __restrict__ gradC,
-                        const int4* __restrict__ t_i, const float* __restrict__ invm,
-                        const float* __restrict__ alpha, int32_t nt, float4* __restrict__ gV,
-                        float* __restrict__ dinv, float4* __restrict__ gT) {
+__global__ void k_jprep(const int32_t* __restrict__ inc_ent, int64_t ne,
+                        const float* __restrict__ gradC, const int4* __restrict__ t_i,
+                        const float* __restrict__ invm, const float* __restrict__ alpha,
+                        int32_t nt, float4* __restrict__ gV, float* __restrict__ dinv,
+                        float4* __restrict__ gT) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < 4LL * nt; k += stride) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < ne; k += stride) {
     const int32_t e = inc_ent[k];
     const float* g = gradC + 3LL * e;
     gV[k] = make_float4(g[0], g[1], g[2], __int_as_float(e >> 2));
@@ -423,9 +424,9 @@ TArgs targs(const JView& j) {
 
 void launch_jform_prepare(const JView& j, const int32_t* inc_ent, float4* gV, float* dinv,
                           float4* gT, cudaStream_t s) {
-  int g = tgrid(4LL * j.nt);
-  k_jprep<<<g, kT, 0, s>>>(inc_ent, j.gradC, reinterpret_cast<const int4*>(j.t_i), j.invm, j.alpha,
-                           j.nt, gV, dinv, gT);
+  int g = tgrid(std::max<int64_t>(j.ne, j.nt));
+  k_jprep<<<g, kT, 0, s>>>(inc_ent, j.ne, j.gradC, reinterpret_cast<const int4*>(j.t_i), j.invm,
+                           j.alpha, j.nt, gV, dinv, gT);
   MGPBD_CHECK_LAUNCH();
 }
 

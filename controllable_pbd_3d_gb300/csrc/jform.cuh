@@ -49,8 +49,9 @@ struct JView {
   const int32_t* t_i = nullptr;      // (nt, 4)
   const float* gradC = nullptr;      // (nt, 4, 3)
   const float4* gT = nullptr;        // gradC as 3 planes of nt float4 (persistent CG)
-  const float4* gV = nullptr;        // (4 nt) vertex-major (g, tet id)
+  const float4* gV = nullptr;        // (ne) vertex-major (g, tet id)
   const int32_t* inc_ptr = nullptr;  // (nv + 1)
+  int64_t ne = 0;                    // incidence entries (<= 4 nt: repeated slots left out)
   const float* invm = nullptr;       // (nv)
   const float* alpha = nullptr;      // (nt)
   const float* dinv = nullptr;       // (nt) 1 / diag(A)

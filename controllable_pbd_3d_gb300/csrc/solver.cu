@@ -309,6 +309,7 @@ void Solver::init() {
   vertex_incidence(t_host.data(), nt_, nv_, ip, ie);
   upload(inc_ptr_, ip, s);
   upload(inc_ent_, ie, s);
+  inc_n_ = static_cast<int64_t>(ie.size());
   if (cheb() && p_.persistent) {
     jplan_ = jcg_plan(ip, nv_, nt_);
     if (primal()) {
@@ -581,6 +582,7 @@ JView Solver::jview() {
   j.gT = gT_.p;
   j.gV = gV_.p;
   j.inc_ptr = inc_ptr_.p;
+  j.ne = inc_n_;
   j.invm = invm_;
   j.alpha = alpha_.p;
   j.dinv = jdinv_.p;

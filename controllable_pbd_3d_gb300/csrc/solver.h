@@ -154,6 +154,7 @@ class Solver {
   DevBuf<float> x_old_, x_pred_, dpos_;
   DevBuf<float> dm_inv_, rest_vol_, alpha_, lambda_, C_, gradC_, rhs_, dlam_;
   DevBuf<int32_t> inc_ptr_, inc_ent_;
+  int64_t inc_n_ = 0;                  // incidence entries
   DevBuf<int32_t> ctype_;              // constraint types (absent: all ARAP)
   std::vector<int32_t> ctype_host_;
   std::vector<Level> levels_;

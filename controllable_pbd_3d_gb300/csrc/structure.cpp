@@ -577,15 +577,25 @@ int32_t graph_aggregate(const Csr& a, int32_t max_agg_size, std::vector<int32_t>
   return n_agg;
 }
 
+// A slot repeating a vertex of an earlier slot of its constraint (a length
+// constraint lists its edge twice) carries a zero gradient and is left out.
 void vertex_incidence(const int32_t* t_i, int32_t nt, int32_t nv, std::vector<int32_t>& ptr,
                       std::vector<int32_t>& ent) {
+  auto repeated = [&](int32_t t, int l) {
+    for (int m = 0; m < l; ++m)
+      if (t_i[4LL * t + m] == t_i[4LL * t + l]) return true;
+    return false;
+  };
   ptr.assign(nv + 1, 0);
-  for (int64_t k = 0; k < 4LL * nt; ++k) ptr[t_i[k] + 1]++;
+  for (int32_t t = 0; t < nt; ++t)
+    for (int l = 0; l < 4; ++l)
+      if (!repeated(t, l)) ptr[t_i[4LL * t + l] + 1]++;
   for (int32_t v = 0; v < nv; ++v) ptr[v + 1] += ptr[v];
   ent.resize(ptr[nv]);
   std::vector<int32_t> cur(ptr.begin(), ptr.end() - 1);
   for (int32_t t = 0; t < nt; ++t)
-    for (int l = 0; l < 4; ++l) ent[cur[t_i[4LL * t + l]]++] = 4 * t + l;
+    for (int l = 0; l < 4; ++l)
+      if (!repeated(t, l)) ent[cur[t_i[4LL * t + l]]++] = 4 * t + l;
 }
 
 }  // namespace mgpbd
