@@ -90,11 +90,20 @@ class BodyBatch:
                                  compliance=self.bodies[0].compliance, **solver_kw)
     self.dt = float(dt)
 
+  def constraint_body(self) -> np.ndarray:
+    """Body id of every constraint: one per tet (ARAP), or the volume
+    constraints in tet order followed by the length constraints (their
+    body from the edge's first vertex) with constraints='edge_volume'."""
+    tet_body = np.repeat(np.arange(len(self.bodies)), np.diff(self.tet_off))
+    if self.solver.constraint_kind != 'edge_volume':
+      return tet_body
+    edge_body = np.searchsorted(self.vert_off, self.solver.edges[:, 0], side='right') - 1
+    return np.concatenate([tet_body, edge_body])
+
   def init(self):
     self.solver.init()
-    alpha = np.empty(int(self.tet_off[-1]), np.float32)
-    for b, body in enumerate(self.bodies):
-      alpha[self.tet_off[b]:self.tet_off[b + 1]] = body.compliance / (self.dt * self.dt)
+    comp = np.array([b.compliance for b in self.bodies], np.float64)
+    alpha = (comp[self.constraint_body()] / (self.dt * self.dt)).astype(np.float32)
     self.solver.alpha_tilde.copy_(torch.from_numpy(alpha).to(self.solver.alpha_tilde.device))
 
   def step(self, frame: int = 0):
@@ -106,6 +115,10 @@ class BodyBatch:
   @property
   def n_tets(self) -> int:
     return int(self.tet_off[-1])
+
+  @property
+  def n_constraints(self) -> int:
+    return int(self.solver.n_tets)
 
   @property
   def n_verts(self) -> int:

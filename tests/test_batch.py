@@ -68,3 +68,44 @@ def test_batched_solve_equals_per_body_solves(cuda):
     ref = first_solve(s)
     got = dl[batch.tet_off[b]:batch.tet_off[b + 1]]
     assert float(np.abs(got - ref).max()) <= 1e-4 * float(np.abs(ref).max()), b
+
+
+@pytest.mark.gpu
+def test_batched_edge_volume_solve_equals_per_body_solves(cuda):
+  """The same with one length constraint per edge and one volume constraint
+  per tet: each body's constraints (its volume block, then its edges) take
+  its own compliance, and the packed solve equals the per-body solves."""
+  from controllable_pbd_3d_gb300.batch import BodyBatch
+  from controllable_pbd_3d_gb300.mgpbd_gpu import MGPBDSolverGPU
+  g, dt = [0.0, -9.8, 0.0], 1 / 300
+  kw = dict(mode='fast', precond='cheb', rel_tol_cg=1e-9, tol_cg=1e-14, maxiter_cg=6000,
+            primal=False, constraints='edge_volume')
+  bodies = random_bodies(3, seed=4, dims=(3, 6))
+
+  def first_solve(s):
+    s.make_prediction()
+    s.lambdaf.zero_()
+    s._compute_C_and_gradC()
+    s._residual_norm_gpu()
+    s._fill_A_and_update_gpu()
+    s._gpu_solver.solve(s._b_gpu, s._dlam_gpu)
+    return s._dlam_gpu.detach().cpu().numpy().copy()
+
+  batch = BodyBatch(bodies, g, dt, **kw)
+  batch.init()
+  owner = batch.constraint_body()
+  nt = batch.n_tets
+  alpha = batch.solver.alpha_tilde.cpu().numpy()
+  for b, body in enumerate(bodies):
+    assert np.allclose(alpha[owner == b], body.compliance / dt ** 2, rtol=1e-6)
+  dl = first_solve(batch.solver)
+  for b, body in enumerate(bodies):
+    x = cuda.tensor(body.x0, device='cuda')
+    s = MGPBDSolverGPU(x, cuda.tensor(body.x_ref, device='cuda'),
+                       cuda.tensor(body.invm, device='cuda'), cuda.tensor(body.t_i, device='cuda'),
+                       None, g, dt, compliance=body.compliance, **kw)
+    s.init()
+    ref = first_solve(s)
+    got = np.concatenate([dl[batch.tet_off[b]:batch.tet_off[b + 1]], dl[nt:][owner[nt:] == b]])
+    assert len(got) == len(ref)
+    assert float(np.abs(got - ref).max()) <= 1e-4 * float(np.abs(ref).max()), b
