@@ -229,47 +229,61 @@ def roofline_matrix_free(torch, s, hbm_peak, peak_kind, reps=50):
   x = torch.randn(nt, device='cuda')
   s.apply_A(x, matrix_free=1)
   dt = _event_time(torch, lambda: s.apply_A(x, matrix_free=2), reps)
-  bytes_ = apply_bytes(nt, nv)
+  ne, _ = operator_shape(s)
+  bytes_ = apply_bytes(nt, nv, ne, 0)  # the per-phase tet kernel reads all four slots
   achieved = bytes_ / dt / 1e9
   return {'kernel': 'k_jv<kSrcX> + k_jt_plain (matrix-free A x, 2 launches)', 'bound': 'hbm',
           'achieved': round(achieved, 1), 'peak': hbm_peak, 'unit': 'GB/s',
           'frac': round(achieved / hbm_peak, 4), 'peak_kind': peak_kind,
           'algorithmic_bytes_per_launch': bytes_, 'launch_us': round(dt * 1e6, 2),
-          'working_set_note': 'the operator data (~46 MB at 320k tets) fits in the 129 MB L2, '
-                              'so repeated applications can exceed the HBM roofline',
+          'working_set_note': 'operator data of repeated applications stays partly in the '
+                              '129 MB L2, so the rate can exceed the HBM roofline',
           'traffic': None}
 
 
-def apply_bytes(nt, nv):
-  """Algorithmic bytes of one matrix-free A x: the vertex phase reads the
-  vertex-major gradients (16 B per tet slot), row offsets and inverse
-  masses, gathers x once per tet and writes u (16 B per vertex); the tet
-  phase reads tet indices (16 B), gradients (48 B), alpha, x, gathers u once
-  per vertex and writes y."""
-  return (16 * 4 * nt + 4 * (nv + 1) + 4 * nv + 4 * nt + 16 * nv) + \
-         (16 * nt + 48 * nt + 16 * nv + 4 * nt + 4 * nt + 4 * nt)
+def apply_bytes(nt, nv, ne=None, n2=0):
+  """Algorithmic bytes of one matrix-free A x over nt constraints, ne
+  vertex-incidence entries (4 per constraint, 2 per length constraint) and
+  n2 length constraints read in compact form: the vertex phase reads the
+  vertex-major gradients (16 B per entry), row offsets and inverse masses,
+  gathers x once per constraint and writes u (16 B per vertex); the tet
+  phase reads constraint indices and gradients (16 + 48 B, compact length
+  constraints 8 + 16 B), alpha, x, gathers u once per vertex and writes y."""
+  ne = 4 * nt if ne is None else ne
+  return (16 * ne + 4 * (nv + 1) + 4 * nv + 4 * nt + 16 * nv) + \
+         (64 * (nt - n2) + 24 * n2 + 16 * nv + 4 * nt + 4 * nt + 4 * nt)
 
 
-def cg_iteration_bytes(nt, nv, degree):
+def cg_iteration_bytes(nt, nv, degree, ne=None, n2=0):
   """Algorithmic bytes of one Chebyshev-preconditioned CG iteration of the
-  persistent kernel: `degree` operator applications, plus per tet the
-  Chebyshev-step vectors (r, d, 1/diag read, d, z written: 20 B per step
+  persistent kernel: `degree` operator applications, plus per constraint
+  the Chebyshev-step vectors (r, d, 1/diag read, d, z written: 20 B per step
   after the first), the p / Ap phase (z, p read, p, Ap written: 16 B) and the
   x / r update (p, Ap, x, x-compensation, r, 1/diag read; x,
   x-compensation, r, z, d written: 44 B)."""
-  return degree * apply_bytes(nt, nv) + (degree - 1) * 20 * nt + 16 * nt + 44 * nt
+  return degree * apply_bytes(nt, nv, ne, n2) + (degree - 1) * 20 * nt + 16 * nt + 44 * nt
 
 
-def primal_iteration_bytes(nt, nv, degree):
+def primal_iteration_bytes(nt, nv, degree, ne=None, n2=0):
   """Algorithmic bytes of one primal (vertex-space) CG iteration: `degree`
-  applications of K, each a tet phase (tet indices 16 B, gradients 48 B,
-  alpha 4 B, s written 4 B, the vertex vector gathered once per vertex
-  16 B) and a vertex phase (vertex-major gradients 64 B per tet, offsets and
-  weights 8 B per vertex, s gathered once per tet); per vertex the
-  Chebyshev epilogue (z, r, d, 3x3 inverse read, d, z written: 112 B) in
-  every step after the first, the first tet phase's extra p and r gathers
-  (32 B), the p / Kp epilogue (64 B) and the y / r update (192 B)."""
-  return degree * (140 * nt + 24 * nv) + (degree - 1) * 112 * nv + (32 + 64 + 192) * nv
+  applications of K, each a tet phase (constraint indices 16 B and
+  gradients 48 B, compact length constraints 8 + 16 B; alpha 4 B, s written
+  4 B, the vertex vector gathered once per vertex 16 B) and a vertex phase
+  (vertex-major gradients 16 B per incidence entry, offsets and weights 8 B
+  per vertex, s gathered once per constraint); per vertex the Chebyshev
+  epilogue (z, r, d, 3x3 inverse read, d, z written: 112 B) in every step
+  after the first, the first tet phase's extra p and r gathers (32 B), the
+  p / Kp epilogue (64 B) and the y / r update (192 B)."""
+  ne = 4 * nt if ne is None else ne
+  per_apply = 72 * (nt - n2) + 32 * n2 + 16 * ne + 4 * nt + 24 * nv
+  return degree * per_apply + (degree - 1) * 112 * nv + (32 + 64 + 192) * nv
+
+
+def operator_shape(s):
+  """(incidence entries, length constraints) of a solver's operator: a
+  length constraint contributes 2 incidence entries instead of 4."""
+  n2 = 0 if s.constraint_types is None else int((s.constraint_types == 1).sum())
+  return 4 * (s.n_tets - n2) + 2 * n2, n2
 
 
 # DRAM bytes (read + write) of one launch of each persistent kernel on the
@@ -280,7 +294,8 @@ TRAFFIC_40 = {'arap': {'k_pcg': 44874752, 'k_jcg': 46275840},
               'edge_volume': {'k_pcg': 21536038400, 'k_jcg': 71564010240}}
 
 
-def roofline_from_steps(st, nt, nv, degree, hbm_peak, peak_kind, size=40, constraints='arap'):
+def roofline_from_steps(st, nt, nv, degree, hbm_peak, peak_kind, size=40, constraints='arap',
+                        shape=(None, 0)):
   """Roofline of the two persistent kernels over the timed steps, from the
   CUDA events the library records around each launch on its stream (stats
   ms_warm / ms_dual) and the iterations each ran.  The one with more GPU
@@ -294,12 +309,16 @@ def roofline_from_steps(st, nt, nv, degree, hbm_peak, peak_kind, size=40, constr
   n_w = sum(x['newton_iters'] for x in st) if it_w else 0
   n_d = launches - n_w
   path = st[-1]['cg_path']
+  ne, n2 = shape
+  # staged kernels read every constraint's four slots in the tet phase; the
+  # unstaged ones take the length constraints in compact form
+  n2 = 0 if path.endswith('staged') else n2
   out = []
   for name, ms, its, n, per_it in (
       (f'k_pcg<{int(path.endswith("staged"))}> (primal warm start, persistent Chebyshev-{degree} '
-       'CG on K)', ms_w, it_w, n_w, primal_iteration_bytes(nt, nv, degree)),
+       'CG on K)', ms_w, it_w, n_w, primal_iteration_bytes(nt, nv, degree, ne, n2)),
       (f'k_jcg<{int(path.endswith("staged"))}> (dual persistent Chebyshev-{degree} CG on A)',
-       ms_d, it_d, n_d, cg_iteration_bytes(nt, nv, degree))):
+       ms_d, it_d, n_d, cg_iteration_bytes(nt, nv, degree, ne, n2))):
     if n <= 0 or ms <= 0:
       continue
     dt = ms / 1e3 / n
@@ -580,7 +599,7 @@ def run_ours(args):
          'h2d_bytes_per_step': 2 * x.numel() * 4, 'd2h_bytes_per_step': 2 * x.numel() * 4}
 
   roof = roofline_from_steps(st, s.n_tets, s.n_verts, FAST_KW['cheb_degree'], hbm, kind,
-                             args.size, cons)
+                             args.size, cons, operator_shape(s))
   roof['matrix_free_apply'] = roofline_matrix_free(torch, s, hbm, kind)
   st0 = st[-1]
   n_verts, n_cons = s.n_verts, s.n_tets
@@ -627,7 +646,7 @@ def run_ours(args):
             'cg_iters_per_step': sum(x['cg_iters_total'] for x in sta) / k,
             'nnz_level0': sta[-1]['nnz'][0],
             'roofline': roofline_from_steps(sta, sa.n_tets, sa.n_verts, FAST_KW['cheb_degree'],
-                                            hbm, kind, args.size, 'arap')}
+                                            hbm, kind, args.size, 'arap', operator_shape(sa))}
     del sa
     torch.cuda.empty_cache()
     if not args.no_plain:

@@ -110,10 +110,21 @@ __device__ __forceinline__ float tdot(const TArgs& a, int64_t t, int4 q) {
          (g1.z * u2.x + g1.w * u2.y + g2.x * u2.z) + (g2.y * u3.x + g2.z * u3.y + g2.w * u3.z);
 }
 
+// A t of constraint t: staged blocks use their shared copy of the indices;
+// unstaged, length constraints (t >= n4) take the compact two-vertex path
+template <bool STAGED>
+__device__ __forceinline__ float tdot_any(const PArgs& a, const Own& o, int64_t t);
+
 template <bool STAGED>
 __device__ __forceinline__ int4 tet_q(const PArgs& a, const Own& o, int64_t t) {
   if (STAGED) return o.q[t - o.tb0];
   return a.ta.t_i[t];
+}
+
+template <bool STAGED>
+__device__ __forceinline__ float tdot_any(const PArgs& a, const Own& o, int64_t t) {
+  if (!STAGED && t >= a.ta.n4) return jt_edge(a.ta, t);
+  return tdot(a.ta, t, tet_q<STAGED>(a, o, t));
 }
 
 // Warm start, vertex phase in float64: u_v = w_v sum x_t g_{t,l} summed in
@@ -293,7 +304,7 @@ __device__ __forceinline__ void tphase_cheb(const PArgs& a, const Own& o, float 
 #pragma unroll
     for (int i = 0; i < kTB; ++i) {
       const int64_t t = tb + i * o.tstep;
-      y[i] = t < o.tend ? tdot(a.ta, t, tet_q<STAGED>(a, o, t)) : 0.0f;
+      y[i] = t < o.tend ? tdot_any<STAGED>(a, o, t) : 0.0f;
     }
 #pragma unroll
     for (int i = 0; i < kTB; ++i) {
@@ -323,7 +334,7 @@ __device__ __forceinline__ void tphase_ap(const PArgs& a, const Own& o, float bf
 #pragma unroll
     for (int i = 0; i < kTB; ++i) {
       const int64_t t = tb + i * o.tstep;
-      y[i] = t < o.tend ? tdot(a.ta, t, tet_q<STAGED>(a, o, t)) : 0.0f;
+      y[i] = t < o.tend ? tdot_any<STAGED>(a, o, t) : 0.0f;
     }
 #pragma unroll
     for (int i = 0; i < kTB; ++i) {
@@ -611,7 +622,7 @@ int64_t staged_smem_bytes(int32_t emax, int32_t tmax, int32_t vmax) {
 
 }  // namespace
 
-JcgPlan jcg_plan(const std::vector<int32_t>& inc_ptr, int32_t nv, int32_t nt) {
+JcgPlan jcg_plan(const std::vector<int32_t>& inc_ptr, int32_t nv, int32_t nt, bool allow_staged) {
   require(static_cast<int64_t>(inc_ptr.size()) == static_cast<int64_t>(nv) + 1, MGPBD_EINVAL,
           "incidence offsets must hold nv + 1 entries");
   int dev = 0, coop = 0, sms = 0, optin = 0;
@@ -621,7 +632,7 @@ JcgPlan jcg_plan(const std::vector<int32_t>& inc_ptr, int32_t nv, int32_t nt) {
   MGPBD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   MGPBD_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   const int64_t ne = inc_ptr[nv];
-  {
+  if (allow_staged) {
     JcgPlan p;
     const int G = sms;
     p.vb.resize(G + 1);
@@ -689,6 +700,10 @@ void launch_jcg_persistent(const JView& j, const JcgVecs& v, const JcgPlan& plan
   a.ta.alpha = j.alpha;
   a.ta.dinv = j.dinv;
   a.ta.nt = j.nt;
+  a.ta.n4 = j.n4;
+  a.ta.gE = j.gE;
+  a.ta.qE = j.qE;
+  require(j.n4 >= j.nt || (j.gE && j.qE), MGPBD_ESTATE, "compact length constraints not prepared");
   a.nv = j.nv;
   a.inc_ptr = j.inc_ptr;
   a.gV = j.gV;

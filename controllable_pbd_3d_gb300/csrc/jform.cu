@@ -25,7 +25,7 @@ __global__ void k_jprep(const int32_t* __restrict__ inc_ent, int64_t ne,
                         const float* __restrict__ gradC, const int4* __restrict__ t_i,
                         const float* __restrict__ invm, const float* __restrict__ alpha,
                         int32_t nt, float4* __restrict__ gV, float* __restrict__ dinv,
-                        float4* __restrict__ gT) {
+                        float4* __restrict__ gT, int32_t n4, float4* __restrict__ gE) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < ne; k += stride) {
     const int32_t e = inc_ent[k];
@@ -48,6 +48,7 @@ __global__ void k_jprep(const int32_t* __restrict__ inc_ent, int64_t ne,
       gT[nt + t] = g4[1];
       gT[2LL * nt + t] = g4[2];
     }
+    if (gE && t >= n4) gE[t - n4] = make_float4(g[0], g[1], g[2], 0.0f);
   }
 }
 
@@ -417,6 +418,10 @@ TArgs targs(const JView& j) {
   a.alpha = j.alpha;
   a.dinv = j.dinv;
   a.nt = j.nt;
+  // the per-phase kernels read every constraint's four slots
+  a.n4 = j.nt;
+  a.gE = nullptr;
+  a.qE = nullptr;
   return a;
 }
 
@@ -426,7 +431,7 @@ void launch_jform_prepare(const JView& j, const int32_t* inc_ent, float4* gV, fl
                           float4* gT, cudaStream_t s) {
   int g = tgrid(std::max<int64_t>(j.ne, j.nt));
   k_jprep<<<g, kT, 0, s>>>(inc_ent, j.ne, j.gradC, reinterpret_cast<const int4*>(j.t_i), j.invm,
-                           j.alpha, j.nt, gV, dinv, gT);
+                           j.alpha, j.nt, gV, dinv, gT, j.n4, j.gE);
   MGPBD_CHECK_LAUNCH();
 }
 

@@ -56,6 +56,12 @@ struct JView {
   const float* alpha = nullptr;      // (nt)
   const float* dinv = nullptr;       // (nt) 1 / diag(A)
   float4* u = nullptr;               // (nv) vertex scratch
+  // compact length constraints (the persistent kernels' unstaged tet
+  // phases): constraints n4 .. nt-1 are length constraints whose gradient n
+  // is gE[t - n4] and vertices qE[t - n4]; n4 = nt when there are none
+  int32_t n4 = 0;
+  float4* gE = nullptr;
+  const int2* qE = nullptr;
 };
 
 // gV[k] = (gradC[inc_ent[k]], tet id) and 1/diag(A) per tet; with gT, also
@@ -132,7 +138,10 @@ struct JcgPlan {
   int32_t vmax = 0, tmax = 0, emax = 0;
   std::vector<int32_t> vb, tb;  // grid + 1 boundaries each (staged)
 };
-JcgPlan jcg_plan(const std::vector<int32_t>& inc_ptr, int32_t nv, int32_t nt);
+// allow_staged = false: the unstaged plan (operator read from L2) even when
+// the staged one would fit
+JcgPlan jcg_plan(const std::vector<int32_t>& inc_ptr, int32_t nv, int32_t nt,
+                 bool allow_staged = true);
 // The whole CG solve (init, iterations to the tolerance or maxiter, the
 // Chebyshev preconditioner of `degree`) as one cooperative kernel; st is
 // zeroed and then filled like the per-phase path fills it.  part_dev holds

@@ -89,7 +89,21 @@ struct TArgs {
   const float* alpha;
   const float* dinv;
   int32_t nt;
+  // constraints n4 .. nt-1 are length constraints (slots a, b, a, b): their
+  // gradient n (slot 0, slot 1 is -n) in gE and (a, b) in qE, from index 0
+  int32_t n4;
+  const float4* gE;
+  const int2* qE;
 };
+
+// g . (u_a - u_b) of length constraint t >= a.n4 (two vertices, one gradient)
+__device__ __forceinline__ float jt_edge(const TArgs& a, int64_t t) {
+  const int64_t e = t - a.n4;
+  const int2 q = __ldg(a.qE + e);
+  const float4 g = __ldg(a.gE + e);
+  const float4 ua = a.u[q.x], ub = a.u[q.y];
+  return (g.x * ua.x + g.y * ua.y + g.z * ua.z) - (g.x * ub.x + g.y * ub.y + g.z * ub.z);
+}
 
 // sum_l g_{t,l} . u_{v_l}
 __device__ __forceinline__ float jt_core(const TArgs& a, int64_t t) {

@@ -53,6 +53,9 @@ constexpr int kBoot = 24; // block-Jacobi PCG iterations that estimate lambda_ma
 
 struct QArgs {
   int32_t nt, nv;
+  int32_t n4;          // length constraints from here on (compact in gE, qE)
+  const float4* gE;    // their gradient n (slot 1 is -n)
+  const int2* qE;      // their two vertices
   const int4* t_i;
   const float4* gradC;  // the 12 gradient entries as three planes of nt float4
   const float* alpha;   // alpha~
@@ -142,7 +145,21 @@ __device__ __forceinline__ void tphase(const QArgs& a, const Own& o, float beta,
       const int64_t t = tb + i * o.tstep;
       y[i] = 0.0f;
       e[i] = 0.0f;
-      if (t < o.tend) {
+      if (!STAGED && t < o.tend && t >= a.n4) {
+        // length constraint: two vertices, gradients n and -n
+        const int2 qe = __ldg(a.qE + (t - a.n4));
+        const float3 n = f3(__ldg(a.gE + (t - a.n4)));
+        float3 v0 = f3(V[qe.x]), v1 = f3(V[qe.y]);
+        if (MODE == kT1) {
+          const float3 p0 = f3(a.p[qe.x]), p1 = f3(a.p[qe.y]);
+          v0 = make_float3(v0.x + beta * p0.x, v0.y + beta * p0.y, v0.z + beta * p0.z);
+          v1 = make_float3(v1.x + beta * p1.x, v1.y + beta * p1.y, v1.z + beta * p1.z);
+          const float4 r0 = a.r[qe.x], r1 = a.r[qe.y];
+          e[i] = dot3(n, make_float3(r0.w * r0.x, r0.w * r0.y, r0.w * r0.z)) -
+                 dot3(n, make_float3(r1.w * r1.x, r1.w * r1.y, r1.w * r1.z));
+        }
+        y[i] = dot3(n, v0) - dot3(n, v1);
+      } else if (t < o.tend) {
         const int4 q = tet_q<STAGED>(a, o, t);
         const float4 g0 = __ldg(a.gradC + t), g1 = __ldg(a.gradC + a.nt + t),
                      g2 = __ldg(a.gradC + 2LL * a.nt + t);
@@ -803,6 +820,10 @@ void launch_pcg_primal(const JView& j, const PcgVecs& v, const JcgPlan& plan,
   QArgs a;
   a.nt = j.nt;
   a.nv = j.nv;
+  a.n4 = j.n4;
+  a.gE = j.gE;
+  a.qE = j.qE;
+  require(j.n4 >= j.nt || (j.gE && j.qE), MGPBD_ESTATE, "compact length constraints not prepared");
   a.t_i = reinterpret_cast<const int4*>(j.t_i);
   require(j.gT != nullptr, MGPBD_ESTATE, "persistent CG needs the gradient planes");
   a.gradC = j.gT;

@@ -108,6 +108,7 @@ Solver::Solver(const mgpbd_params& p) : p_(p) {
   require(p.n_smooth >= 0 && p.maxiter >= 0 && p.maxiter_cg >= 0, MGPBD_EINVAL,
           "iteration counts must be non-negative");
   require(p.mode == MGPBD_MODE_PARITY || p.mode == MGPBD_MODE_FAST, MGPBD_EINVAL, "unknown mode");
+  require(p.persistent >= 0 && p.persistent <= 2, MGPBD_EINVAL, "persistent must be 0, 1 or 2");
   require(p.precond == MGPBD_PRECOND_VCYCLE || p.precond == MGPBD_PRECOND_CHEB ||
               p.precond == MGPBD_PRECOND_LEARNED,
           MGPBD_EINVAL, "unknown preconditioner");
@@ -310,8 +311,27 @@ void Solver::init() {
   upload(inc_ptr_, ip, s);
   upload(inc_ent_, ie, s);
   inc_n_ = static_cast<int64_t>(ie.size());
+  // trailing length constraints in compact form (gradient n, two vertices)
+  // for the unstaged tet phases of the persistent kernels
+  n4_ = nt_;
+  gE_.release();
+  qE_.release();
+  if (cheb() && p_.persistent && !ctype_host_.empty()) {
+    int32_t n4 = nt_;
+    while (n4 > 0 && ctype_host_[n4 - 1] == MGPBD_CONS_LENGTH) --n4;
+    if (n4 < nt_) {
+      std::vector<int32_t> qe(2LL * (nt_ - n4));
+      for (int32_t c = n4; c < nt_; ++c) {
+        qe[2LL * (c - n4)] = t_host[4LL * c];
+        qe[2LL * (c - n4) + 1] = t_host[4LL * c + 1];
+      }
+      upload(qE_, qe, s);
+      gE_.alloc(nt_ - n4);
+      n4_ = n4;
+    }
+  }
   if (cheb() && p_.persistent) {
-    jplan_ = jcg_plan(ip, nv_, nt_);
+    jplan_ = jcg_plan(ip, nv_, nt_, p_.persistent != 2);
     if (primal()) {
       pplan_ = jplan_;
       if (!pplan_.staged || !pcg_plan_fits(pplan_)) {
@@ -587,6 +607,9 @@ JView Solver::jview() {
   j.alpha = alpha_.p;
   j.dinv = jdinv_.p;
   j.u = u_.p;
+  j.n4 = n4_;
+  j.gE = gE_.p;
+  j.qE = reinterpret_cast<const int2*>(qE_.p);
   return j;
 }
 

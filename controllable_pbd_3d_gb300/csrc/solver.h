@@ -155,6 +155,9 @@ class Solver {
   DevBuf<float> dm_inv_, rest_vol_, alpha_, lambda_, C_, gradC_, rhs_, dlam_;
   DevBuf<int32_t> inc_ptr_, inc_ent_;
   int64_t inc_n_ = 0;                  // incidence entries
+  int32_t n4_ = 0;                     // first trailing length constraint (nt_: none)
+  DevBuf<float4> gE_;                  // their gradients n
+  DevBuf<int32_t> qE_;                 // their vertex pairs
   DevBuf<int32_t> ctype_;              // constraint types (absent: all ARAP)
   std::vector<int32_t> ctype_host_;
   std::vector<Level> levels_;

@@ -100,7 +100,9 @@ class MGPBDSolverGPU:
                    compliance / dt^2; n_tets then counts constraints, the
                    mesh's tets are in mesh_t_i / n_mesh_tets);
     persistent     FAST + 'cheb': each CG solve is one cooperative persistent
-                   kernel (False: one kernel per phase, per use_graph);
+                   kernel (False: one kernel per phase, per use_graph; 2: the
+                   persistent kernel reading the operator from L2 instead of
+                   staging it in shared memory);
     primal         FAST + 'cheb' + persistent: warm-start each solve through
                    the vertex-space system K y = J^T alpha~^-1 b (Woodbury)
                    to a dual residual of primal_tol |b|, then CG on A;
@@ -200,7 +202,7 @@ class MGPBDSolverGPU:
     p.cheb_degree = int(cheb_degree)
     p.cheb_lo = float(cheb_lo)
     p.use_graph = int(bool(use_graph))
-    p.persistent = int(bool(persistent))
+    p.persistent = int(persistent)  # True / 1, 2 (unstaged) or False / 0
     p.primal = int(bool(primal))
     p.primal_tol = float(primal_tol)
     p.learned_accept = float(learned_accept)

@@ -116,8 +116,10 @@ typedef struct mgpbd_params {
   int32_t use_graph;
   /* FAST mode with MGPBD_PRECOND_CHEB: 1 (default) runs each CG solve as ONE
    * cooperative persistent kernel (grid barriers between its phases, float32
-   * vectors, compensated solution sum); 0 runs the per-phase kernels
-   * (use_graph selects graph or host loop for those). */
+   * vectors, compensated solution sum); 2 the same without staging the
+   * operator in shared memory (read from L2, as for meshes too large to
+   * stage); 0 runs the per-phase kernels (use_graph selects graph or host
+   * loop for those). */
   int32_t persistent;
   /* FAST mode, MGPBD_PRECOND_CHEB, persistent: 1 warm-starts each solve
    * through the primal system K y = J^T alpha~^-1 b with K = W^-1 +

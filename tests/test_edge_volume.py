@@ -149,16 +149,26 @@ def test_gpu_stages_match_oracle(cuda):
   assert np.abs(A - Ao).max() <= 1e-4 * np.abs(Ao).max()
 
 
+VARIANTS = {
+    'vcycle': dict(smoother='safe'),
+    'fast-primal': dict(mode='fast', precond='cheb', cheb_lo=1e-3, primal=True, primal_tol=1e-2),
+    # the persistent kernels reading the operator from L2, with the length
+    # constraints in compact two-vertex form (the path of large meshes)
+    'fast-primal-l2': dict(mode='fast', precond='cheb', cheb_lo=1e-3, primal=True,
+                           primal_tol=1e-2, persistent=2),
+    'fast-dual-l2': dict(mode='fast', precond='cheb', cheb_lo=1e-3, primal=False, persistent=2),
+}
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize('variant', ['vcycle', 'fast-primal'])
+@pytest.mark.parametrize('variant', list(VARIANTS))
 def test_gpu_substeps_match_float64_oracle(cuda, variant):
   torch = cuda
   xr, x0, t, invm = body(6)
   kw = dict(damp=0.993, maxiter=5, rtol=1e-6, atol=1e-9, maxiter_cg=4000, tol_cg=1e-12,
             rel_tol_cg=1e-7)
   o = oracle(xr, x0, t, invm, dtype=np.float64, smoother='safe', **kw)
-  extra = dict(smoother='safe') if variant == 'vcycle' else dict(
-      mode='fast', precond='cheb', cheb_lo=1e-3, primal=True, primal_tol=1e-2)
+  extra = VARIANTS[variant]
   s, x = gpu_solver(torch, xr, x0, t, invm, **kw, **extra)
   for k in range(2):
     o.step(k)
@@ -166,6 +176,8 @@ def test_gpu_substeps_match_float64_oracle(cuda, variant):
   err = float(np.abs(x.cpu().numpy() - o.x).max())
   assert err <= 1e-5 * float(np.abs(o.x).max()), err
   assert s.stats()['newton_iters'] >= 1
+  if variant.endswith('-l2'):
+    assert s.stats()['cg_path'] in ('persistent', 'primal')  # unstaged
 
 
 @pytest.mark.gpu

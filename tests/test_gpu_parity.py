@@ -184,7 +184,8 @@ def test_matrix_free_apply_equals_csr(cuda, name):
 # the FAST-mode Chebyshev solve paths: one kernel per phase, the persistent
 # kernel on the dual system, the persistent kernel on the primal system
 CHEB_PATHS = {'kernels': dict(persistent=False), 'dual': dict(persistent=True, primal=False),
-              'primal': dict(persistent=True, primal=True)}
+              'primal': dict(persistent=True, primal=True),
+              'dual-l2': dict(persistent=2, primal=False), 'primal-l2': dict(persistent=2, primal=True)}
 
 
 @pytest.mark.parametrize('path', list(CHEB_PATHS))
