@@ -291,7 +291,7 @@ def operator_shape(s):
 # --size 40 --constraints arap|edge_volume` (dram__bytes_read.sum +
 # dram__bytes_write.sum)
 TRAFFIC_40 = {'arap': {'k_pcg': 44874752, 'k_jcg': 46275840},
-              'edge_volume': {'k_pcg': 21536038400, 'k_jcg': 71564010240}}
+              'edge_volume': {'k_pcg': 5098314240, 'k_jcg': 33447385856}}
 
 
 def roofline_from_steps(st, nt, nv, degree, hbm_peak, peak_kind, size=40, constraints='arap',
