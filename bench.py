@@ -151,9 +151,17 @@ def max_over_ranks(ws, v):
     return v
   import torch
   import torch.distributed as dist
-  t = torch.tensor([v], dtype=torch.float64, device='cuda')
+  dev = 'cuda' if dist.get_backend() == 'nccl' else 'cpu'
+  t = torch.tensor([v], dtype=torch.float64, device=dev)
   dist.all_reduce(t, op=dist.ReduceOp.MAX)
   return float(t.item())
+
+
+def replica_value(ws, steps, t_max):
+  """Whole-job substeps/s of ws independent replicas that each ran
+  `steps` substeps: all replicas' substeps over the slowest replica's time
+  t_max (weak scaling)."""
+  return ws * steps / t_max
 
 
 CONSTRAINT_NAMES = {'edge_volume': 'one length constraint per tet edge + one volume '
@@ -577,7 +585,7 @@ def run_ours(args):
   t_max = max_over_ranks(ws, t)
   newton = sum(x['newton_iters'] for x in st)
   cg = sum(x['cg_iters_total'] for x in st)
-  value = ws * args.steps / t_max
+  value = replica_value(ws, args.steps, t_max)
 
   # end to end through the public API with host buffers
   xh = torch.empty_like(x, device='cpu').pin_memory()
