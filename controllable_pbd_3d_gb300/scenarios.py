@@ -1,0 +1,60 @@
+"""Seeded scenarios of the benchmark configuration (input generation and
+host-side drivers only; the step itself runs in libmgpbd.so).
+
+`drag_slab` is the stiff-drag case: an nx x ny x nz hex slab (5 tets per
+hex), one long edge pinned, the opposite corner vertex dragged along +z.
+Dragging follows the reference's mechanism (`experiments/exp_tool_tissue.py`,
+`experiments/exp_adaptive.py`): the dragged vertex is a pinned vertex
+(inverse mass 0, kinematic) whose position the host overwrites before each
+frame, and the solve pulls the body after it.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import meshgen
+
+
+def grid_edge_vertices(nx, ny, nz, j=0, k=0):
+  """Vertex ids of the grid line along x at (y index j, z index k)."""
+  i = np.arange(nx + 1)
+  return (i + (nx + 1) * (j + (ny + 1) * k)).astype(np.int64)
+
+
+def drag_slab(nx=100, ny=25, nz=100, h=None, jitter=0.0, seed=0):
+  """The slab, its pinned long edge (y = 0, z = 0, along x) and the dragged
+  corner (x, y, z max).  Returns dict(x_ref, x0, t_i, invm, pinned, drag)."""
+  xr, t = meshgen.hex_grid_tets(nx, ny, nz, h=h)
+  x0, _ = meshgen.hex_grid_tets(nx, ny, nz, h=h, jitter=jitter, seed=seed) if jitter else (xr, t)
+  pinned = grid_edge_vertices(nx, ny, nz, 0, 0)
+  drag = int(nx + (nx + 1) * (ny + (ny + 1) * nz))
+  invm = np.ones(len(xr), np.float32)
+  invm[pinned] = 0.0
+  invm[drag] = 0.0
+  return dict(x_ref=xr.astype(np.float32), x0=x0.astype(np.float32), t_i=t.astype(np.int32),
+              invm=invm, pinned=pinned, drag=drag)
+
+
+class DragDriver:
+  """Moves the dragged vertex of `solver` (an MGPBDSolverGPU with
+  kinematic_pins=True) by `distance` along `direction` over `frames`
+  frames, linearly, before each frame's substeps."""
+
+  def __init__(self, solver, vertex, distance=0.5, frames=60, direction=(0.0, 0.0, 1.0)):
+    self.solver = solver
+    self.vertex = int(vertex)
+    self.start = solver.v_p[self.vertex].detach().clone()
+    d = torch.tensor(direction, dtype=torch.float32, device=solver.v_p.device)
+    self.step_vec = d / torch.linalg.norm(d) * (float(distance) / int(frames))
+    self.frames = int(frames)
+
+  def target(self, frame):
+    return self.start + self.step_vec * min(int(frame) + 1, self.frames)
+
+  def frame(self, frame, substeps=5):
+    with torch.no_grad():
+      self.solver.v_p[self.vertex] = self.target(frame)
+    for _ in range(substeps):
+      self.solver.step(frame)
