@@ -352,8 +352,15 @@ def roofline_from_steps(st, nt, nv, degree, hbm_peak, peak_kind, size=40, constr
     roof['traffic_source'] = ('ncu dram__bytes_read.sum + dram__bytes_write.sum of one '
                               'launch of bench.py --profile-solve --size 40 --constraints '
                               f'{constraints} (same workload)')
-  roof['working_set_note'] = ('operator data staged in shared memory / resident in L2 across '
-                              'each solve: the rate is on-chip, not HBM')
+  if path.endswith('staged'):
+    roof['working_set_note'] = ('operator data staged in shared memory / resident in L2 across '
+                                'each solve: the rate is on-chip, not HBM')
+  else:
+    roof['working_set_note'] = ('operator read from L2 / HBM each application (too large to '
+                                'stage in shared memory); part of it stays in the 129 MB L2')
+  if roof['traffic'] is not None:
+    roof['traffic_over_algorithmic'] = round(roof['traffic'] /
+                                             max(roof['algorithmic_bytes_per_launch'], 1), 4)
   if len(out) > 1:
     roof['other'] = out[1]
   return roof
