@@ -745,6 +745,94 @@ def run_profile_net(args):
                     'weights_mean': float(w.mean()), 'reps': args.profile_reps}))
 
 
+SLAB_DIMS = (100, 25, 100)  # the 100 x 100 x 25 slab, y (25) the thin axis
+SLAB_COMPLIANCE = 1e-10
+SLAB_DRAG = dict(distance=0.5, frames=60)
+SUBSTEPS_PER_FRAME = 5
+
+
+def run_slab(args):
+  """The stiff-drag slab: 100 x 100 x 25 hexes (265,226 vertices, 1.25 M
+  tets, 5 per hex) with one length constraint per tet edge and one volume
+  constraint per tet, compliance 1e-10, one long edge pinned and the
+  opposite corner dragged 0.5 along +z over 60 frames as a kinematic
+  vertex (moved before each frame of 5 substeps).  The fast step only (the
+  plain AMG-PCG is hours at this size); one JSON line with the same
+  metric."""
+  import torch
+  from controllable_pbd_3d_gb300 import _native as N
+  from controllable_pbd_3d_gb300.mgpbd_gpu import MGPBDSolverGPU
+  from controllable_pbd_3d_gb300.scenarios import DragDriver, drag_slab
+  torch.cuda.set_device(0)
+  hbm, kind = peaks()
+  t_setup = time.perf_counter()
+  sl = drag_slab(*SLAB_DIMS)
+  x = torch.tensor(sl['x0'], device='cuda')
+  s = MGPBDSolverGPU(x, torch.tensor(sl['x_ref'], device='cuda'),
+                     torch.tensor(sl['invm'], device='cuda'),
+                     torch.tensor(sl['t_i'], device='cuda'), None, [0.0, -9.8, 0.0], DT,
+                     compliance=SLAB_COMPLIANCE, constraints='edge_volume', **fast_kw(args))
+  s.init()
+  t_setup = time.perf_counter() - t_setup
+  drv = DragDriver(s, sl['drag'], **SLAB_DRAG)
+
+  def substep(i):
+    if i % SUBSTEPS_PER_FRAME == 0:
+      with torch.no_grad():
+        s.v_p[drv.vertex] = drv.target(i // SUBSTEPS_PER_FRAME)
+    s.step(i // SUBSTEPS_PER_FRAME)
+
+  for i in range(args.warmup):
+    substep(i)
+  torch.cuda.synchronize()
+  L = N.lib()
+  c0 = L.mgpbd_launch_count()
+  flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device='cuda')
+  stream = torch.cuda.current_stream()
+  e0 = torch.cuda.Event(enable_timing=True)
+  e1 = torch.cuda.Event(enable_timing=True)
+  st = []
+  with ClockSampler(0) as clk:
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for i in range(args.warmup, args.warmup + args.steps):
+      substep(i)
+      st.append(s.stats())
+      flush.fill_(i)
+    e1.record(stream)
+    torch.cuda.synchronize()
+  t = e0.elapsed_time(e1) / 1e3
+  launches = L.mgpbd_launch_count() - c0
+  xs = x.cpu().numpy()
+  target = drv.target((args.warmup + args.steps - 1) // SUBSTEPS_PER_FRAME).cpu().numpy()
+  roof = roofline_from_steps(st, s.n_tets, s.n_verts, FAST_KW['cheb_degree'], hbm, kind,
+                             0, 'edge_volume', operator_shape(s))
+  out = {
+      'metric': METRIC, 'value': round(args.steps / t, 4), 'unit': UNIT, 'n_gpus': 1,
+      'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(t * 1e3 / args.steps, 1),
+      'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+      'data': 'synthetic (hex-grid slab)',
+      'config': {'workload': '100x100x25 hex slab, 5 tets/hex, one long edge pinned, the '
+                             'opposite corner dragged 0.5 along +z over 60 frames '
+                             f'({SUBSTEPS_PER_FRAME} substeps per frame)',
+                 'n_verts': s.n_verts, 'n_tets': s.n_mesh_tets,
+                 'constraints': CONSTRAINT_NAMES['edge_volume'], 'n_constraints': s.n_tets,
+                 'nnz_level0': st[-1]['nnz'][0], 'levels': st[-1]['rows'],
+                 'compliance': SLAB_COMPLIANCE, 'dt': DT, 'rel_res_cg': 1e-6, 'mode': 'fast',
+                 'solver': 'primal warm start + dual persistent Chebyshev-8 CG',
+                 'l2': 'flushed between timed substeps (256 MB write, inside the timed region)',
+                 'setup_s': round(t_setup, 1)},
+      'newton_iters_per_step': sum(r['newton_iters'] for r in st) / args.steps,
+      'cg_iters_per_step': sum(r['cg_iters_total'] for r in st) / args.steps,
+      'max_cg_iters_last_solve': max(r['cg_iters_last'] for r in st),
+      'maxiter_cg': SOLVER_KW['maxiter_cg'],
+      'gpu_launches': int(launches), 'clocks': clk.summary(), 'roofline': roof,
+      'drag_vertex_error': float(np.abs(xs[sl['drag']] - target).max()),
+      'pinned_edge_moved': bool(not np.array_equal(xs[sl['pinned']], sl['x0'][sl['pinned']])),
+      'finite': bool(np.isfinite(xs).all()), 'status': st[-1]['status']}
+  print(json.dumps(out), flush=True)
+
+
 def run_reference(args):
   """The reference algorithm on the host cores: the OpenMP CPU port of the
   plain step (the reference itself needs Taichi, which is not available).
@@ -809,9 +897,13 @@ def main():
   # the coarse network's weights pass alone (for ncu)
   ap.add_argument('--profile-net', action='store_true')
   ap.add_argument('--profile-reps', type=int, default=5)
+  # the 40^3 cube (headline) or the stiff-drag slab (one line, fast step only)
+  ap.add_argument('--workload', default='cube', choices=['cube', 'slab'])
   args = ap.parse_args()
   if args.profile_net:
     run_profile_net(args)
+  elif args.workload == 'slab' and args.impl == 'ours':
+    run_slab(args)
   elif args.profile_solve:
     run_profile_solve(args)
   elif args.impl == 'reference':
