@@ -44,9 +44,12 @@ namespace {
 using namespace jdev;
 using namespace pdev;
 
-// One block of kPT threads per SM: up to 112 registers a thread, so each
-// thread can issue the gathers of several tets (vertices) before it uses
-// them, and 152 arrivals per grid barrier.
+// Staged: one block of kPT threads per SM, up to 112 registers a thread,
+// so each thread can issue the gathers of several tets (vertices) before
+// it uses them, and 152 arrivals per grid barrier.  Unstaged: two blocks
+// per SM (56 registers a thread): the phases wait on L2 gathers, and twice
+// the resident warps hide more of that latency than the extra registers
+// would.
 constexpr int kPT = 576;
 constexpr int kTB = 4;   // tets a thread handles per round of a tet phase
 constexpr int kVS = 4;   // lanes per vertex in the staged vertex phase
@@ -352,7 +355,7 @@ __device__ __forceinline__ void tphase_ap(const PArgs& a, const Own& o, float bf
 }
 
 template <bool STAGED>
-__global__ void __launch_bounds__(kPT, 1) k_jcg(PArgs a) {
+__global__ void __launch_bounds__(kPT, STAGED ? 1 : 2) k_jcg(PArgs a) {
   extern __shared__ __align__(16) unsigned char s_dyn[];
   __shared__ float s_c1[kMaxCheb], s_c2[kMaxCheb];
   __shared__ float s_scal;  // alpha or beta, broadcast from thread 0
