@@ -294,12 +294,20 @@ def operator_shape(s):
   return 4 * (s.n_tets - n2) + 2 * n2, n2
 
 
-# DRAM bytes (read + write) of one launch of each persistent kernel on the
-# 40^3 workload, from one ncu capture each of `bench.py --profile-solve
-# --size 40 --constraints arap|edge_volume` (dram__bytes_read.sum +
-# dram__bytes_write.sum)
+# DRAM bytes (read + write: dram__bytes_read.sum + dram__bytes_write.sum) of
+# one launch of each persistent kernel on the 40^3 workload, from one ncu
+# capture each.  Length + volume: the timed substep's two launches of
+# `bench.py --no-cpu-baseline --no-plain --no-learned --no-arap --steps 1
+# --warmup 3` (-k regex:"k_pcg|k_jcg" -s 10 -c 2; 56 primal and 714 dual CG
+# iterations).  ARAP: `bench.py --profile-solve --size 40 --constraints arap`.
 TRAFFIC_40 = {'arap': {'k_pcg': 44874752, 'k_jcg': 46275840},
-              'edge_volume': {'k_pcg': 5098314240, 'k_jcg': 33447385856}}
+              'edge_volume': {'k_pcg': 729190400, 'k_jcg': 81323029760}}
+TRAFFIC_SOURCE = {
+    'arap': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of bench.py '
+            '--profile-solve --size 40 --constraints arap (same workload)',
+    'edge_volume': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of the timed substep\'s '
+                   'launches of bench.py --no-cpu-baseline --no-plain --no-learned --no-arap '
+                   '--steps 1 --warmup 3 (56 primal, 714 dual CG iterations)'}
 
 
 def roofline_from_steps(st, nt, nv, degree, hbm_peak, peak_kind, size=40, constraints='arap',
@@ -349,9 +357,7 @@ def roofline_from_steps(st, nt, nv, degree, hbm_peak, peak_kind, size=40, constr
   roof = dict(out[0])
   roof['cg_path'] = path
   if roof['traffic'] is not None:
-    roof['traffic_source'] = ('ncu dram__bytes_read.sum + dram__bytes_write.sum of one '
-                              'launch of bench.py --profile-solve --size 40 --constraints '
-                              f'{constraints} (same workload)')
+    roof['traffic_source'] = TRAFFIC_SOURCE[constraints]
   if path.endswith('staged'):
     roof['working_set_note'] = ('operator data staged in shared memory / resident in L2 across '
                                 'each solve: the rate is on-chip, not HBM')
