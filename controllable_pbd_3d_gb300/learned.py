@@ -213,3 +213,51 @@ class CoarseNet:
       out.append(self.loss_grad(g, s[idx]))
       self.adam_step(lr)
     return np.asarray(out)
+
+
+
+# the plain solver that produces training pairs: the reference's V-cycle PCG
+# on CSR (parity mode) with the capped smoother weight, one Newton iteration
+PAIR_SOLVER_KW = dict(mode='parity', smoother='safe', precond='vcycle', damp=1.0, maxiter=1,
+                      maxiter_cg=6000, tol_cg=1e-12, rel_tol_cg=1e-6, n_smooth=2,
+                      kinematic_pins=True)
+
+
+def collect_pairs(body, n_pairs=64, every=4, constraints='edge_volume', dt=1.0 / 300.0,
+                  device='cuda'):
+  """Training pairs of one body (a dict of `scenarios.training_body`): one
+  Newton iteration of the plain solver, recording up to `n_pairs`
+  restricted residuals r_c (every `every`-th V-cycle); returns the level-1
+  graph (a snapshot that outlives the solver) and the (k, n1) residuals."""
+  from .mgpbd_gpu import MGPBDSolverGPU
+  x = torch.tensor(body['x0'], device=device)
+  s = MGPBDSolverGPU(x, torch.tensor(body['x_ref'], device=device),
+                     torch.tensor(body['invm'], device=device),
+                     torch.tensor(body['t_i'], device=device), None, [0.0, -9.8, 0.0], dt,
+                     compliance=float(body['compliance']), constraints=constraints,
+                     **PAIR_SOLVER_KW)
+  s.init()
+  s.record_coarse(int(n_pairs), int(every))
+  s.step(0)
+  rc, _ = s.recorded_coarse()
+  g = s.coarse_graph().snapshot()
+  rc = rc.clone()
+  del s
+  return g, rc
+
+
+def train_on_bodies(net: CoarseNet, bodies, pairs_per_body=64, every=4, steps=600, batch=8,
+                    lr=2e-3, constraints='edge_volume'):
+  """Train `net` on pairs from several bodies (an iterable of
+  `scenarios.training_body` dicts): pairs are collected body by body, then
+  `fit_many` alternates Adam steps over the bodies.  Returns
+  (losses, [(graph, residuals)])."""
+  data = []
+  for b in bodies:
+    g, rc = collect_pairs(b, pairs_per_body, every, constraints)
+    if rc.shape[0] > 0:
+      data.append((g, rc))
+  if not data:
+    raise RuntimeError('no training pairs recorded (every solve converged before the '
+                       'first recorded V-cycle)')
+  return net.fit_many(data, steps=steps, batch=batch, lr=lr), data

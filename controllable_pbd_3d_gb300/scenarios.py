@@ -58,3 +58,48 @@ class DragDriver:
       self.solver.v_p[self.vertex] = self.target(frame)
     for _ in range(substeps):
       self.solver.step(frame)
+
+
+def grid_surface_vertices(nx, ny, nz):
+  """Ids of the grid's boundary vertices (by index, robust to jitter and to
+  the ball projection)."""
+  ii, jj, kk = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), np.arange(nz + 1),
+                           indexing='ij')
+  on = (ii == 0) | (ii == nx) | (jj == 0) | (jj == ny) | (kk == 0) | (kk == nz)
+  vid = ii + (nx + 1) * (jj + (ny + 1) * kk)
+  return np.sort(vid[on]).astype(np.int64)
+
+
+def training_body(rng, sides=(20, 40), compliance=(1e-9, 1e-4), pinned=(0.01, 0.04),
+                  jitter=0.01):
+  """One body of the learned preconditioner's training set: a hex-grid cube
+  (5 tets per hex) with side count uniform in `sides`, with probability 1/2
+  radially projected onto its ball, compliance log-uniform in `compliance`,
+  and a fraction uniform in `pinned` of its surface vertices pinned at
+  random.  Returns dict(x_ref, x0, t_i, invm, compliance, side, ball,
+  pinned)."""
+  n = int(rng.integers(sides[0], sides[1] + 1))
+  xr, t = meshgen.hex_grid_tets(n, n, n)
+  x0, _ = meshgen.hex_grid_tets(n, n, n, jitter=jitter, seed=int(rng.integers(1 << 31)))
+  ball = bool(rng.random() < 0.5)
+  if ball:
+    # project the rest shape and the jittered start with the same centre
+    c = 0.5 * (xr.min(axis=0) + xr.max(axis=0))
+    xr = meshgen.ball_project(xr, c)
+    x0 = meshgen.ball_project(x0, c)
+  surf = grid_surface_vertices(n, n, n)
+  k = max(1, int(round(rng.uniform(*pinned) * len(surf))))
+  pin = np.sort(rng.choice(surf, size=k, replace=False))
+  invm = np.ones(len(xr), np.float32)
+  invm[pin] = 0.0
+  comp = float(10.0 ** rng.uniform(np.log10(compliance[0]), np.log10(compliance[1])))
+  return dict(x_ref=xr.astype(np.float32), x0=x0.astype(np.float32), t_i=t.astype(np.int32),
+              invm=invm, compliance=comp, side=n, ball=ball, pinned=pin)
+
+
+def training_bodies(n_bodies=256, seed=0, **kw):
+  """`n_bodies` seeded training bodies (`training_body`), generated one at a
+  time so the set never sits in memory at once."""
+  rng = np.random.default_rng(seed)
+  for _ in range(int(n_bodies)):
+    yield training_body(rng, **kw)

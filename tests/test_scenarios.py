@@ -50,3 +50,48 @@ def test_gpu_drag_follows_the_target(cuda):
   # the body followed: the free vertex next to the dragged corner moved up in z
   near = s['drag'] - 1
   assert xn[near, 2] - s['x0'][near, 2] > 0.05
+
+
+def test_training_bodies_follow_the_configuration():
+  """Seeded training bodies: side counts in 20..40, half of them projected
+  onto a ball, compliance log-uniform in [1e-9, 1e-4], 1-4 % of the
+  surface vertices pinned."""
+  from controllable_pbd_3d_gb300 import meshgen
+  from controllable_pbd_3d_gb300.scenarios import grid_surface_vertices, training_bodies
+  bodies = list(training_bodies(6, seed=3))
+  again = list(training_bodies(6, seed=3))
+  for b, c in zip(bodies, again):
+    assert np.array_equal(b['x0'], c['x0']) and np.array_equal(b['pinned'], c['pinned'])
+    n = b['side']
+    assert 20 <= n <= 40
+    assert len(b['x_ref']) == (n + 1) ** 3 and len(b['t_i']) == 4 * 5 * n ** 3
+    assert 1e-9 <= b['compliance'] <= 1e-4
+    surf = grid_surface_vertices(n, n, n)
+    assert np.isin(b['pinned'], surf).all()
+    frac = len(b['pinned']) / len(surf)
+    assert 0.01 - 1 / len(surf) <= frac <= 0.04 + 1 / len(surf)
+    assert (b['invm'] == 0).sum() == len(b['pinned'])
+    xr = b['x_ref'].astype(np.float64)
+    c0 = 0.5 * (xr.min(axis=0) + xr.max(axis=0))
+    r = np.linalg.norm(xr - c0, axis=1)
+    if b['ball']:
+      assert r.max() <= 0.5 + 1e-5  # the unit cube's inscribed ball
+    else:
+      assert r.max() == pytest.approx(0.5 * np.sqrt(3), rel=1e-5)
+  assert {b['ball'] for b in bodies} == {True, False}
+  x, t = meshgen.hex_grid_tets(4, 4, 4)
+  assert np.array_equal(grid_surface_vertices(4, 4, 4), meshgen.surface_vertices(t))
+
+
+@pytest.mark.gpu
+def test_gpu_training_over_several_bodies_lowers_the_loss(cuda):
+  """Pairs from two seeded training bodies (reduced sides), recorded by the
+  plain solver, then Adam steps alternating over the bodies."""
+  from controllable_pbd_3d_gb300.learned import CoarseNet, train_on_bodies
+  from controllable_pbd_3d_gb300.scenarios import training_bodies
+  net = CoarseNet(seed=1)
+  losses, data = train_on_bodies(net, training_bodies(2, seed=5, sides=(8, 10)),
+                                 pairs_per_body=32, every=2, steps=200, batch=8, lr=2e-3)
+  assert len(data) == 2 and all(rc.shape[0] > 0 for _, rc in data)
+  assert np.isfinite(losses).all()
+  assert losses[-20:].mean() < losses[:10].mean()
