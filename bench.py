@@ -20,7 +20,6 @@ Synthetic data: the reference's experiment meshes are not available.
 from __future__ import annotations
 
 import argparse
-import ctypes as C
 import json
 import os
 import statistics
@@ -58,13 +57,16 @@ def workload(n, seed=0):
 
 
 # CG runs to relative residual 1e-6 (the cap is never reached on this
-# workload: ~2000 iterations for the plain AMG-PCG, ~650 for the fast step)
+# workload: ~2,500 iterations per solve for the plain AMG-PCG, ~760 per
+# substep for the fast step)
 SOLVER_KW = dict(damp=1.0, maxiter=20, atol=1e-4, rtol=1e-2, maxiter_cg=6000, tol_cg=1e-12,
                  rel_tol_cg=1e-6, n_smooth=2, kinematic_pins=True)
 # the optimised step: each CG solve is a primal (Woodbury) warm start to a
 # 1e-2 dual residual, then CG on the dual system to 1e-6, each one
-# cooperative persistent kernel (matrix-free operator, per-block operator
-# data in shared memory, degree-8 Chebyshev preconditioners)
+# cooperative persistent kernel (matrix-free operator, degree-8 Chebyshev
+# preconditioners; the operator data is staged in shared memory where a
+# block's share fits, as for the ARAP body, and read through L2 otherwise,
+# as for the length + volume body)
 FAST_KW = dict(mode='fast', precond='cheb', cheb_degree=8, cheb_lo=1e-3, primal=True,
                primal_tol=1e-2)
 # the plain float32 AMG-PCG: the reference's two-level tet-aggregation V-cycle

@@ -17,8 +17,7 @@ import pytest
 
 from controllable_pbd_3d_gb300 import _native as N
 from controllable_pbd_3d_gb300 import meshgen
-from controllable_pbd_3d_gb300.edge_volume import (edge_volume_hierarchy, edge_volume_system,
-                                                   tet_edges)
+from controllable_pbd_3d_gb300.edge_volume import edge_volume_hierarchy, edge_volume_system
 from oracle import mgpbd_oracle as MO
 
 

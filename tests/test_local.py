@@ -9,7 +9,6 @@ against the same golden substeps and against the oracle on larger meshes,
 colour kernels run twice for determinism.
 """
 
-import os
 
 import numpy as np
 import pytest
