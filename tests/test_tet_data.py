@@ -1,18 +1,16 @@
 """Mesh ingest (`load_tets` / `TetData`, data/tet_data.py:9-94): a MEDIT
 file written from a seeded body is read back with the reference's face
-handling, lumped masses and surface extraction; where the reference source
-is present, its own mass and face routines (numpy only) pin ours."""
-
-import importlib.util
-import os
+handling, lumped masses and surface extraction; the reference's own mass
+and face routines (`utils/geom3d.py`, outputs in `tests/golden/geom3d_ref.npz`
+from `tests/golden/make_geom_fixture.py`) pin ours bit for bit."""
 
 import numpy as np
 import pytest
 
+from conftest import golden
+
 from controllable_pbd_3d_gb300 import meshgen
 from controllable_pbd_3d_gb300.tet_data import revert_faces, vertex_mass
-
-REF_GEOM = '/root/reference/utils/geom3d.py'
 
 
 def write_medit(path, verts, tets, tris):
@@ -42,24 +40,17 @@ def boundary_triangles(t_i):
   return np.stack([b, b[:, [0, 2, 1]]], axis=1).reshape(-1)
 
 
-def load_geom():
-  spec = importlib.util.spec_from_file_location('ref_geom3d', REF_GEOM)
-  mod = importlib.util.module_from_spec(spec)
-  spec.loader.exec_module(mod)
-  return mod
-
-
-@pytest.mark.skipif(not os.path.exists(REF_GEOM), reason='reference source not present')
 def test_vertex_mass_and_faces_match_the_reference():
-  geom = load_geom()
+  z = golden('geom3d_ref.npz')
   x, t = meshgen.hex_grid_tets(4, 3, 5, jitter=0.1, seed=3)
   x = x.astype(np.float64) * 1.7
+  assert np.array_equal(x, z['x']) and np.array_equal(t, z['t'])
   order, vm, tm = vertex_mass(x, t)
-  r_order, r_vm, r_tm = geom.compute_vertex_mass(x, t.astype(np.int64))
-  assert np.array_equal(order, r_order)
-  assert np.array_equal(vm, r_vm) and np.array_equal(tm, r_tm)
+  assert np.array_equal(order, z['order'])
+  assert np.array_equal(vm, z['vm']) and np.array_equal(tm, z['tm'])
   f = boundary_triangles(t)
-  assert np.array_equal(revert_faces(f), geom.revert_all_faces(f.copy()))
+  assert np.array_equal(f, z['faces'])
+  assert np.array_equal(revert_faces(f), z['reverted'])
 
 
 def test_load_tets_reads_a_medit_file(tmp_path, cuda_or_cpu):
