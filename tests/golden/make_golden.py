@@ -3,7 +3,7 @@
 Usage (needs a checkout of JamesYang-7/Controllable_PBD_3D; not available on
 the GPU machines, which only read the committed `.npz` files):
 
-    python tests/golden/make_golden.py --ref /root/reference [--only structure|local|step]
+    python tests/golden/make_golden.py --ref /root/reference [--only structure|local|zone|step]
 
 Taichi is not installed, so `taichi_cpu_shim` stands in for it (see that
 module's docstring for what it can and cannot reproduce).  The reference
@@ -496,6 +496,47 @@ def local_fixtures(ref, out):
   np.savez_compressed(os.path.join(out, 'local.npz'), **res)
 
 
+def zone_fixtures(ref, out):
+  """The reference's AdaptiveZone (cons/adaptive_zone.py) on a seeded body
+  whose vertices moved: proximity flags, two face rings around them, and
+  strain-rate flags, as int32 per tet."""
+  import taichi as ti
+  import cons.adaptive_zone as az
+  res = {}
+  for name, n, seed in (('cube5', 5, 11), ('box6x3x4', None, 12)):
+    if n is not None:
+      xr, t = meshgen.hex_grid_tets(n, n, n)
+    else:
+      xr, t = meshgen.hex_grid_tets(6, 3, 4)
+    rng = np.random.default_rng(seed)
+    x_old = (xr + rng.uniform(-0.02, 0.02, xr.shape)).astype(np.float32)
+    x = (x_old + rng.normal(0.0, 0.004, xr.shape)).astype(np.float32)
+    nt = len(t) // 4
+    v_p = ti.Vector.field(3, dtype=ti.f32, shape=len(x))
+    v_p.from_numpy(x)
+    v_old = ti.Vector.field(3, dtype=ti.f32, shape=len(x))
+    v_old.from_numpy(x_old)
+    t_i = ti.field(ti.i32, len(t))
+    t_i.from_numpy(t.astype(np.int32))
+    zone = az.AdaptiveZone(nt, t_i, v_p)
+    center = x.mean(axis=0).astype(np.float32)
+    radius = np.float32(0.3)
+    zone.update_by_proximity(float(center[0]), float(center[1]), float(center[2]), float(radius))
+    prox = zone.tet_active.to_numpy().astype(np.int32).copy()
+    zone.expand_zone(2)
+    ring2 = zone.tet_active.to_numpy().astype(np.int32).copy()
+    threshold, dt = np.float32(3.0), np.float32(1.0 / 300.0)
+    zone.update_by_strain(v_old, float(threshold), float(dt))
+    strain = zone.tet_active.to_numpy().astype(np.int32).copy()
+    res.update({f'{name}_x': x, f'{name}_x_old': x_old, f'{name}_t': t.astype(np.int32),
+                f'{name}_center': center, f'{name}_radius': radius,
+                f'{name}_threshold': threshold, f'{name}_dt': dt,
+                f'{name}_prox': prox, f'{name}_ring2': ring2, f'{name}_strain': strain})
+    print(f'[zone] {name}: nt={nt} prox={prox.sum()} ring2={ring2.sum()} strain={strain.sum()}',
+          flush=True)
+  np.savez_compressed(os.path.join(out, 'zone.npz'), **res)
+
+
 def main():
   ap = argparse.ArgumentParser()
   ap.add_argument('--ref', default='/root/reference')
@@ -507,6 +548,8 @@ def main():
     structure_fixtures(a.ref, mg, ta, a.out)
   if a.only in (None, 'local'):
     local_fixtures(a.ref, a.out)
+  if a.only in (None, 'zone'):
+    zone_fixtures(a.ref, a.out)
   if a.only in (None, 'step'):
     for name, (build, kw, n) in STEP_CASES.items():
       for alias in (False, True):

@@ -103,3 +103,20 @@ def test_adaptive_step_matches_masked_oracle_step(cuda):
   err = float(np.abs(x.cpu().numpy() - o.x).max())
   assert err <= 1e-5 * float(np.abs(o.x).max()), err
   np.testing.assert_array_equal(s.alpha_tilde.cpu().numpy(), alpha_gpu)  # restored
+
+
+@pytest.mark.parametrize('name', ['cube5', 'box6x3x4'])
+def test_oracle_zones_match_the_reference(name):
+  """The oracle's zone restatement against the reference's own AdaptiveZone
+  (proximity, two face rings, strain rate), bit for bit
+  (`tests/golden/zone.npz`, written by `make_golden.py --only zone`)."""
+  from conftest import golden
+  from oracle.mgpbd_oracle import face_adjacency_sets, zone_expand, zone_proximity, zone_strain
+  z = golden('zone.npz')
+  g = lambda k: z[f'{name}_{k}']  # noqa: E731
+  t = g('t')
+  nt = len(t) // 4
+  prox = zone_proximity(g('x'), t, g('center'), g('radius'))
+  assert np.array_equal(prox, g('prox'))
+  assert np.array_equal(zone_expand(prox, face_adjacency_sets(t, nt), 2), g('ring2'))
+  assert np.array_equal(zone_strain(g('x'), g('x_old'), t, g('threshold'), g('dt')), g('strain'))
