@@ -3,7 +3,7 @@
 Usage (needs a checkout of JamesYang-7/Controllable_PBD_3D; not available on
 the GPU machines, which only read the committed `.npz` files):
 
-    python tests/golden/make_golden.py --ref /root/reference [--only structure|local|zone|step]
+    python tests/golden/make_golden.py --ref /root/reference [--only structure|local|zone|length|step]
 
 Taichi is not installed, so `taichi_cpu_shim` stands in for it (see that
 module's docstring for what it can and cannot reproduce).  The reference
@@ -537,6 +537,40 @@ def zone_fixtures(ref, out):
   np.savez_compressed(os.path.join(out, 'zone.npz'), **res)
 
 
+def length_fixtures(ref, out):
+  """One Gauss-Seidel sweep of the reference's LengthCons (cons/length.py)
+  over the unique edges of a seeded jittered body: the positions and
+  multipliers after the sweep."""
+  import taichi as ti
+  import cons.length as lc
+  from controllable_pbd_3d_gb300.edge_volume import tet_edges
+  xr, t = meshgen.hex_grid_tets(3, 2, 2)
+  x0, _ = meshgen.hex_grid_tets(3, 2, 2, jitter=0.15, seed=21)
+  edges, _ = tet_edges(t)
+  rest = np.sqrt(((xr[edges[:, 0]].astype(np.float64) - xr[edges[:, 1]]) ** 2).sum(1))
+  invm = np.ones(len(xr), np.float32)
+  invm[:3] = 0.0
+  compliance, dt = 1e-4, 1.0 / 300.0
+  v_p = ti.Vector.field(3, dtype=ti.f32, shape=len(x0))
+  v_p.from_numpy(x0.astype(np.float32))
+  v_ref = ti.Vector.field(3, dtype=ti.f32, shape=len(xr))
+  v_ref.from_numpy(xr.astype(np.float32))
+  e_i = ti.field(ti.i32, 2 * len(edges))
+  e_i.from_numpy(edges.reshape(-1).astype(np.int32))
+  e_rl = ti.field(ti.f32, len(edges))
+  e_rl.from_numpy(rest.astype(np.float32))
+  v_invm = ti.field(ti.f32, len(xr))
+  v_invm.from_numpy(invm)
+  cons = lc.LengthCons(v_p, v_ref, e_i, e_rl, v_invm, dt, alpha=compliance,
+                       method='gauss_seidel')
+  cons.preupdate_cons()
+  cons.update_cons()
+  np.savez_compressed(os.path.join(out, 'length.npz'), x0=x0.astype(np.float32), edges=edges,
+                      rest=rest.astype(np.float32), invm=invm, compliance=compliance, dt=dt,
+                      x1=v_p.to_numpy(), lam=cons.lambdaf.to_numpy())
+  print(f'[length] {len(edges)} edges', flush=True)
+
+
 def main():
   ap = argparse.ArgumentParser()
   ap.add_argument('--ref', default='/root/reference')
@@ -550,6 +584,8 @@ def main():
     local_fixtures(a.ref, a.out)
   if a.only in (None, 'zone'):
     zone_fixtures(a.ref, a.out)
+  if a.only in (None, 'length'):
+    length_fixtures(a.ref, a.out)
   if a.only in (None, 'step'):
     for name, (build, kw, n) in STEP_CASES.items():
       for alias in (False, True):

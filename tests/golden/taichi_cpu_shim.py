@@ -10,7 +10,7 @@ can be stored as golden fixtures.  Installing this module as `taichi` in
   *view*, so `ti.atomic_add(field[i], v)` and `field[i] += v` update storage;
 * scalar arithmetic stays float32 (numpy's weak Python-scalar promotion);
 * kernel return values become Python floats, as Taichi returns them;
-* vector / matrix methods (`dot`, `norm_sqr`, `cross`, `outer_product`,
+* vector / matrix methods (`dot`, `norm_sqr`, `normalized`, `cross`, `outer_product`,
   `inverse`, `determinant`, `Matrix.identity`) as float32 numpy operations
   (inverse and determinant through float64 LAPACK);
 * `ti.svd` is the rotation-variant SVD (U, V proper rotations, the sign of
@@ -72,6 +72,10 @@ class TiArray(np.ndarray):
 
   def norm(self):
     return np.sqrt(self.norm_sqr())
+
+  def normalized(self):
+    # the vector over its norm, in the element type
+    return (np.asarray(self) / self.norm()).view(TiArray)
 
   # matrix API
   def inverse(self):

@@ -195,3 +195,50 @@ def test_gpu_rejects_a_bad_length_constraint(cuda):
   N.check(s._lib.mgpbd_set_constraint_types(s._h, types.ctypes.data), 'types')
   with pytest.raises(MGPBDError):
     s.init()
+
+
+def test_oracle_length_constraint_replays_the_reference_sweep():
+  """One Gauss-Seidel sweep of the reference's own length constraints
+  (cons/length.py, `tests/golden/length.npz` from `make_golden.py --only
+  length`) replayed with the oracle's length C and slot gradients (slots a,
+  b, a, b): same positions and multipliers to float32 rounding."""
+  from conftest import golden
+  z = golden('length.npz')
+  x = z['x0'].astype(np.float64)
+  edges, rest, invm = z['edges'], z['rest'], z['invm'].astype(np.float64)
+  alpha = float(z['compliance']) / float(z['dt']) ** 2
+  lam = np.zeros(len(edges))
+  dm0 = np.zeros((1, 3, 3))
+  for k, (a, b) in enumerate(edges):
+    t4 = np.array([a, b, a, b], np.int32)
+    c, g = MO.constraints(x, t4, dm0, np.float64, ctype=[MO.CONS_LENGTH], rest=rest[k:k + 1])
+    g = g.reshape(4, 3)
+    assert np.allclose(g[2:], 0) and np.allclose(g[0], -g[1])
+    d = -(c[0] + alpha * lam[k]) / (invm[a] * (g[0] @ g[0]) + invm[b] * (g[1] @ g[1]) + alpha)
+    lam[k] += d
+    x[a] += invm[a] * d * g[0]
+    x[b] += invm[b] * d * g[1]
+  assert np.abs(x - z['x1']).max() <= 2e-6
+  assert np.allclose(lam, z['lam'], rtol=1e-4, atol=1e-7)
+  assert np.abs(z['lam']).max() > 1e-3  # the sweep did move the body
+
+
+def test_oracle_volume_constraint_is_the_local_hydrostatic_constraint():
+  """C = det F - 1 and its four slot gradients from the MGPBD oracle equal
+  the hydrostatic constraint of the local XPBD oracle (cons/deform3d.py:
+  81-83), whose substeps are pinned to the reference's own Deform3D
+  (`test_local.py`)."""
+  from oracle import local_oracle as LO
+  xr, t = meshgen.hex_grid_tets(3, 3, 2)
+  x, _ = meshgen.hex_grid_tets(3, 3, 2, jitter=0.2, seed=8)
+  x = x.astype(np.float64)
+  nt = len(t) // 4
+  dm_inv, _, _ = MO.rest_shape(xr, t, 1e5, 1 / 300, np.float64)
+  c, g = MO.constraints(x, t, dm_inv, np.float64, ctype=np.full(nt, MO.CONS_VOLUME))
+  B, _ = LO.rest_shape(xr.astype(np.float64), t.reshape(-1, 4))
+  q = t.reshape(-1, 4).astype(np.int64)
+  F = LO._deformation(x, q, B)
+  gH3 = LO._cof(F) @ np.transpose(B, (0, 2, 1))
+  gH = np.concatenate([np.transpose(gH3, (0, 2, 1)), -gH3.sum(axis=2)[:, None, :]], axis=1)
+  assert np.allclose(c, np.linalg.det(F) - 1.0, rtol=0, atol=1e-12)
+  assert np.allclose(g.reshape(nt, 4, 3), gH, rtol=1e-10, atol=1e-10)
