@@ -3,7 +3,7 @@
 Usage (needs a checkout of JamesYang-7/Controllable_PBD_3D; not available on
 the GPU machines, which only read the committed `.npz` files):
 
-    python tests/golden/make_golden.py --ref /root/reference [--only structure|local|zone|length|step]
+    python tests/golden/make_golden.py --ref /root/reference [--only structure|local|zone|length|adaptive|step]
 
 Taichi is not installed, so `taichi_cpu_shim` stands in for it (see that
 module's docstring for what it can and cannot reproduce).  The reference
@@ -571,6 +571,50 @@ def length_fixtures(ref, out):
   print(f'[length] {len(edges)} edges', flush=True)
 
 
+def adaptive_fixture(ref, mg, out):
+  """Two substeps of the reference's MGPBDAdaptiveSolver
+  (cons/mgpbd_adaptive.py) around its MGPBDSolverGPU, with a tool near one
+  corner: the positions and the active flags after each substep (level-0
+  order kept, V-cycle residual kept apart, as in the step fixtures)."""
+  import taichi as ti
+  import cons.adaptive_zone as az
+  import cons.mgpbd_adaptive as ma
+  xr, x0, t, invm = grid_case(5, 4, 5, 0.02, 3)
+  kw = dict(mu=1e5, damp=0.993, maxiter=3)
+  tool, radius = (0.9, 0.1, 0.85), 0.45
+  set_astype_keeps_order(True)
+  s = make_solver(mg, ti, xr, x0, t, invm, **kw)
+  s.init()
+  gs = s._gpu_solver
+  orig_vcycle = gs.vcycle
+
+  def vcycle_keep_r0(level=0):
+    saved = gs._r[0].to_numpy() if level == 0 else None
+    orig_vcycle(level)
+    if level == 0:
+      gs._r[0].from_numpy(saved)
+
+  gs.vcycle = vcycle_keep_r0
+  zone = az.AdaptiveZone(s.n_tets, s.t_i, s.v_p)
+  ad = ma.MGPBDAdaptiveSolver(s, zone)
+  traj, masks = [], []
+  for k in range(2):
+    ad.step(k, tool_pos=tool, tool_radius=radius)
+    traj.append(s.v_p.to_numpy())
+    masks.append(zone.tet_active.to_numpy().astype(np.int32))
+  set_astype_keeps_order(False)
+  res = {'x_ref': xr, 'x0': x0, 't_i': t, 'invm': invm,
+         'gravity': np.array([0.0, -9.8, 0.0], np.float32), 'dt': np.array(1.0 / 300.0),
+         'tool': np.array(tool, np.float32), 'radius': np.array(radius, np.float32),
+         'x_traj': np.stack(traj), 'masks': np.stack(masks),
+         'alpha_tilde': s.alpha_tilde.to_numpy(), 'cg_alias': np.array(False)}
+  for k, v in kw.items():
+    res['param_' + k] = np.array(v)
+  np.savez_compressed(os.path.join(out, 'adaptive.npz'), **res)
+  print(f'[adaptive] active per substep {[int(m.sum()) for m in masks]} of {s.n_tets}',
+        flush=True)
+
+
 def main():
   ap = argparse.ArgumentParser()
   ap.add_argument('--ref', default='/root/reference')
@@ -586,6 +630,8 @@ def main():
     zone_fixtures(a.ref, a.out)
   if a.only in (None, 'length'):
     length_fixtures(a.ref, a.out)
+  if a.only in (None, 'adaptive'):
+    adaptive_fixture(a.ref, mg, a.out)
   if a.only in (None, 'step'):
     for name, (build, kw, n) in STEP_CASES.items():
       for alias in (False, True):

@@ -120,3 +120,36 @@ def test_oracle_zones_match_the_reference(name):
   assert np.array_equal(prox, g('prox'))
   assert np.array_equal(zone_expand(prox, face_adjacency_sets(t, nt), 2), g('ring2'))
   assert np.array_equal(zone_strain(g('x'), g('x_old'), t, g('threshold'), g('dt')), g('strain'))
+
+
+@pytest.mark.parametrize('dtype', [np.float32, np.float64])
+def test_oracle_adaptive_step_matches_the_reference(dtype):
+  """Two substeps of the reference's own MGPBDAdaptiveSolver
+  (`tests/golden/adaptive.npz`, `make_golden.py --only adaptive`): the
+  oracle, stepping with its zone flags (proximity of the predicted
+  positions, one face ring) and alpha~ = 1e20 on passive tets, reproduces
+  the flags bit for bit and the positions to the step fixtures' tolerance."""
+  from conftest import golden, solver_kwargs
+  from oracle.mgpbd_oracle import (MGPBDOracle, face_adjacency_sets, zone_expand,
+                                   zone_proximity)
+  z = golden('adaptive.npz')
+  t = z['t_i']
+  nt = len(t) // 4
+  o = MGPBDOracle(z['x0'], z['x_ref'], z['invm'], t, z['gravity'], float(z['dt']), dtype=dtype,
+                  **solver_kwargs(z))
+  o.init()
+  adj = face_adjacency_sets(t, nt)
+  alpha0 = o.alpha.copy()
+  for k in range(len(z['x_traj'])):
+    o.make_prediction()
+    mask = zone_expand(zone_proximity(o.x.astype(np.float32), t, z['tool'], z['radius']), adj, 1)
+    assert np.array_equal(mask, z['masks'][k])
+    o.alpha = np.where(mask == 1, alpha0, dtype(1e20)).astype(dtype)
+    o.solve(k)
+    o.alpha = alpha0.copy()
+    o.update_vel()
+    scale = float(np.abs(z['x_traj'][k]).max())
+    err = float(np.abs(o.x - z['x_traj'][k]).max())
+    assert err <= (2e-6 if dtype == np.float32 else 1e-5) * scale, (k, err)
+  assert np.array_equal(o.alpha, alpha0)  # restored after every substep
+  assert np.allclose(alpha0, z['alpha_tilde'], rtol=1e-6, atol=0)
