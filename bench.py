@@ -15,6 +15,11 @@ ARAP constraint per tet (25.9M nonzeros), also reported as a secondary leg.
 Synthetic data: the reference's experiment meshes are not available.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--constraints edge_volume|arap] [--workload cube|slab]
+
+`--workload slab` prints the stiff-drag slab's line instead: 100x100x25
+hexes (1.25 M tets), compliance 1e-10, one long edge pinned, the opposite
+corner dragged 0.5 along +z over 60 frames; fast step only.
 """
 
 from __future__ import annotations
