@@ -242,3 +242,32 @@ def test_oracle_volume_constraint_is_the_local_hydrostatic_constraint():
   gH = np.concatenate([np.transpose(gH3, (0, 2, 1)), -gH3.sum(axis=2)[:, None, :]], axis=1)
   assert np.allclose(c, np.linalg.det(F) - 1.0, rtol=0, atol=1e-12)
   assert np.allclose(g.reshape(nt, 4, 3), gH, rtol=1e-10, atol=1e-10)
+
+
+def test_cpp_structure_matches_oracle_on_the_length_volume_system():
+  """Level-0 pattern (constraints sharing a vertex, itself last) and the
+  Galerkin pattern and contribution map of the length + volume system,
+  whose length constraints repeat their vertices (a, b, a, b): the C++
+  builders equal the oracle bit for bit."""
+  from controllable_pbd_3d_gb300 import tet_aggregation as ta
+  xr, t = meshgen.hex_grid_tets(6, 5, 4, jitter=0.05, seed=9)
+  c, types, _, _ = edge_volume_system(t)
+  nc = len(types)
+  ip, ix = ta.sparsity_pattern(c, nc)
+  ip2, ix2 = MO.sparsity_pattern(c, nc)
+  np.testing.assert_array_equal(ip, ip2)
+  np.testing.assert_array_equal(ix, ix2)
+  rows = np.repeat(np.arange(nc), np.diff(ip))
+  assert (ix[ip[1:] - 1] == np.arange(nc)).all()  # the constraint itself last
+  assert len(np.unique(rows * nc + ix)) == len(ix)  # no duplicate columns
+  agg = edge_volume_hierarchy(t)
+  n1 = int(agg.max()) + 1
+  rng = np.random.default_rng(3)
+  data = rng.standard_normal(len(ix)).astype(np.float32)
+  data[rng.random(len(ix)) < 0.2] = 0.0
+  ci, cx, cidx, coff = ta.galerkin_structure(ip, ix, data, agg, n1)
+  ci2, cx2, cidx2, coff2, _ = MO.galerkin(ip2, ix2, data, agg, n1)
+  np.testing.assert_array_equal(ci, ci2)
+  np.testing.assert_array_equal(cx, cx2)
+  np.testing.assert_array_equal(cidx, cidx2)
+  np.testing.assert_array_equal(coff, coff2)
