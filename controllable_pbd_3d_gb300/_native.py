@@ -172,6 +172,7 @@ _SIGS = {
     'mgpbd_record_coarse': (C.c_int, [vp, vp, vp, i32, i32]),
     'mgpbd_record_count': (C.c_int, [vp, P_i32]),
     'mgpbd_host_pattern': (C.c_int, [vp, i32, P_i64, vp, vp]),
+    'mgpbd_host_vertex_incidence': (C.c_int, [vp, i32, i32, P_i64, vp, vp]),
     'mgpbd_host_aggregate': (C.c_int, [vp, i32, i32, vp, P_i32]),
     'mgpbd_host_tet_hierarchy': (C.c_int, [vp, i32, i32, i32, P_i32, vp, vp]),
     'mgpbd_host_galerkin': (C.c_int, [i32, vp, vp, vp, vp, i32, P_i64, P_i64, vp, vp, vp, vp]),

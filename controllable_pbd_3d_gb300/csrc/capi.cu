@@ -568,6 +568,23 @@ int mgpbd_scale(int32_t n, float alpha, float* x, void* stream) {
 }
 
 // ---- host structure builders ----------------------------------------------
+int mgpbd_host_vertex_incidence(const int32_t* t_i, int32_t nt, int32_t nv, int64_t* n_entries,
+                                int32_t* ptr, int32_t* entries) {
+  if (!t_i || nt < 0 || nv < 0 || !n_entries) return MGPBD_EINVAL;
+  return guarded([&] {
+    for (int64_t k = 0; k < 4LL * nt; ++k)
+      mgpbd::require(t_i[k] >= 0 && t_i[k] < nv, MGPBD_EINVAL, "vertex id out of range");
+    std::vector<int32_t> p, e;
+    mgpbd::vertex_incidence(t_i, nt, nv, p, e);
+    *n_entries = static_cast<int64_t>(e.size());
+    if (ptr) {
+      mgpbd::require(entries != nullptr || e.empty(), MGPBD_EINVAL, "entries buffer missing");
+      std::memcpy(ptr, p.data(), sizeof(int32_t) * p.size());
+      if (!e.empty()) std::memcpy(entries, e.data(), sizeof(int32_t) * e.size());
+    }
+  });
+}
+
 int mgpbd_host_pattern(const int32_t* t_i, int32_t nt, int64_t* nnz, int32_t* indptr,
                        int32_t* indices) {
   if (!t_i || nt < 0 || !nnz) return MGPBD_EINVAL;

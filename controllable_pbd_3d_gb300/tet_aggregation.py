@@ -98,6 +98,23 @@ def sparsity_pattern(t_i_np, n_tets):
   return indptr, indices
 
 
+def vertex_incidence(t_i_np, n_tets, n_verts):
+  """Vertex-major incidence of the matrix-free operator (no reference
+  counterpart): (ptr, entries) with entries 4 * t + l, ascending t, slots
+  repeating an earlier vertex of their constraint left out."""
+  t = _as_i32(t_i_np)
+  n = C.c_int64(0)
+  N.check(N.lib().mgpbd_host_vertex_incidence(t.ctypes.data, int(n_tets), int(n_verts),
+                                              C.byref(n), None, None),
+          'mgpbd_host_vertex_incidence')
+  ptr = np.empty(n_verts + 1, np.int32)
+  ent = np.empty(max(n.value, 1), np.int32)
+  N.check(N.lib().mgpbd_host_vertex_incidence(t.ctypes.data, int(n_tets), int(n_verts),
+                                              C.byref(n), ptr.ctypes.data, ent.ctypes.data),
+          'mgpbd_host_vertex_incidence')
+  return ptr, ent[:n.value]
+
+
 def galerkin_structure(indptr, indices, data, agg_ids, n_agg):
   """Coarse CSR pattern and contribution map of `cons/mgpcg_gpu.py:43-99`
   for piecewise-constant P: returns (c_indptr, c_indices, contrib_idx,

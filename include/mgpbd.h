@@ -523,6 +523,15 @@ int mgpbd_scale(int32_t n, float alpha, float* x, void* stream);
  * NULL to get *nnz, then again with indptr (nt+1) and indices (*nnz). */
 int mgpbd_host_pattern(const int32_t* t_i, int32_t nt, int64_t* nnz,
                        int32_t* indptr, int32_t* indices);
+/* Vertex incidence of the matrix-free operator (no reference counterpart:
+ * the reference assembles A in CSR): for each vertex v, entries
+ * ptr[v] .. ptr[v+1]-1 hold 4 * t + l for every slot l of constraint t that
+ * names v, in ascending t; a slot repeating a vertex of an earlier slot of
+ * its constraint (a length constraint's a, b, a, b) is left out.  Vertex ids
+ * must lie in [0, nv).  Call with ptr == NULL to get *n_entries, then again
+ * with ptr (nv+1) and entries (*n_entries). */
+int mgpbd_host_vertex_incidence(const int32_t* t_i, int32_t nt, int32_t nv, int64_t* n_entries,
+                                int32_t* ptr, int32_t* entries);
 /* tet_geometry_aggregation pass 1 (cons/tet_aggregation.py:40-127), with
  * the reference's tie order reproduced; agg_ids has nt entries. */
 int mgpbd_host_aggregate(const int32_t* t_i, int32_t nt, int32_t max_agg_size,

@@ -271,3 +271,29 @@ def test_cpp_structure_matches_oracle_on_the_length_volume_system():
   np.testing.assert_array_equal(cx, cx2)
   np.testing.assert_array_equal(cidx, cidx2)
   np.testing.assert_array_equal(coff, coff2)
+
+
+def test_vertex_incidence_leaves_out_repeated_slots():
+  """The operator's vertex incidence (host builder of the library) against a
+  numpy restatement: 4 * t + l per slot naming the vertex, ascending t, the
+  repeated slots of length constraints (a, b, a, b) left out; bad ids are
+  rejected."""
+  from controllable_pbd_3d_gb300 import tet_aggregation as ta
+  xr, t = meshgen.hex_grid_tets(4, 3, 3)
+  c, types, _, _ = edge_volume_system(t)
+  nc, nv = len(types), len(xr)
+  ptr, ent = ta.vertex_incidence(c, nc, nv)
+  q = c.reshape(-1, 4)
+  keep = np.ones_like(q, bool)
+  for l in range(1, 4):
+    keep[:, l] = ~(q[:, :l] == q[:, l:l + 1]).any(axis=1)
+  slot = (4 * np.arange(nc)[:, None] + np.arange(4)[None, :])[keep]
+  vert = q[keep]
+  order = np.lexsort((slot, vert))
+  assert np.array_equal(ent, slot[order])
+  assert np.array_equal(ptr, np.concatenate([[0], np.cumsum(np.bincount(vert, minlength=nv))]))
+  assert len(ent) == 4 * int((types == MO.CONS_VOLUME).sum()) + 2 * int((types == MO.CONS_LENGTH).sum())
+  bad = c.copy()
+  bad[5] = nv
+  with pytest.raises(Exception):
+    ta.vertex_incidence(bad, nc, nv)
