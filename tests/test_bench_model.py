@@ -82,3 +82,25 @@ def test_roofline_from_steps_picks_the_dominant_kernel():
   assert r['traffic_over_algorithmic'] == pytest.approx(r['traffic'] / per_launch, abs=1e-4)
   assert r['share_of_cg_gpu_time'] + r['other']['share_of_cg_gpu_time'] == pytest.approx(1, abs=2e-3)
   assert np.isclose(r['frac'], r['achieved'] / 6701.2, atol=1e-4)
+
+
+def test_reference_arm_prints_one_contract_line():
+  """`bench.py --impl reference` (the OpenMP CPU port of the plain step on
+  the host cores) prints one JSON line with the contract's keys: impl,
+  cpu_baseline (kind, cores, sample, value = the line's) and an e2e block
+  with no host-device copies."""
+  import json
+  import subprocess
+  import sys
+  from conftest import ROOT
+  out = subprocess.run([sys.executable, 'bench.py', '--impl', 'reference', '--steps', '1',
+                        '--warmup', '0', '--size', '10'], cwd=ROOT, capture_output=True, text=True,
+                       timeout=600, check=True).stdout.strip().splitlines()
+  assert len(out) == 1
+  d = json.loads(out[0])
+  assert d['impl'] == 'reference' and d['unit'] == 'substeps/s' and d['higher_is_better']
+  assert d['value'] > 0 and d['n_gpus'] == 1
+  cb = d['cpu_baseline']
+  assert cb['value'] == d['value'] and cb['kind'] == 'port' and cb['cores'] >= 1 and cb['sample']
+  assert d['e2e'] == {'value': d['value'], 'unit': d['unit'], 'h2d_bytes_per_step': 0,
+                      'd2h_bytes_per_step': 0}
