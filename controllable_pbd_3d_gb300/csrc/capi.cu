@@ -65,6 +65,12 @@ int guarded(F&& f) {
 
 cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+}  // namespace
+
+void mgpbd::set_last_error(const std::string& msg) { g_last_error = msg; }
+
+namespace {
+
 // copies a colouring into caller arrays of the documented capacities
 void put_coloring(const mgpbd::Coloring& c, int32_t* ordered, int32_t* offsets, int32_t* n_colors) {
   std::copy(c.ordered.begin(), c.ordered.end(), ordered);

@@ -40,6 +40,10 @@ inline void require(bool ok, int code, const char* msg) {
   if (!ok) throw Error(code, msg);
 }
 
+// Records the message that mgpbd_last_error() returns on the calling
+// thread (defined in capi.cu beside the C ABI's error mapping).
+void set_last_error(const std::string& msg);
+
 // Owning device buffer (cudaMalloc / cudaFree).
 template <class T>
 struct DevBuf {

@@ -93,8 +93,15 @@ __global__ void k_na_final(const double* __restrict__ partials, int64_t nb, doub
 
 extern "C" int mgpbd_dot_noalloc(int32_t n, const float* a, const float* b, double* out,
                                  void* stream) {
-  if (n < 0 || !out || (n > 0 && (!a || !b))) return MGPBD_EINVAL;
-  if (static_cast<int64_t>(n) > mgpbd::kNaMaxN) return MGPBD_ERANGE;
+  if (n < 0 || !out || (n > 0 && (!a || !b))) {
+    mgpbd::set_last_error("mgpbd_dot_noalloc: n < 0 or a null pointer");
+    return MGPBD_EINVAL;
+  }
+  if (static_cast<int64_t>(n) > mgpbd::kNaMaxN) {
+    mgpbd::set_last_error("mgpbd_dot_noalloc: n above 67,108,864 (the fixed scratch holds one "
+                          "partial sum per 1024 elements, 65,536 at most)");
+    return MGPBD_ERANGE;
+  }
   try {
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     double* scratch = mgpbd::scratch_address();
@@ -112,8 +119,10 @@ extern "C" int mgpbd_dot_noalloc(int32_t n, const float* a, const float* b, doub
     MGPBD_CUDA(cudaStreamSynchronize(s));
     return MGPBD_OK;
   } catch (const mgpbd::Error& e) {
+    mgpbd::set_last_error(std::string("mgpbd_dot_noalloc: ") + e.what());
     return e.code;
-  } catch (...) {
+  } catch (const std::exception& e) {
+    mgpbd::set_last_error(std::string("mgpbd_dot_noalloc: ") + e.what());
     return MGPBD_EINVAL;
   }
 }

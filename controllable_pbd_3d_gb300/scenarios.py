@@ -17,6 +17,19 @@ import torch
 from . import meshgen
 
 
+def cube_body(n, seed=0):
+  """The benchmark's cube: n x n x n hexes of side 1/n (5 tets per hex), start
+  positions jittered U(+-0.01 h) from `seed`, unit vertex mass, the top face
+  (max y) pinned, compliance log-uniform in [1e-9, 1e-4] drawn from a fresh
+  `default_rng(seed)`.  Returns (x_ref, x0, t_i, invm, compliance)."""
+  xr, t = meshgen.hex_grid_tets(n, n, n)
+  x0, _ = meshgen.hex_grid_tets(n, n, n, jitter=0.01, seed=seed)
+  invm = np.ones(len(xr), np.float32)
+  invm[meshgen.grid_face_vertices(n, n, n, axis=1, side='max')] = 0.0
+  compliance = float(10.0 ** np.random.default_rng(seed).uniform(-9.0, -4.0))
+  return xr, x0, t, invm, compliance
+
+
 def grid_edge_vertices(nx, ny, nz, j=0, k=0):
   """Vertex ids of the grid line along x at (y index j, z index k)."""
   i = np.arange(nx + 1)

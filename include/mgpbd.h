@@ -507,10 +507,12 @@ int mgpbd_dot(int32_t n, const float* a, const float* b, double* out, void* stre
  * result), held by every GPU that loads the library until the process
  * exits.  n is limited to 67,108,864 elements (MGPBD_ERANGE beyond).  The
  * first call on each device looks up the array's address (with that
- * device current); make that first call before any stream capture.  All
- * calls share the one array: calls that overlap on the GPU (other streams,
- * other host threads) race and must be serialised by the caller.  `out` is
- * host memory; the call returns after the result is copied back. */
+ * device current).  All calls share the one array: calls that overlap on
+ * the GPU (other streams, other host threads) race and must be serialised
+ * by the caller.  `out` is host memory: the call synchronises `stream` and
+ * blocks the host until the result is copied back, so it cannot be called
+ * while `stream` is being captured into a CUDA graph.  A failure records
+ * its message for mgpbd_last_error(). */
 int mgpbd_dot_noalloc(int32_t n, const float* a, const float* b, double* out, void* stream);
 /* gpu_axpy (:26-30) y += alpha x ; gpu_xpay (:33-37) y = x + alpha y */
 int mgpbd_axpy(int32_t n, float alpha, const float* x, float* y, void* stream);

@@ -236,6 +236,45 @@ def graph_aggregate(indptr, indices, max_agg_size=8):
   return agg.astype(np.int32), n_agg
 
 
+def edge_volume_system(t_i):
+  """The length + volume constraint set of a tet mesh, restated for the
+  oracle: one volume constraint per tet (slots v0..v3, C = det F - 1 as in
+  cons/deform3d.py:81-83), then one length constraint per unique tet edge
+  (a < b, edges in ascending (a, b) order; slots a, b, a, b; C = |x_a - x_b|
+  - L0 as in cons/length.py:65-90).  Returns (c_i, ctype, edges, owner),
+  owner = the lowest-numbered tet containing the edge."""
+  t = np.asarray(t_i, np.int64).reshape(-1, 4)
+  nt = len(t)
+  nv = int(t.max()) + 1
+  pairs = [(0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)]
+  a = np.concatenate([np.minimum(t[:, i], t[:, j]) for i, j in pairs])
+  b = np.concatenate([np.maximum(t[:, i], t[:, j]) for i, j in pairs])
+  tet = np.tile(np.arange(nt), len(pairs))
+  key = a * nv + b
+  uniq, inv = np.unique(key, return_inverse=True)
+  owner = np.full(len(uniq), nt, np.int64)
+  np.minimum.at(owner, inv, tet)
+  edges = np.stack([uniq // nv, uniq % nv], 1)
+  c = np.concatenate([t, edges[:, [0, 1, 0, 1]]]).astype(np.int32)
+  ctype = np.concatenate([np.full(nt, CONS_VOLUME), np.full(len(edges), CONS_LENGTH)])
+  return c.reshape(-1), ctype.astype(np.int32), edges.astype(np.int32), owner.astype(np.int32)
+
+
+def edge_volume_hierarchy(t_i, max_coarse=400):
+  """Level-0 aggregates of the length + volume constraints from the
+  reference's tet aggregation (cons/tet_aggregation.py:145-211): a volume
+  constraint lies in its tet's aggregate, a length constraint in its owner
+  tet's.  Returns (aggs, sizes) as tet_hierarchy does, one level."""
+  t = np.asarray(t_i, np.int32).reshape(-1)
+  nt = len(t) // 4
+  aggs, sizes = tet_hierarchy(t, nt, max_coarse)
+  if not aggs:
+    return [], [nt]
+  _, _, edges, owner = edge_volume_system(t)
+  agg_t = np.asarray(aggs[0], np.int64)
+  return [np.concatenate([agg_t, agg_t[owner]]).astype(np.int32)], [nt + len(edges), sizes[1]]
+
+
 # ----------------------------------------------------------------------------
 # per-tet / per-vertex arithmetic
 # ----------------------------------------------------------------------------
@@ -435,7 +474,19 @@ class MGPBDOracle:
                rtol=1e-2, maxiter_cg=100, tol_cg=1e-5, n_smooth=2, omega_jacobi=2.0 / 3.0,
                use_line_search=True, dtype=np.float32, kinematic_pins=False, rel_tol_cg=0.0,
                smoother='jacobi', coarse='jacobi', extra_levels=0, max_coarse=400,
-               coarse_sweeps=0, hierarchy=None, cg_alias=False, compliance=0.0, ctype=None):
+               coarse_sweeps=0, hierarchy=None, cg_alias=False, compliance=0.0, ctype=None,
+               linear='pcg', exact_tol=1e-11):
+    """linear='pcg': the reference's V-cycle PCG; 'exact': each Newton
+    system solved to a float64 dual residual of exact_tol |b|
+    (oracle/exact_solve.py), for checking positions against the step with
+    an exact linear solve (float64 only)."""
+    if linear not in ('pcg', 'exact'):
+      raise ValueError("linear must be 'pcg' or 'exact'")
+    if linear == 'exact' and dtype != np.float64:
+      raise ValueError("linear='exact' is a float64 oracle")
+    self.linear = linear
+    self.exact_tol = exact_tol
+    self.exact_log = []
     self.dtype = dtype
     f = dtype
     self.x = np.array(x0, f).reshape(-1, 3)
@@ -477,11 +528,14 @@ class MGPBDOracle:
     f = self.dtype
     self.dm_inv, self.rest_vol, self.alpha = rest_shape(self.x_ref, self.t_i, self.mu, float(self.dt), f,
                                                         self.compliance, self.ctype)
+    self.lam = np.zeros(self.nt, f)
+    self.C, self.gradC = constraints(self.x, self.t_i, self.dm_inv, f, self.ctype, self.rest_vol)
+    if self.linear == 'exact':
+      self.levels = []  # no assembled matrix: the exact solve is matrix-free in A
+      return
     ip, ix = sparsity_pattern(self.t_i, self.nt)
     L0 = Level(ip, ix, f)
     self.levels = [L0]
-    self.lam = np.zeros(self.nt, f)
-    self.C, self.gradC = constraints(self.x, self.t_i, self.dm_inv, f, self.ctype, self.rest_vol)
     L0.data = fill_A(ip, ix, self.t_i, self.invm, self.gradC, self.alpha, f)
     if self._hierarchy is None:
       aggs, sizes = tet_hierarchy(self.t_i, self.nt, self.max_coarse)
@@ -695,8 +749,15 @@ class MGPBDOracle:
       if r < self.atol or (r0 > 1e-12 and r < self.rtol * r0):
         self.log.append((ite, r, 0, 1.0))
         break
-      self.fill_matrices()
-      dlam, it = self.pcg(b)
+      if self.linear == 'exact':
+        from .exact_solve import ExactDualSolve
+        ex = ExactDualSolve(self.t_i, self.gradC, self.invm, self.alpha)
+        dlam, rel = ex.solve(b, self.exact_tol)
+        self.exact_log.append((ite, rel, list(ex.iters)))
+        it = 0
+      else:
+        self.fill_matrices()
+        dlam, it = self.pcg(b)
       self.scatter(dlam)
       omega = self.line_search() if self.use_line_search else 1.0
       self.apply(omega)

@@ -3,7 +3,7 @@ solver_benchmark_ref_summary.json with the reference's own recorder
 (`utils/bench.py`, SolverBenchmark), imported from the reference checkout.
 The timestamps are overwritten with fixed values so the files are stable.
 
-    python tests/golden/make_bench_record.py /root/reference
+    python tests/golden/make_bench_record.py <reference checkout>   (or REFERENCE_ROOT=<checkout>)
 """
 
 import importlib.util
@@ -40,4 +40,7 @@ def main(ref_root):
 
 
 if __name__ == '__main__':
-  main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+  ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get('REFERENCE_ROOT')
+  if not ref:
+    raise SystemExit(f'usage: python {sys.argv[0]} <reference checkout> (or set REFERENCE_ROOT)')
+  main(ref)

@@ -2,7 +2,7 @@
 masses, tet volumes and face reversal (`utils/geom3d.py`, numpy only, imported
 from the reference checkout) on a seeded jittered hex body.
 
-    python tests/golden/make_geom_fixture.py /root/reference
+    python tests/golden/make_geom_fixture.py <reference checkout>   (or REFERENCE_ROOT=<checkout>)
 """
 
 import importlib.util
@@ -34,4 +34,7 @@ def main(ref_root):
 
 
 if __name__ == '__main__':
-  main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+  ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get('REFERENCE_ROOT')
+  if not ref:
+    raise SystemExit(f'usage: python {sys.argv[0]} <reference checkout> (or set REFERENCE_ROOT)')
+  main(ref)

@@ -3,7 +3,7 @@
 Usage (needs a checkout of JamesYang-7/Controllable_PBD_3D; not available on
 the GPU machines, which only read the committed `.npz` files):
 
-    python tests/golden/make_golden.py --ref /root/reference [--only structure|local|zone|length|adaptive|step]
+    python tests/golden/make_golden.py --ref <reference checkout> [--only structure|local|zone|length|adaptive|step]
 
 Taichi is not installed, so `taichi_cpu_shim` stands in for it (see that
 module's docstring for what it can and cannot reproduce).  The reference
@@ -617,10 +617,13 @@ def adaptive_fixture(ref, mg, out):
 
 def main():
   ap = argparse.ArgumentParser()
-  ap.add_argument('--ref', default='/root/reference')
+  ap.add_argument('--ref', default=os.environ.get('REFERENCE_ROOT'),
+                  help='the reference checkout (default: $REFERENCE_ROOT)')
   ap.add_argument('--only', default=None)
   ap.add_argument('--out', default=HERE)
   a = ap.parse_args()
+  if not a.ref:
+    ap.error('pass --ref <reference checkout> or set REFERENCE_ROOT')
   mg, ta = load_reference(a.ref)
   if a.only in (None, 'structure'):
     structure_fixtures(a.ref, mg, ta, a.out)

@@ -107,3 +107,16 @@ def test_stats_struct_layout_matches_the_header(tmp_path):
   assert int(out['size']) == C.sizeof(N.Stats)
   for f in fields:
     assert int(out[f]) == getattr(N.Stats, f).offset, f
+
+
+def test_dot_noalloc_rejects_bad_sizes_with_a_message():
+  """The allocation-free dot product checks its size against the fixed
+  scratch before any CUDA call and leaves a message (no GPU needed)."""
+  import ctypes as C
+  L = N.lib()
+  out = C.c_double(-1.0)
+  assert L.mgpbd_dot_noalloc(67_108_864 + 1, C.c_void_p(16), C.c_void_p(16), C.byref(out),
+                             None) == -6  # MGPBD_ERANGE
+  assert b'67,108,864' in L.mgpbd_last_error()
+  assert L.mgpbd_dot_noalloc(-1, None, None, C.byref(out), None) == -1  # MGPBD_EINVAL
+  assert b'mgpbd_dot_noalloc' in L.mgpbd_last_error()

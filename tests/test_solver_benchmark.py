@@ -48,10 +48,10 @@ def test_new_record_has_the_reference_layout(tmp_path):
   path = tmp_path / 'rec.json'
   b.save(str(path))
   data = json.loads(path.read_text())
-  assert set(data) == set(ref)
+  assert list(data) == list(ref)
   fr, rf = data['frames'][0], ref['frames'][0]
-  assert set(fr) == set(rf)
-  assert set(fr['iterations'][0]) == set(rf['iterations'][0])
+  assert list(fr) == list(rf)
+  assert list(fr['iterations'][0]) == list(rf['iterations'][0])
   assert fr['iterations'][1]['t'] == 123.0
   assert fr['t_start'] <= fr['iterations'][0]['t'] <= fr['t_end']
   s = SolverBenchmark.load(str(path)).summary()

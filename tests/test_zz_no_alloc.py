@@ -55,3 +55,6 @@ def test_dot_noalloc_empty_and_limit(cuda):
   assert L.mgpbd_dot_noalloc(too_many, a.data_ptr(), a.data_ptr(), C.byref(out),
                              C.c_void_p(stream)) == -6
   assert L.mgpbd_strerror(-6) == b'size out of range'
+  assert b'67,108,864' in L.mgpbd_last_error()
+  assert L.mgpbd_dot_noalloc(-1, None, None, C.byref(out), C.c_void_p(stream)) == -1
+  assert b'mgpbd_dot_noalloc' in L.mgpbd_last_error()
