@@ -138,6 +138,9 @@ _SIGS = {
     'mgpbd_apply_matrix': (C.c_int, [vp, i32, vp, vp]),
     'mgpbd_level_sweep': (C.c_int, [vp, i32, i32, vp, vp, vp, f32]),
     'mgpbd_set_hierarchy': (C.c_int, [vp, vp, i32, vp]),
+    'mgpbd_set_matrix': (C.c_int, [vp, i32, C.c_int64, vp, vp, vp]),
+    'mgpbd_update_matrix': (C.c_int, [vp, vp]),
+    'mgpbd_set_barrier_limit': (C.c_int, [vp, C.c_double]),
     'mgpbd_zone_proximity': (C.c_int, [vp, vp, f32, f32, f32, f32]),
     'mgpbd_zone_strain': (C.c_int, [vp, vp, vp, f32, f32]),
     'mgpbd_zone_expand': (C.c_int, [vp, vp, i32]),

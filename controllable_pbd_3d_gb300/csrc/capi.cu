@@ -164,6 +164,22 @@ int mgpbd_set_hierarchy(mgpbd_handle h, const int32_t* agg_ids, int32_t n_levels
   return guarded([&] { h->impl.set_hierarchy(agg_ids, n_levels, level_sizes); });
 }
 
+int mgpbd_set_matrix(mgpbd_handle h, int32_t n, int64_t nnz, const int32_t* indptr,
+                     const int32_t* indices, const float* data) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.set_matrix(n, nnz, indptr, indices, data); });
+}
+
+int mgpbd_update_matrix(mgpbd_handle h, const float* data) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.update_matrix(data); });
+}
+
+int mgpbd_set_barrier_limit(mgpbd_handle h, double seconds) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.set_barrier_limit(seconds); });
+}
+
 int mgpbd_init(mgpbd_handle h) {
   if (!h) return MGPBD_EINVAL;
   return guarded([&] { h->impl.init(); });

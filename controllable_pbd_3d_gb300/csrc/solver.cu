@@ -149,6 +149,95 @@ void Solver::require_init() const {
   require(inited_, MGPBD_ESTATE, "mgpbd_init has not been called");
 }
 
+void Solver::require_mesh() const {
+  require_init();
+  require(!matrix_mode_, MGPBD_ESTATE,
+          "this handle solves a caller's matrix (mgpbd_set_matrix): it has no mesh");
+}
+
+void Solver::set_matrix(int32_t n, int64_t nnz, const int32_t* indptr, const int32_t* indices,
+                        const float* data) {
+  require(indptr && indices && data, MGPBD_EINVAL, "null matrix array");
+  require(n > 0 && nnz > 0, MGPBD_EINVAL, "empty matrix");
+  require(nnz < INT32_MAX, MGPBD_ERANGE, "too many nonzeros for int32 row pointers");
+  require(indptr[0] == 0 && indptr[n] == nnz, MGPBD_EINVAL, "indptr must run from 0 to nnz");
+  for (int32_t i = 0; i < n; ++i) {
+    require(indptr[i + 1] >= indptr[i], MGPBD_EINVAL, "indptr must not decrease");
+    bool diag = false;
+    for (int64_t k = indptr[i]; k < indptr[i + 1]; ++k) {
+      require(indices[k] >= 0 && indices[k] < n, MGPBD_EINVAL, "column index outside [0, n)");
+      diag |= indices[k] == i;
+    }
+    require(diag, MGPBD_EINVAL, "every row needs its diagonal entry (Jacobi smoother)");
+  }
+  x_ref_ = invm_ = nullptr;
+  t_i_ = nullptr;
+  x_ = v_ = nullptr;
+  nv_ = 0;
+  nt_ = n;
+  mat_csr_.n_rows = mat_csr_.n_cols = n;
+  mat_csr_.indptr.assign(indptr, indptr + n + 1);
+  mat_csr_.indices.assign(indices, indices + nnz);
+  mat_vals_.assign(data, data + nnz);
+  matrix_mode_ = true;
+  inited_ = false;
+  user_sizes_.clear();
+  user_aggs_.clear();
+  ctype_host_.clear();
+  if (cg_exec_) {
+    cudaGraphExecDestroy(cg_exec_);
+    cg_exec_ = nullptr;
+  }
+}
+
+void Solver::update_matrix(const float* data) {
+  require_init();
+  require(matrix_mode_, MGPBD_ESTATE, "mgpbd_update_matrix needs mgpbd_set_matrix");
+  require(data != nullptr, MGPBD_EINVAL, "null values");
+  Level& L0 = levels_[0];
+  MGPBD_CUDA(cudaMemcpyAsync(L0.data.p, data, sizeof(float) * L0.nnz, cudaMemcpyDeviceToDevice,
+                             stream_));
+  launch_diag_inv_scan(L0.indptr.p, L0.indices.p, L0.data.p, L0.n, L0.diag_inv.p, stream_);
+  refill_coarse();
+}
+
+void Solver::init_matrix() {
+  require(!cheb() && !learned(), MGPBD_ENOTSUP,
+          "a caller's matrix is solved by the V-cycle PCG (precond vcycle)");
+  cudaStream_t s = stream_;
+  if (!h_buf_) MGPBD_CUDA(cudaMallocHost(&h_buf_, sizeof(double) * 64));
+  if (!h_state_) MGPBD_CUDA(cudaMallocHost(&h_state_, sizeof(CgState)));
+  if (!h_cf_) MGPBD_CUDA(cudaMallocHost(&h_cf_, sizeof(ChebCoef)));
+  for (cudaEvent_t& e : ev_)
+    if (!e) MGPBD_CUDA(cudaEventCreate(&e));
+  partials_.alloc(static_cast<int64_t>(kMaxReduceBlocks) * 16);
+  scalars_.alloc(64);
+  omegas_.alloc(16);
+  cg_state_.alloc(1);
+  levels_.clear();
+  levels_.emplace_back();
+  Level& L0 = levels_[0];
+  L0.host = mat_csr_;
+  L0.n = nt_;
+  L0.nnz = L0.host.nnz();
+  upload(L0.indptr, L0.host.indptr, s);
+  upload_padded(L0.indices, L0.host.indices, s);
+  upload_padded(L0.data, mat_vals_, s);
+  L0.diag_inv.alloc(nt_);
+  launch_diag_inv_scan(L0.indptr.p, L0.indices.p, L0.data.p, L0.n, L0.diag_inv.p, s);
+  build_hierarchy({}, mat_vals_);
+  alloc_work();
+  inited_ = true;
+  refill_coarse();
+  MGPBD_CUDA(cudaStreamSynchronize(s));
+  stats_ = mgpbd_stats{};
+  stats_.n_levels = n_levels();
+  for (int32_t l = 0; l < n_levels() && l < 8; ++l) {
+    stats_.rows[l] = levels_[l].n;
+    stats_.nnz[l] = levels_[l].nnz;
+  }
+}
+
 // Caller-provided aggregation hierarchy (used by the next init instead of
 // the built-in tet aggregation): level_sizes[0] = nt, and for each level l
 // the level_sizes[l] entries of agg_ids from offset sum(level_sizes[0..l))
@@ -164,7 +253,8 @@ void Solver::set_constraint_types(const int32_t* types) {
 }
 
 void Solver::set_hierarchy(const int32_t* agg_ids, int32_t n_levels, const int32_t* level_sizes) {
-  require(x_ && t_i_, MGPBD_ESTATE, "mgpbd_set_mesh must come before mgpbd_set_hierarchy");
+  require((x_ && t_i_) || matrix_mode_, MGPBD_ESTATE,
+          "mgpbd_set_mesh or mgpbd_set_matrix must come before mgpbd_set_hierarchy");
   require(n_levels >= 2 && n_levels <= 8, MGPBD_EINVAL, "n_levels must be in [2, 8]");
   require(level_sizes != nullptr && agg_ids != nullptr, MGPBD_EINVAL, "null hierarchy array");
   require(level_sizes[0] == nt_, MGPBD_EINVAL, "level_sizes[0] must equal nt");
@@ -201,6 +291,7 @@ void Solver::set_mesh(const float* x_ref, const float* invm, const int32_t* t_i,
   nt_ = nt;
   x_ = x;
   v_ = v;
+  matrix_mode_ = false;
   inited_ = false;
   user_sizes_.clear();
   user_aggs_.clear();
@@ -229,6 +320,10 @@ double Solver::finalize_read(const double* partials, int blocks) {
 // ---------------------------------------------------------------------------
 // MGPBDSolverGPU.init (cons/mgpbd_gpu.py:92-114)
 void Solver::init() {
+  if (matrix_mode_) {
+    init_matrix();
+    return;
+  }
   require(x_ && t_i_, MGPBD_ESTATE, "mgpbd_set_mesh has not been called");
   cudaStream_t s = stream_;
   if (!h_buf_) MGPBD_CUDA(cudaMallocHost(&h_buf_, sizeof(double) * 64));
@@ -382,7 +477,7 @@ void Solver::build_hierarchy(const std::vector<int32_t>& t_host, const std::vect
   if (!user_sizes_.empty()) {
     sizes = user_sizes_;
     aggs = user_aggs_;
-  } else {
+  } else if (!matrix_mode_) {
     tet_hierarchy(t_host.data(), nt_, max_coarse, 4, sizes, aggs);
   }
   std::vector<float> fine_vals = a0;
@@ -493,6 +588,7 @@ void Solver::alloc_work() {
   }
   // matrix-free operator data (used by the Chebyshev path and by
   // mgpbd_apply_matrix in every mode)
+  if (matrix_mode_) return;  // a caller's matrix has no operator data
   gV_.alloc(4LL * nt_);
   u_.alloc(nv_);
   jdinv_.alloc(nt_);
@@ -526,7 +622,7 @@ void Solver::alloc_work() {
 // y = A x on level 0: matrix-free from the current gradients, or the CSR
 // values of the last fill
 void Solver::apply_matrix(int matrix_free, const float* x, float* y) {
-  require_init();
+  require_mesh();
   if (matrix_free) {
     JView j = jview();
     if (matrix_free == 1) launch_jform_prepare(j, inc_ent_.p, gV_.p, jdinv_.p, gT_.p, stream_);
@@ -538,20 +634,20 @@ void Solver::apply_matrix(int matrix_free, const float* x, float* y) {
 
 // ---- adaptive zones ------------------------------------------------------
 void Solver::zone_proximity(int32_t* active, float cx, float cy, float cz, float radius) {
-  require_init();
+  require_mesh();
   require(active != nullptr, MGPBD_EINVAL, "active must be a device array of nt int32");
   launch_zone_proximity(t_i_, x_, nt_, cx, cy, cz, radius, active, stream_);
 }
 
 void Solver::zone_strain(int32_t* active, const float* x_old, float threshold, float dt) {
-  require_init();
+  require_mesh();
   require(active != nullptr, MGPBD_EINVAL, "active must be a device array of nt int32");
   require(dt > 0.0f, MGPBD_EINVAL, "dt must be positive");
   launch_zone_strain(t_i_, x_, x_old ? x_old : x_old_.p, nt_, threshold, dt, active, stream_);
 }
 
 void Solver::zone_expand(int32_t* active, int32_t n_rings) {
-  require_init();
+  require_mesh();
   require(active != nullptr && n_rings >= 0, MGPBD_EINVAL, "bad zone expansion arguments");
   if (!adj_ptr_.p) {
     std::vector<int32_t> t_host(4LL * nt_);
@@ -569,13 +665,13 @@ void Solver::zone_expand(int32_t* active, int32_t n_rings) {
 }
 
 void Solver::mask_alpha(const int32_t* active, float* saved) {
-  require_init();
+  require_mesh();
   require(active != nullptr && saved != nullptr, MGPBD_EINVAL, "bad alpha mask arguments");
   launch_mask_alpha(active, alpha_.p, saved, nt_, stream_);
 }
 
 void Solver::restore_alpha(const float* saved) {
-  require_init();
+  require_mesh();
   require(saved != nullptr, MGPBD_EINVAL, "saved must be a device array of nt float");
   MGPBD_CUDA(cudaMemcpyAsync(alpha_.p, saved, sizeof(float) * nt_, cudaMemcpyDeviceToDevice,
                              stream_));
@@ -651,7 +747,6 @@ void Solver::jform_setup() {
 // float32 copy of the float64 solution.
 int32_t Solver::pcg_cheb(const float* b, float* x) {
   cudaStream_t outer = stream_;
-  constexpr double kBarrierLimitS = 4.0;
   if (p_.persistent) {
     int32_t its = 0, left = p_.maxiter_cg;
     bool warm = false;
@@ -684,7 +779,7 @@ int32_t Solver::pcg_cheb(const float* b, float* x) {
       const double tol = std::max<double>(p_.primal_tol, p_.rel_tol_cg);
       MGPBD_CUDA(cudaEventRecord(ev_[0], outer));
       launch_pcg_primal(jview(), v, pplan_, jpart_.p, cg_state_.p, p_.tol_cg, tol, p_.maxiter_cg,
-                        p_.cheb_degree, p_.cheb_lo, kPrimalStall, kPrimalMaxAmp, kBarrierLimitS,
+                        p_.cheb_degree, p_.cheb_lo, kPrimalStall, kPrimalMaxAmp, barrier_limit_s_,
                         outer);
       MGPBD_CUDA(cudaEventRecord(ev_[1], outer));
       sync_read(h_state_, cg_state_.p, sizeof(CgState));
@@ -692,8 +787,10 @@ int32_t Solver::pcg_cheb(const float* b, float* x) {
       stats_.cg_launches += 1;
       stats_.cg_iters_warm += h_state_->iters;
       const uint32_t st = static_cast<uint32_t>(h_state_->status);
-      if (st & MGPBD_STATUS_SYNC_TIMEOUT)
+      if (st & MGPBD_STATUS_SYNC_TIMEOUT) {
+        status_ |= MGPBD_STATUS_SYNC_TIMEOUT;
         throw Error(MGPBD_ECUDA, "primal CG kernel: a grid barrier wait timed out");
+      }
       // the dual solve below decides convergence; keep only the alarms
       status_ |= st & (MGPBD_STATUS_NAN | MGPBD_STATUS_PAP_NONPOS);
       if (st & MGPBD_STATUS_NAN) return h_state_->iters;
@@ -723,13 +820,15 @@ int32_t Solver::pcg_cheb(const float* b, float* x) {
     v.ulo = primal() ? pv_[6].p : nullptr;  // the primal Kp vector, free by now
     MGPBD_CUDA(cudaEventRecord(ev_[0], outer));
     launch_jcg_persistent(jview(), v, jplan_, jpart_.p, jst_.p, cg_state_.p, p_.tol_cg,
-                          p_.rel_tol_cg, left, p_.cheb_degree, warm, kBarrierLimitS, outer);
+                          p_.rel_tol_cg, left, p_.cheb_degree, warm, barrier_limit_s_, outer);
     MGPBD_CUDA(cudaEventRecord(ev_[1], outer));
     sync_read(h_state_, cg_state_.p, sizeof(CgState));
     stats_.ms_dual += event_ms(ev_[0], ev_[1]);
     stats_.cg_launches += 1;
-    if (static_cast<uint32_t>(h_state_->status) & MGPBD_STATUS_SYNC_TIMEOUT)
+    if (static_cast<uint32_t>(h_state_->status) & MGPBD_STATUS_SYNC_TIMEOUT) {
+      status_ |= MGPBD_STATUS_SYNC_TIMEOUT;
       throw Error(MGPBD_ECUDA, "persistent CG kernel: a grid barrier wait timed out");
+    }
     status_ |= static_cast<uint32_t>(h_state_->status);
     return its + h_state_->iters;
   }
@@ -824,13 +923,13 @@ int32_t Solver::pcg_cheb(const float* b, float* x) {
 
 // ---------------------------------------------------------------------------
 void Solver::make_prediction() {
-  require_init();
+  require_mesh();
   launch_predict(x_, v_, x_old_.p, x_pred_.p, invm_, nv_, p_.dt, p_.gravity, p_.damp,
                  p_.kinematic_pins, stream_);
 }
 
 void Solver::update_vel() {
-  require_init();
+  require_mesh();
   launch_update_vel(x_, x_old_.p, v_, nv_, p_.dt, p_.damp, stream_);
 }
 
@@ -841,13 +940,13 @@ void Solver::step(int32_t frame) {
 }
 
 void Solver::compute_constraints() {
-  require_init();
+  require_mesh();
   launch_constraints(x_, t_i_, ctype_.p, dm_inv_.p, rest_vol_.p, nt_, C_.p, gradC_.p, stream_);
 }
 
 // _fill_A_and_update_gpu (cons/mgpbd_gpu.py:320-324)
 void Solver::fill_matrices() {
-  require_init();
+  require_mesh();
   if (cheb()) {
     // matrix-free: no CSR values; the gradients are the operator
     jform_setup();
@@ -902,7 +1001,7 @@ void Solver::factor_coarsest() {
 }
 
 double Solver::compute_rhs() {
-  require_init();
+  require_mesh();
   int blocks = reduce_blocks(nt_);
   launch_rhs(C_.p, alpha_.p, lambda_.p, nt_, rhs_.p, partials_.p, stream_);
   return std::sqrt(finalize_read(partials_.p, blocks));
@@ -1293,7 +1392,7 @@ int32_t Solver::pcg_graph(const float* b, float* x) {
 
 // _zero_dpos + _scatter_dlam_gpu (cons/mgpbd_gpu.py:330-355)
 void Solver::scatter(const float* dlam) {
-  require_init();
+  require_mesh();
   launch_lambda_update(lambda_.p, dlam, nt_, stream_);
   launch_scatter(inc_ptr_.p, inc_ent_.p, invm_, dlam, gradC_.p, dpos_.p, nv_, stream_);
 }
@@ -1305,7 +1404,7 @@ void Solver::scatter(const float* dlam) {
 // arithmetic as recomputing it); trials 2..10 are evaluated in one pass
 // only when trial 1 fails.
 double Solver::line_search() {
-  require_init();
+  require_mesh();
   cudaStream_t s = stream_;
   int blocks = reduce_blocks(nt_);
   h_buf_[0] = 1.0;
@@ -1332,14 +1431,14 @@ double Solver::line_search() {
 }
 
 void Solver::apply_dpos(double omega) {
-  require_init();
+  require_mesh();
   launch_apply(x_, dpos_.p, invm_, nv_, static_cast<float>(omega), stream_);
 }
 
 // MGPBDSolverGPU.solve (cons/mgpbd_gpu.py:397-446)
 void Solver::solve(int32_t frame) {
   (void)frame;
-  require_init();
+  require_mesh();
   status_ = 0;
   MGPBD_CUDA(cudaMemsetAsync(lambda_.p, 0, sizeof(float) * nt_, stream_));
   double r0 = 0.0;

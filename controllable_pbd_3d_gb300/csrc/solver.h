@@ -57,6 +57,20 @@ class Solver {
   void set_mesh(const float* x_ref, const float* invm, const int32_t* t_i, int32_t nv, int32_t nt,
                 float* x, float* v);
   void set_hierarchy(const int32_t* agg_ids, int32_t n_levels, const int32_t* level_sizes);
+  // GPUMultigridSolver.setup (cons/mgpcg_gpu.py:30-173) for a caller's
+  // level-0 matrix instead of a mesh: host CSR arrays, kept in the caller's
+  // column order; init() then builds the coarse levels of the hierarchy
+  // given by set_hierarchy (none: one level) and the V-cycle PCG solves it
+  void set_matrix(int32_t n, int64_t nnz, const int32_t* indptr, const int32_t* indices,
+                  const float* data);
+  // update_fine_matrix_data + update_all_coarse_matrices (cons/mgpcg_gpu.py:
+  // 175-212): new level-0 values (device, nnz), 1/diag and coarse refill
+  void update_matrix(const float* data);
+  // wait limit of the persistent CG kernels' grid barriers (seconds)
+  void set_barrier_limit(double seconds) {
+    require(seconds > 0.0 && seconds <= 60.0, MGPBD_EINVAL, "barrier limit must be in (0, 60] s");
+    barrier_limit_s_ = seconds;
+  }
   // per-constraint MGPBD_CONS_* types (host array of nt; nullptr: all ARAP)
   void set_constraint_types(const int32_t* types);
   void init();
@@ -110,6 +124,9 @@ class Solver {
 
  private:
   void require_init() const;
+  // the per-mesh stages need set_mesh (not a caller's matrix)
+  void require_mesh() const;
+  void init_matrix();
   void build_hierarchy(const std::vector<int32_t>& t_i_host, const std::vector<float>& a0);
   void alloc_work();
   // V-cycle on `l` with rhs b_l (device) and zero initial guess; the result
@@ -150,6 +167,10 @@ class Solver {
   float* v_ = nullptr;
   int32_t nv_ = 0, nt_ = 0;
   bool inited_ = false;
+  bool matrix_mode_ = false;     // set_matrix: a caller's level-0 matrix, no mesh
+  double barrier_limit_s_ = 4.0; // grid-barrier wait limit of the persistent kernels
+  Csr mat_csr_;                  // its structure and values (host)
+  std::vector<float> mat_vals_;
 
   DevBuf<float> x_old_, x_pred_, dpos_;
   DevBuf<float> dm_inv_, rest_vol_, alpha_, lambda_, C_, gradC_, rhs_, dlam_;

@@ -246,6 +246,21 @@ int mgpbd_set_mesh(mgpbd_handle h, const float* x_ref, const float* invm,
 int mgpbd_set_hierarchy(mgpbd_handle h, const int32_t* agg_ids, int32_t n_levels,
                         const int32_t* level_sizes);
 
+/* Replaces GPUMultigridSolver.setup (cons/mgpcg_gpu.py:30-173) for a
+ * caller's own level-0 matrix instead of a mesh: host CSR arrays (n rows,
+ * nnz entries, every row with its diagonal; the caller's column order is
+ * kept).  Then, optionally, mgpbd_set_hierarchy (the Ps of setup as
+ * aggregate ids: one 1 per row of each P) and mgpbd_init, which builds
+ * the Galerkin coarse levels; mgpbd_pcg / mgpbd_vcycle solve with it.  The
+ * handle has no mesh (mesh stages return MGPBD_ESTATE); the parameters
+ * must select the V-cycle (precond MGPBD_PRECOND_VCYCLE). */
+int mgpbd_set_matrix(mgpbd_handle h, int32_t n, int64_t nnz, const int32_t* indptr,
+                     const int32_t* indices, const float* data);
+/* Replaces update_fine_matrix_data + update_all_coarse_matrices
+ * (cons/mgpcg_gpu.py:175-212) of a mgpbd_set_matrix handle: new level-0
+ * values (device pointer, nnz, same pattern), 1/diag, coarse refill. */
+int mgpbd_update_matrix(mgpbd_handle h, const float* data);
+
 /* Constraint types.  The reference's step has one ARAP constraint per tet
  * (C = |S - I|_F, cons/mgpbd_gpu.py:226-247).  The library also takes, per
  * constraint, the two blocks of a length + volume discretisation:
@@ -265,6 +280,14 @@ int mgpbd_set_hierarchy(mgpbd_handle h, const int32_t* agg_ids, int32_t n_levels
  * MGPBD_CONS_* values), or NULL for all ARAP.  mgpbd_set_mesh clears it;
  * mgpbd_init validates it.  No counterpart in the reference. */
 int mgpbd_set_constraint_types(mgpbd_handle h, const int32_t* types);
+
+/* Wait limit, in seconds (0, 60], of every grid-barrier wait of the
+ * persistent CG kernels (default 4).  A wait that reaches it ends the
+ * kernel on every block, marks MGPBD_STATUS_SYNC_TIMEOUT and makes the call
+ * return MGPBD_ECUDA; the next launch starts afresh, so the handle stays
+ * usable.  A very short limit makes a solve fail this way on purpose (how
+ * the tests exercise the path).  No counterpart in the reference. */
+int mgpbd_set_barrier_limit(mgpbd_handle h, double seconds);
 
 /* Replaces MGPBDSolverGPU.init (cons/mgpbd_gpu.py:92-114): rest shape,
  * sparsity pattern, first A, tet hierarchy, multigrid setup. */
