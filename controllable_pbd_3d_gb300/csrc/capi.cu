@@ -116,6 +116,7 @@ void mgpbd_default_params(mgpbd_params* p) {
   p->primal_tol = 1e-2f;
   p->learned_accept = 0.1f;
   p->learned_stall = 1000;
+  p->cheb_scale = MGPBD_CHEB_JACOBI;
 }
 
 const char* mgpbd_strerror(int code) {

@@ -25,7 +25,8 @@ __global__ void k_jprep(const int32_t* __restrict__ inc_ent, int64_t ne,
                         const float* __restrict__ gradC, const int4* __restrict__ t_i,
                         const float* __restrict__ invm, const float* __restrict__ alpha,
                         int32_t nt, float4* __restrict__ gV, float* __restrict__ dinv,
-                        float4* __restrict__ gT, int32_t n4, float4* __restrict__ gE) {
+                        float4* __restrict__ gT, int32_t n4, float4* __restrict__ gE,
+                        int unit_dinv) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < ne; k += stride) {
     const int32_t e = inc_ent[k];
@@ -41,7 +42,7 @@ __global__ void k_jprep(const int32_t* __restrict__ inc_ent, int64_t ne,
     for (int l = 0; l < 4; ++l)
       d += w[l] * (g[3 * l] * g[3 * l] + g[3 * l + 1] * g[3 * l + 1] + g[3 * l + 2] * g[3 * l + 2]);
     d += alpha[t];
-    dinv[t] = fabsf(d) > 1e-30f ? 1.0f / d : 0.0f;
+    dinv[t] = unit_dinv ? 1.0f : (fabsf(d) > 1e-30f ? 1.0f / d : 0.0f);
     if (gT) {
       const float4* g4 = reinterpret_cast<const float4*>(g);
       gT[t] = g4[0];
@@ -428,10 +429,10 @@ TArgs targs(const JView& j) {
 }  // namespace
 
 void launch_jform_prepare(const JView& j, const int32_t* inc_ent, float4* gV, float* dinv,
-                          float4* gT, cudaStream_t s) {
+                          float4* gT, bool unit_dinv, cudaStream_t s) {
   int g = tgrid(std::max<int64_t>(j.ne, j.nt));
   k_jprep<<<g, kT, 0, s>>>(inc_ent, j.ne, j.gradC, reinterpret_cast<const int4*>(j.t_i), j.invm,
-                           j.alpha, j.nt, gV, dinv, gT, j.n4, j.gE);
+                           j.alpha, j.nt, gV, dinv, gT, j.n4, j.gE, unit_dinv ? 1 : 0);
   MGPBD_CHECK_LAUNCH();
 }
 

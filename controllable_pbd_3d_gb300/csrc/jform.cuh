@@ -64,12 +64,13 @@ struct JView {
   const int2* qE = nullptr;
 };
 
-// gV[k] = (gradC[inc_ent[k]], tet id) and 1/diag(A) per tet; with gT, also
+// gV[k] = (gradC[inc_ent[k]], tet id) and 1/diag(A) per tet (1 with
+// unit_dinv: the unscaled Chebyshev base); with gT, also
 // the gradients as three planes (gT[t], gT[nt + t], gT[2 nt + t] = the
 // float4s 0, 1, 2 of tet t), so a warp's loads of one float4 per tet are
 // contiguous
 void launch_jform_prepare(const JView& j, const int32_t* inc_ent, float4* gV, float* dinv,
-                          float4* gT, cudaStream_t s);
+                          float4* gT, bool unit_dinv, cudaStream_t s);
 // y = A x (plain), for tests and the power iteration
 void launch_jform_apply(const JView& j, const float* x, float* y, cudaStream_t s);
 // `steps` Lanczos steps on S = D^-1/2 A D^-1/2 from a fixed start vector;

@@ -625,7 +625,9 @@ void Solver::apply_matrix(int matrix_free, const float* x, float* y) {
   require_mesh();
   if (matrix_free) {
     JView j = jview();
-    if (matrix_free == 1) launch_jform_prepare(j, inc_ent_.p, gV_.p, jdinv_.p, gT_.p, stream_);
+    if (matrix_free == 1)
+      launch_jform_prepare(j, inc_ent_.p, gV_.p, jdinv_.p, gT_.p,
+                           p_.cheb_scale == MGPBD_CHEB_UNSCALED, stream_);
     launch_jform_apply(j, x, y, stream_);
   } else {
     launch_spmv(levels_[0].view(), x, y, stream_);
@@ -723,14 +725,15 @@ JVecs Solver::jvecs(const float* b, float* x) {
   return v;
 }
 
-// Per Newton iteration: vertex-major gradients, 1/diag(A), lambda_max of
-// D^-1 A by 24 Lanczos steps (upper end taken 2% above the Ritz value; a
+// Per Newton iteration: vertex-major gradients, 1/diag(A) (all ones for the
+// unscaled base), lambda_max of D^-1 A by 24 Lanczos steps (upper end taken 2% above the Ritz value; a
 // Chebyshev interval that misses the top of the spectrum makes the
 // preconditioner indefinite) and the Chebyshev coefficients.
 void Solver::jform_setup() {
   constexpr int kSteps = 24;
   JView j = jview();
-  launch_jform_prepare(j, inc_ent_.p, gV_.p, jdinv_.p, gT_.p, stream_);
+  launch_jform_prepare(j, inc_ent_.p, gV_.p, jdinv_.p, gT_.p,
+                       p_.cheb_scale == MGPBD_CHEB_UNSCALED, stream_);
   launch_jform_lanczos(j, pw_v_.p, jd_.p, pw_w_.p, partials_.p, jst_.p, kSteps, stream_);
   static_assert(2 * kMaxLanczos <= 64, "h_buf_ holds the Lanczos coefficients");
   MGPBD_CUDA(cudaMemcpyAsync(h_buf_, jst_.p->lz_a, sizeof(double) * kMaxLanczos,

@@ -86,7 +86,9 @@ class MGPBDSolverGPU:
     compliance     > 0: alpha~ = compliance / dt^2 for every tet;
     precond        'vcycle' (reference) or 'cheb' (FAST only: Chebyshev
                    polynomial of degree cheb_degree on [lmax*cheb_lo, lmax],
-                   matrix-free operator, no CSR assembly) or 'learned' (the
+                   matrix-free operator, no CSR assembly; cheb_scale
+                   'jacobi' builds it on D^-1 A, 'none' on A itself) or
+                   'learned' (the
                    V-cycle with its coarse sweeps replaced by the linear
                    correction w * r / diag(A_c), w from a trained CoarseNet
                    attached with set_coarse_net; the plain V-cycle judges it
@@ -114,7 +116,8 @@ class MGPBDSolverGPU:
                aggregation='tet', benchmark=None, *, mode='parity', rel_tol_cg=0.0,
                coarse_solver='jacobi', smoother='jacobi', max_levels=0, max_coarse=400,
                kinematic_pins=False, coarse_sweeps=0, cg_alias=False, compliance=0.0,
-               precond='vcycle', cheb_degree=8, cheb_lo=0.01, use_graph=True,
+               precond='vcycle', cheb_degree=8, cheb_lo=0.01, cheb_scale='jacobi',
+               use_graph=True,
                persistent=True, primal=False, primal_tol=1e-2, learned_accept=0.1, learned_stall=1000,
                constraints='arap', check_finite=True):
     if aggregation != 'tet':
@@ -201,6 +204,7 @@ class MGPBDSolverGPU:
     p.precond = {'vcycle': 0, 'cheb': 1, 'learned': 2}[precond]
     p.cheb_degree = int(cheb_degree)
     p.cheb_lo = float(cheb_lo)
+    p.cheb_scale = {'jacobi': 0, 'none': 1}[cheb_scale]
     p.use_graph = int(bool(use_graph))
     p.persistent = int(persistent)  # True / 1, 2 (unstaged) or False / 0
     p.primal = int(bool(primal))

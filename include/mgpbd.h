@@ -150,7 +150,20 @@ typedef struct mgpbd_params {
    * and NaN still fall back).  CG residual norms plateau for a few hundred
    * iterations in ordinary solves of stiff bodies. */
   int32_t learned_stall;
+  /* MGPBD_PRECOND_CHEB: the base the Chebyshev polynomial is built on.
+   * MGPBD_CHEB_JACOBI (0, default): a polynomial in D^-1 A, D = diag(A).
+   * MGPBD_CHEB_UNSCALED (1): a polynomial in A itself.  With one compliance
+   * for every constraint, the null space of J^T (most of constraint space
+   * when constraints outnumber vertex coordinates) is the single eigenvalue
+   * alpha~ of A; Jacobi scaling spreads it over alpha~ / d_i, and with
+   * gradients of very different sizes (volume vs length constraints) that
+   * band sits at the bottom of the spectrum, where CG pays for it.  No
+   * counterpart in the reference. */
+  int32_t cheb_scale;
 } mgpbd_params;
+
+#define MGPBD_CHEB_JACOBI 0
+#define MGPBD_CHEB_UNSCALED 1
 
 #define MGPBD_PRECOND_VCYCLE 0
 #define MGPBD_PRECOND_CHEB 1

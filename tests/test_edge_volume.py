@@ -156,6 +156,16 @@ VARIANTS = {
     'fast-primal-l2': dict(mode='fast', precond='cheb', cheb_lo=1e-3, primal=True,
                            primal_tol=1e-2, persistent=2),
     'fast-dual-l2': dict(mode='fast', precond='cheb', cheb_lo=1e-3, primal=False, persistent=2),
+    # the Chebyshev polynomial on A itself (no Jacobi scaling): staged, from
+    # L2, with the primal warm start, and as per-phase kernels
+    'fast-unscaled': dict(mode='fast', precond='cheb', cheb_lo=1e-3, cheb_scale='none',
+                          primal=False),
+    'fast-unscaled-l2': dict(mode='fast', precond='cheb', cheb_lo=1e-3, cheb_scale='none',
+                             primal=False, persistent=2),
+    'fast-unscaled-primal': dict(mode='fast', precond='cheb', cheb_lo=1e-3, cheb_scale='none',
+                                 primal=True, primal_tol=1e-2),
+    'fast-unscaled-kernels': dict(mode='fast', precond='cheb', cheb_lo=1e-3, cheb_scale='none',
+                                  primal=False, persistent=0),
 }
 
 
