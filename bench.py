@@ -171,6 +171,16 @@ CONSTRAINT_NAMES = {'edge_volume': 'one length constraint per tet edge + one vol
                     'arap': 'one ARAP constraint per tet (the reference step)'}
 
 
+def bench_config(args, ws, n_verts, n_tets, n_cons, nnz0, compliance):
+  """The workload's description, the same dict in both arms."""
+  return {'workload': f'{args.size}^3 hex cube, 5 tets/hex', 'n_verts': int(n_verts),
+          'n_tets': int(n_tets), 'constraints': CONSTRAINT_NAMES[args.constraints],
+          'n_constraints': int(n_cons), 'nnz_level0': int(nnz0), 'compliance': compliance,
+          'dt': DT, 'rel_res_cg': 1e-6,
+          'l2': 'GPU arm: flushed between timed substeps (256 MB write, inside the timed region)',
+          'parallelism': f'replicas{ws}'}
+
+
 def make_solver(torch, n, kw, constraints='edge_volume'):
   from controllable_pbd_3d_gb300.mgpbd_gpu import MGPBDSolverGPU
   xr, x0, t, invm, compliance = workload(n)
@@ -405,52 +415,89 @@ def roofline_csr(torch, s, hbm_peak, peak_kind, reps=40):
   return roof
 
 
-# Newton iterations per substep and CG iterations per Newton iteration of
-# the plain AMG-PCG on the 40^3 workload, per constraint construction
-# (GB300 runs; ARAP: every substep runs the full 20 Newton iterations at
-# 1877-2138 CG iterations, mean 1970; length + volume: 2 Newton iterations
-# at ~2577 CG iterations).  The GPU arm re-measures both every run from its
-# plain leg; the reference arm, which has no GPU, uses these.
-PLAIN_CG_PER_NEWTON = {'arap': 1970, 'edge_volume': 2577}
-NEWTON_PER_SUBSTEP = {'arap': 20, 'edge_volume': 2}
+def cpu_model():
+  """The host CPU's model name (lscpu, else /proc/cpuinfo), for the record."""
+  try:
+    out = subprocess.run(['lscpu'], capture_output=True, text=True, timeout=10).stdout
+    for ln in out.splitlines():
+      if ln.lower().startswith('model name'):
+        return ln.split(':', 1)[1].strip()
+  except (OSError, subprocess.SubprocessError):
+    pass
+  try:
+    for ln in open('/proc/cpuinfo'):
+      if ln.lower().startswith(('model name', 'cpu part')):
+        return ln.split(':', 1)[1].strip()
+  except OSError:
+    pass
+  return 'unknown'
 
 
-class CpuSampler:
-  """The OpenMP CPU port of the plain MGPBD step (oracle/cpu_step.cpp) on
-  the same workload, all host threads.  One sample = one Newton iteration
-  of substep 0 with its CG capped at `cg_sample` iterations: constraints,
-  residual, matrix fill, Galerkin refill, smoother weights, the CG
-  iterations, scatter, line search, apply.  A substep is then
-  newton_per_substep x (non-CG time + cg_per_newton x time per CG iteration)."""
+# CG iteration cap of the CPU substeps: far above what a solve to 1e-6 takes
+# on this workload (~2,500-3,000), so it never decides a timing
+CPU_MAXITER_CG = 100000
+# seconds of whole CPU substeps the CPU legs time (at least one substep)
+CPU_BUDGET_S = 120.0
 
-  def __init__(self, n, cg_sample=20, constraints='edge_volume'):
+
+class CpuSubsteps:
+  """Whole substeps of the plain MGPBD step on the host cores: the OpenMP
+  CPU port of the reference algorithm (oracle/cpu_step.cpp, all host
+  threads) on the same workload.  A substep is the prediction, every Newton
+  iteration (constraints, residual, matrix fill, Galerkin refill, smoother
+  weights, V-cycle PCG to relative residual 1e-6, scatter, line search,
+  apply) until the Newton test holds, and the velocity update.  The
+  constraint set, its CSR pattern, the tet aggregation and the Galerkin
+  structure come from the oracle's restatement (oracle/mgpbd_oracle.py);
+  no library of the product is loaded."""
+
+  def __init__(self, n, constraints='edge_volume'):
+    from oracle import mgpbd_oracle as MO
     from oracle.cpu_port import CpuPort, threads
     xr, x0, t, invm, compliance = workload(n)
-    self.cg_sample = cg_sample
     ctype = agg = None
+    t0 = time.perf_counter()
     if constraints == 'edge_volume':
-      from controllable_pbd_3d_gb300.edge_volume import edge_volume_hierarchy, edge_volume_system
-      c, ctype, _, _ = edge_volume_system(t)
-      agg = edge_volume_hierarchy(t)
+      c, ctype, _, _ = MO.edge_volume_system(t)
+      aggs, _ = MO.edge_volume_hierarchy(t)
+      agg = aggs[0] if aggs else None
       t = c
     self.port = CpuPort(x0, xr, invm, t, [0.0, -9.8, 0.0], DT, compliance=compliance,
-                        maxiter=20, atol=1e-4, rtol=1e-2, maxiter_cg=cg_sample, tol_cg=1e-12,
-                        rel_tol_cg=1e-6, n_smooth=2, kinematic_pins=True, ctype=ctype,
+                        maxiter=SOLVER_KW['maxiter'], atol=SOLVER_KW['atol'],
+                        rtol=SOLVER_KW['rtol'], maxiter_cg=CPU_MAXITER_CG,
+                        tol_cg=SOLVER_KW['tol_cg'], rel_tol_cg=SOLVER_KW['rel_tol_cg'],
+                        n_smooth=SOLVER_KW['n_smooth'], kinematic_pins=True, ctype=ctype,
                         hierarchy=agg)
+    self.setup_s = time.perf_counter() - t0
     self.threads = threads()
-    from oracle.cpu_port import lib
-    lib().cpu_predict(self.port.h)
 
-  def sample(self):
-    import ctypes as C_
-    r0 = C_.c_double(0.0)
-    _, out = self.port.newton_iteration(0, r0, self.cg_sample)
-    t_cg = out[5] / max(out[1], 1.0)
-    t_other = out[3] + out[4] + out[6]
-    return t_other, t_cg, int(out[1])
+  def run(self, max_steps, budget_s):
+    """Time whole substeps, one after another from substep 0, until
+    max_steps are done or the time spent reaches budget_s (at least one).
+    Returns (seconds per substep, substeps timed, Newton iterations and CG
+    iterations per substep)."""
+    times, newton, cg = [], [], []
+    while len(times) < max(1, max_steps):
+      t0 = time.perf_counter()
+      self.port.step()
+      times.append(time.perf_counter() - t0)
+      log = self.port.log  # one row per residual check; solves have PCG time
+      newton.append(sum(1 for r in log if r[5] > 0))
+      cg.append(sum(r[1] for r in log))
+      if sum(times) >= budget_s:
+        break
+    k = len(times)
+    return sum(times) / k, k, sum(newton) / k, sum(cg) / k
 
-  def substeps_per_s(self, t_other, t_cg, cg_per_newton, newton_per_substep):
-    return 1.0 / (newton_per_substep * (t_other + cg_per_newton * t_cg))
+
+def cpu_line(sub, per_step, k, newton, cg):
+  return {'value': round(1.0 / per_step, 6), 'unit': UNIT, 'cores': sub.threads, 'kind': 'port',
+          'cpu_model': cpu_model(),
+          'sample': f'{k} whole substep(s) from substep 0, timed one by one: {newton:g} Newton '
+                    f'iterations and {cg:.0f} CG iterations (V-cycle PCG to relative residual '
+                    f'1e-6) per substep, {per_step:.1f} s each; OpenMP CPU port of the plain '
+                    f'step (oracle/cpu_step.cpp), {sub.threads} host threads; structure built by '
+                    f'the oracle in {sub.setup_s:.1f} s (not timed)'}
 
 
 def net_forward_bytes(n, nnz):
@@ -547,27 +594,28 @@ def fast_kw(args):
 
 
 def plain_leg(torch, args, hbm, kind, constraints):
-  """The plain float32 AMG-PCG on the same workload (fewer steps: it is
-  slow), its row-kernel tile shapes picked by the autotuner."""
+  """The plain float32 AMG-PCG on the same workload: the reference's
+  V-cycle PCG on CSR matrices, each CG solve one CUDA graph with a
+  device-side loop, its row-kernel tile shapes picked by the autotuner.
+  The length + volume body warms up like the fast leg (3 substeps) and
+  times --plain-steps substeps (default 3); every ARAP substep runs the
+  full 20 Newton iterations (~25 s), so ARAP times one substep."""
   kwp = dict(SOLVER_KW)
   kwp.update(PLAIN_KW)
   sp_, _, _ = make_solver(torch, args.size, kwp, constraints)
   shapes = sp_.autotune(reps=5)
-  # the same substeps as the fast leg where that is affordable: the length +
-  # volume body needs 2 Newton iterations in substep 0 and 1 later (warm up
-  # like the fast leg, ~6 s a substep); every ARAP substep runs the full 20
-  # Newton iterations (~36 s), so ARAP times its first substep
   warm = 0 if constraints == 'arap' else min(args.warmup, 3)
   for i in range(warm):
     sp_.step(i)
-  k_plain = max(1, min(args.steps, args.plain_steps))
+  k_plain = 1 if constraints == 'arap' else max(1, args.plain_steps)
   tp, stp = time_steps(torch, sp_, k_plain, warm)
   roof_csr = roofline_csr(torch, sp_, hbm, kind)
   plain = {'value': round(k_plain / tp, 4), 'unit': UNIT, 'steps': k_plain, 'warmup': warm,
            'newton_iters_per_step': sum(x['newton_iters'] for x in stp) / k_plain,
            'cg_iters_per_step': sum(x['cg_iters_total'] for x in stp) / k_plain,
-           'config': 'parity-mode CSR V-cycle (2-level tet aggregation, 50 coarse Jacobi '
-                     'sweeps, smoother weight min(2/3, 4/(3 lambda_max))), host-checked loops',
+           'config': 'CSR V-cycle PCG (2-level tet aggregation, 50 coarse Jacobi sweeps, '
+                     'smoother weight min(2/3, 4/(3 lambda_max))), each CG solve one CUDA '
+                     'graph with a device-side WHILE loop',
            'row_shapes': {str(l): c for l, c in shapes.items()},
            'row_shape_us': {str(l): round(t, 2) for l, (_, t) in sp_.last_tuning.items()},
            'roofline': roof_csr}
@@ -636,14 +684,10 @@ def run_ours(args):
       'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(t_max * 1e3 / args.steps, 3),
       'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
       'data': 'synthetic (seeded hex-grid cube; reference meshes unavailable)',
-      'config': {'workload': f'{args.size}^3 hex cube, 5 tets/hex', 'n_verts': n_verts,
-                 'n_tets': n_tets, 'constraints': CONSTRAINT_NAMES[cons],
-                 'n_constraints': n_cons, 'nnz_level0': st0['nnz'][0], 'levels': st0['rows'],
-                 'compliance': compliance, 'dt': DT, 'rel_res_cg': 1e-6, 'mode': 'fast',
-                 'solver': ('primal warm start + dual persistent Chebyshev-8 CG'
-                            if kw.get('primal') else 'dual persistent Chebyshev-8 CG'),
-                 'l2': 'flushed between timed substeps (256 MB write, inside the timed region)',
-                 'parallelism': f'replicas{ws}'},
+      'config': bench_config(args, ws, n_verts, n_tets, n_cons, st0['nnz'][0], compliance),
+      'solver': ('FAST: primal warm start + dual persistent Chebyshev-8 CG'
+                 if kw.get('primal') else 'FAST: dual persistent Chebyshev-8 CG'),
+      'levels': [int(r) for r in st0['rows'] if r],
       'newton_iters_per_step': newton / args.steps, 'cg_iters_per_step': cg / args.steps,
       'cg_iters_per_s': round(ws * cg / t_max, 1), 'gpu_launches': int(launches),
       'clocks': clk.summary(), 'e2e': e2e, 'roofline': roof,
@@ -677,22 +721,9 @@ def run_ours(args):
       arap['speedup_vs_plain'] = round(arap['value'] / arap['plain_fp32_amg_pcg']['value'], 2)
     out['arap'] = arap
   if rank == 0 and not args.no_cpu_baseline:
-    cpu = CpuSampler(args.size, constraints=cons)
-    cpu.sample()  # warm-up (first-touch of the host arrays)
-    t_other, t_cg, n_cg = cpu.sample()
-    if plain is not None:
-      newton_ps = max(plain['newton_iters_per_step'], 1.0)
-      cg_per_newton = plain['cg_iters_per_step'] / newton_ps
-    else:
-      newton_ps, cg_per_newton = NEWTON_PER_SUBSTEP[cons], PLAIN_CG_PER_NEWTON[cons]
-    out['cpu_baseline'] = {
-        'value': round(cpu.substeps_per_s(t_other, t_cg, cg_per_newton, newton_ps), 6),
-        'unit': UNIT, 'cores': cpu.threads, 'kind': 'port',
-        'sample': f'OpenMP CPU port of the plain step (oracle/cpu_step.cpp), one Newton '
-                  f'iteration of substep 0 with {n_cg} CG iterations: {t_other:.2f} s outside '
-                  f'CG + {t_cg * 1e3:.1f} ms per CG iteration, scaled to '
-                  f'{newton_ps:g} x ({cg_per_newton:.0f} CG iterations + the rest) per '
-                  'substep; setup excluded'}
+    sub = CpuSubsteps(args.size, cons)
+    per, k, newton_c, cg_c = sub.run(1, CPU_BUDGET_S)
+    out['cpu_baseline'] = cpu_line(sub, per, k, newton_c, cg_c)
   if rank == 0:
     print(json.dumps(out), flush=True)
   if ws > 1:
@@ -842,39 +873,32 @@ def run_slab(args):
 
 
 def run_reference(args):
-  """The reference algorithm on the host cores: the OpenMP CPU port of the
-  plain step (the reference itself needs Taichi, which is not available).
-  Each step is one bounded sample (CpuSampler.sample)."""
+  """The reference algorithm on the host cores (the reference itself needs
+  Taichi, absent here): whole substeps of the OpenMP CPU port of the plain
+  step, from substep 0, as many as fit in CPU_BUDGET_S (at least one; a
+  40^3 substep takes about two minutes on 16 Arm cores).  `steps` is the
+  number of substeps actually timed, `steps_requested` the --steps asked
+  for.  One JSON line on rank 0; other ranks exit."""
   ws = int(os.environ.get('WORLD_SIZE', '1'))
   rank = int(os.environ.get('RANK', '0'))
   if rank != 0:
     return
-  cons = args.constraints
-  cpu = CpuSampler(args.size, constraints=cons)
-  others, cgs = [], []
-  t0 = time.perf_counter()
-  for i in range(args.warmup + args.steps):
-    t_other, t_cg, n_cg = cpu.sample()
-    if i >= args.warmup:
-      others.append(t_other)
-      cgs.append(t_cg)
-  wall = time.perf_counter() - t0
-  t_other, t_cg = float(np.mean(others)), float(np.mean(cgs))
-  value = cpu.substeps_per_s(t_other, t_cg, PLAIN_CG_PER_NEWTON[cons], NEWTON_PER_SUBSTEP[cons])
-  sample = (f'per step: one Newton iteration of substep 0 with {n_cg} CG iterations '
-            f'({t_other:.2f} s outside CG + {t_cg * 1e3:.1f} ms per CG iteration); value scaled '
-            f'to {NEWTON_PER_SUBSTEP[cons]} x ({PLAIN_CG_PER_NEWTON[cons]} CG iterations + the '
-            'rest) per substep; OpenMP CPU port of the plain step, all host threads')
-  out = {'metric': METRIC, 'value': round(value, 6), 'unit': UNIT, 'n_gpus': ws,
-         'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(1e3 / value, 1),
-         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
-         'data': 'synthetic (seeded hex-grid cube)', 'impl': 'reference',
-         'config': {'workload': f'{args.size}^3 hex cube, 5 tets/hex', 'rel_res_cg': 1e-6,
-                    'constraints': CONSTRAINT_NAMES[cons], 'sample_wall_s': round(wall, 1)},
-         'cpu_baseline': {'value': round(value, 6), 'unit': UNIT, 'cores': cpu.threads,
-                          'kind': 'port', 'sample': sample},
-         'e2e': {'value': round(value, 6), 'unit': UNIT, 'h2d_bytes_per_step': 0,
-                 'd2h_bytes_per_step': 0}}
+  sub = CpuSubsteps(args.size, args.constraints)
+  per, k, newton_c, cg_c = sub.run(args.steps, CPU_BUDGET_S)
+  port = sub.port
+  cpu = cpu_line(sub, per, k, newton_c, cg_c)
+  value = cpu['value']
+  out = {'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': ws, 'steps': k,
+         'steps_requested': args.steps, 'warmup': 0, 'warmup_requested': args.warmup,
+         'ms_per_step': round(per * 1e3, 1), 'higher_is_better': True, 'scaling': 'weak',
+         'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded hex-grid cube)',
+         'impl': 'reference',
+         'config': bench_config(args, ws, port.nv, port.n_mesh_tets, port.nt, port.nnz0,
+                                port.compliance),
+         'solver': 'plain FP32 AMG-PCG (two-level tet-aggregation V-cycle PCG), OpenMP CPU port',
+         'newton_iters_per_step': newton_c, 'cg_iters_per_step': cg_c,
+         'cpu_baseline': cpu,
+         'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
   print(json.dumps(out), flush=True)
 
 
@@ -887,7 +911,7 @@ def main():
   ap.add_argument('--size', type=int, default=40)
   ap.add_argument('--no-cpu-baseline', action='store_true')
   ap.add_argument('--no-plain', action='store_true')
-  ap.add_argument('--plain-steps', type=int, default=1)
+  ap.add_argument('--plain-steps', type=int, default=3)
   ap.add_argument('--no-learned', action='store_true')
   ap.add_argument('--no-arap', action='store_true')
   # the constraint construction of the headline workload

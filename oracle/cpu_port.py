@@ -87,8 +87,11 @@ class CpuPort:
                           t.ctypes.data, dt, mu, compliance, damp, g.ctypes.data, maxiter, atol,
                           rtol, maxiter_cg, tol_cg, rel_tol_cg, n_smooth, omega_jacobi,
                           int(bool(kinematic_pins)), None if ct is None else ct.ctypes.data)
+    self.compliance = float(compliance)
+    self.n_mesh_tets = self.nt if ctype is None else int(np.sum(np.asarray(ctype) != 1))
     # structure from the oracle restatement
     ip, ix = orc.sparsity_pattern(t, self.nt)
+    self.nnz0 = int(len(ix))
     L.cpu_add_level(self.h, self.nt, ip.ctypes.data, ix.ctypes.data, len(ix), None, None, None)
     if hierarchy is not None:
       aggs, sizes = [np.asarray(hierarchy)], [self.nt, int(np.max(hierarchy)) + 1]

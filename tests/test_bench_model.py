@@ -104,3 +104,23 @@ def test_reference_arm_prints_one_contract_line():
   assert cb['value'] == d['value'] and cb['kind'] == 'port' and cb['cores'] >= 1 and cb['sample']
   assert d['e2e'] == {'value': d['value'], 'unit': d['unit'], 'h2d_bytes_per_step': 0,
                       'd2h_bytes_per_step': 0}
+  # whole substeps actually timed, the workload described as the GPU arm does
+  assert d['steps'] >= 1 and d['steps_requested'] == 1 and cb['cpu_model']
+  assert 'whole substep' in cb['sample']
+  assert set(d['config']) == {'workload', 'n_verts', 'n_tets', 'constraints', 'n_constraints',
+                              'nnz_level0', 'compliance', 'dt', 'rel_res_cg', 'l2',
+                              'parallelism'}
+  assert d['config']['n_tets'] == 5000 and d['config']['n_constraints'] == 11930
+
+
+def test_cpu_substeps_load_no_product_library():
+  """The CPU legs build their structure with the oracle: libmgpbd.so is
+  never mapped into the process."""
+  import subprocess
+  import sys
+  from conftest import ROOT
+  code = ('import bench; s = bench.CpuSubsteps(5); s.run(1, 0.0); '
+          'print(open("/proc/self/maps").read().count("libmgpbd"))')
+  out = subprocess.run([sys.executable, '-c', code], cwd=ROOT, capture_output=True, text=True,
+                       timeout=600, check=True).stdout.strip().splitlines()
+  assert out[-1] == '0'
