@@ -60,14 +60,14 @@ def workload(n, seed=0):
 # substep for the fast step)
 SOLVER_KW = dict(damp=1.0, maxiter=20, atol=1e-4, rtol=1e-2, maxiter_cg=6000, tol_cg=1e-12,
                  rel_tol_cg=1e-6, n_smooth=2, kinematic_pins=True)
-# the optimised step: each CG solve is a primal (Woodbury) warm start to a
-# 1e-2 dual residual, then CG on the dual system to 1e-6, each one
-# cooperative persistent kernel (matrix-free operator, degree-8 Chebyshev
-# preconditioners; the operator data is staged in shared memory where a
-# block's share fits, as for the ARAP body, and read through L2 otherwise,
-# as for the length + volume body)
-FAST_KW = dict(mode='fast', precond='cheb', cheb_degree=8, cheb_lo=1e-3, primal=True,
-               primal_tol=1e-2)
+# the optimised step: each CG solve is one cooperative persistent kernel on
+# the dual system, preconditioned by a degree-8 Chebyshev polynomial in A
+# itself (matrix-free operator; no Jacobi scaling, which would spread the
+# single alpha~ eigenvalue of the null space of J^T); the operator data is
+# staged in shared memory where a block's share fits, as for the ARAP body,
+# and read through L2 otherwise, as for the length + volume body
+FAST_KW = dict(mode='fast', precond='cheb', cheb_degree=8, cheb_lo=1e-3, cheb_scale='none',
+               primal=False)
 # the plain float32 AMG-PCG: the reference's two-level tet-aggregation V-cycle
 # PCG on CSR matrices (smoother weight capped at 4/(3 lambda_max) because
 # omega = 2/3 diverges at this stiffness), each CG solve one CUDA graph with
@@ -685,8 +685,8 @@ def run_ours(args):
       'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
       'data': 'synthetic (seeded hex-grid cube; reference meshes unavailable)',
       'config': bench_config(args, ws, n_verts, n_tets, n_cons, st0['nnz'][0], compliance),
-      'solver': ('FAST: primal warm start + dual persistent Chebyshev-8 CG'
-                 if kw.get('primal') else 'FAST: dual persistent Chebyshev-8 CG'),
+      'solver': ('FAST: primal warm start + ' if kw.get('primal') else 'FAST: ') +
+                f'dual persistent Chebyshev-8 CG on {"D^-1 A" if kw.get("cheb_scale") == "jacobi" else "A"}',
       'levels': [int(r) for r in st0['rows'] if r],
       'newton_iters_per_step': newton / args.steps, 'cg_iters_per_step': cg / args.steps,
       'cg_iters_per_s': round(ws * cg / t_max, 1), 'gpu_launches': int(launches),

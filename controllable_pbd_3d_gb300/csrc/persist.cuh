@@ -49,7 +49,8 @@ __device__ __forceinline__ void fence_acq_rel() { asm volatile("fence.acq_rel.gp
 // are released), polls with relaxed loads and ends with an acquire fence
 // before the closing bar.sync; the block that arrives last skips the poll.
 // Returns false in all threads of the block if the wait gave up (limit
-// reached, or another block gave up); the failure is recorded in gs->err
+// reached, or another block gave up; spin_ns = 0 gives up at once when
+// another block has not arrived yet); the failure is recorded in gs->err
 // and as MGPBD_STATUS_SYNC_TIMEOUT in *status_word.
 __device__ __forceinline__ bool grid_sync(GridSync* gs, int32_t* status_word,
                                           unsigned long long spin_ns, unsigned long long& gen) {
@@ -64,7 +65,9 @@ __device__ __forceinline__ bool grid_sync(GridSync* gs, int32_t* status_word,
       const unsigned long long t0 = global_ns();
       unsigned int n = 0;
       while (ld_relaxed(&gs->count) < target) {
-        if ((++n & 63u) == 0) {
+        // the limit is checked every 64 polls; a limit of 0 gives up at the
+        // first poll that finds the barrier incomplete
+        if ((++n & 63u) == 0 || spin_ns == 0) {
           if (ld_relaxed(&gs->err) != 0u || global_ns() - t0 > spin_ns) {
             ok = 0;
             break;

@@ -68,7 +68,7 @@ class Solver {
   void update_matrix(const float* data);
   // wait limit of the persistent CG kernels' grid barriers (seconds)
   void set_barrier_limit(double seconds) {
-    require(seconds > 0.0 && seconds <= 60.0, MGPBD_EINVAL, "barrier limit must be in (0, 60] s");
+    require(seconds >= 0.0 && seconds <= 60.0, MGPBD_EINVAL, "barrier limit must be in [0, 60] s");
     barrier_limit_s_ = seconds;
   }
   // per-constraint MGPBD_CONS_* types (host array of nt; nullptr: all ARAP)

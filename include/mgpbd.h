@@ -294,12 +294,13 @@ int mgpbd_update_matrix(mgpbd_handle h, const float* data);
  * mgpbd_init validates it.  No counterpart in the reference. */
 int mgpbd_set_constraint_types(mgpbd_handle h, const int32_t* types);
 
-/* Wait limit, in seconds (0, 60], of every grid-barrier wait of the
+/* Wait limit, in seconds [0, 60], of every grid-barrier wait of the
  * persistent CG kernels (default 4).  A wait that reaches it ends the
  * kernel on every block, marks MGPBD_STATUS_SYNC_TIMEOUT and makes the call
  * return MGPBD_ECUDA; the next launch starts afresh, so the handle stays
- * usable.  A very short limit makes a solve fail this way on purpose (how
- * the tests exercise the path).  No counterpart in the reference. */
+ * usable.  0 gives up at the first wait that finds another block not yet
+ * arrived, which makes a solve fail this way on purpose (how the tests
+ * exercise the path).  No counterpart in the reference. */
 int mgpbd_set_barrier_limit(mgpbd_handle h, double seconds);
 
 /* Replaces MGPBDSolverGPU.init (cons/mgpbd_gpu.py:92-114): rest shape,

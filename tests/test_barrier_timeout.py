@@ -4,9 +4,11 @@ out into an error code, and the handle keeps working.
 Every grid-barrier wait of the cooperative CG kernels polls with a time
 limit; a block whose wait reaches it sets the error flag and
 MGPBD_STATUS_SYNC_TIMEOUT and returns, the other blocks leave at their next
-wait, and the call returns MGPBD_ECUDA.  Here the limit is set to 1 ns
-(`mgpbd_set_barrier_limit`), so waits run out at once (no block withholds
-an arrival): every block ends within its first barriers, nothing can hang.
+wait, and the call returns MGPBD_ECUDA.  Here the limit is set to 0
+(`mgpbd_set_barrier_limit`): a block gives up at the first poll that finds
+another block not yet arrived, which the launch ramp of a few hundred
+blocks makes certain at the first barrier.  No block withholds an arrival,
+and every block ends within its first barriers: nothing can hang.
 The same solve, repeated with the default limit back, must succeed and land
 where an untouched solver does.
 """
@@ -30,7 +32,8 @@ def test_barrier_limit_is_validated():
   h = C.c_void_p()
   N.check(L.mgpbd_create(C.byref(p), C.byref(h)), 'mgpbd_create')
   try:
-    assert L.mgpbd_set_barrier_limit(h, 0.0) == -1
+    assert L.mgpbd_set_barrier_limit(h, -1.0) == -1
+    assert L.mgpbd_set_barrier_limit(h, 0.0) == 0
     assert L.mgpbd_set_barrier_limit(h, 61.0) == -1
     assert L.mgpbd_set_barrier_limit(h, 4.0) == 0
     assert L.mgpbd_set_barrier_limit(None, 4.0) == -1
@@ -65,7 +68,7 @@ def test_barrier_timeout_is_an_error_and_the_handle_recovers(cuda, variant):
   ref, xr = body(torch, **variant)
   s.step(0)
   ref.step(0)
-  assert L.mgpbd_set_barrier_limit(s._h, 1e-9) == 0
+  assert L.mgpbd_set_barrier_limit(s._h, 0.0) == 0
   s.make_prediction()
   x_before = x.clone()
   with pytest.raises(MGPBDError) as e:

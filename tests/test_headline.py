@@ -2,9 +2,10 @@
 float64 oracle with exact linear solves.
 
 The solver is `bench.py`'s FAST step exactly (`SOLVER_KW` + `FAST_KW`:
-primal warm start + dual persistent Chebyshev-8 CG, CG to relative residual
-1e-6, Newton maxiter 20 / atol 1e-4 / rtol 1e-2, no damping, pinned
-vertices kinematic) on the length + volume constraint system.  The oracle
+dual persistent CG preconditioned by a Chebyshev-8 polynomial in A, CG to
+relative residual 1e-6, Newton maxiter 20 / atol 1e-4 / rtol 1e-2, no
+damping, pinned vertices kinematic) on the length + volume constraint
+system.  The oracle
 (`oracle/mgpbd_oracle.py`, `linear='exact'`) runs the same Newton loop and
 line search in float64 and solves every Newton system to a dual residual of
 1e-11 |b| (`oracle/exact_solve.py`); its trajectories are committed
@@ -21,7 +22,8 @@ iteration count per substep where the oracle's Newton test is not within
   by seeds 0 (1.53e-6, the benchmark's draw), 1 (3.6e-7) and 4 (5.2e-5);
   the stiffest draws, seeds 3 (2.7e-9) and 11 (4.4e-9), on the 20^3 cube
   for three substeps (the float64 oracle factorises its vertex system
-  there; at 40^3 its iterative route takes hours per substep).
+  there; at 40^3 its iterative route takes hours per substep).  Every CG
+  solve of these runs must end below the iteration cap.
 * FAST and the plain FP32 AMG-PCG (the CSR V-cycle PCG the benchmark
   compares against) reach the same positions at 40^3.
 """
@@ -178,6 +180,7 @@ def test_cube_substeps_match_float64_oracle(cuda, n, seed):
   assert abs(float(z['compliance']) - s.params.compliance) <= 1e-6 * float(z['compliance'])
   for i in range(len(z['disp'])):
     s.step(0)
+    assert s.stats()['status'] == 0, (n, seed, i + 1, s.stats())  # no CG cap, no alarm
     ref = x0.astype(np.float64) + z['disp'][i].astype(np.float64)
     err = float(np.abs(x.cpu().numpy() - ref).max()) / float(np.abs(ref).max())
     assert err <= POS_TOL, (n, seed, i + 1, err, s.stats())

@@ -94,10 +94,10 @@ def test_standalone_setup_solve_and_refill(cuda):
   assert np.linalg.norm(A.astype(np.float64) @ xs - b) <= 1e-4 * np.linalg.norm(b)
   # new level-0 values (same pattern, still symmetric): 1/diag and the
   # coarse level follow
-  s = (1.0 + 0.1 * rng.random(A.shape[0])).astype(np.float32)
-  A2 = (sp.diags(s) @ A @ sp.diags(s)).tocsr()
-  A2 = sp.csr_matrix((A2[A.nonzero()].A1.astype(np.float32), A.indices, A.indptr),
-                     shape=A.shape)
+  s = 1.0 + 0.1 * rng.random(A.shape[0])
+  rows = np.repeat(np.arange(A.shape[0]), np.diff(A.indptr))
+  d2 = (A.data * s[rows] * s[A.indices]).astype(np.float32)  # D A D, same pattern
+  A2 = sp.csr_matrix((d2, A.indices, A.indptr), shape=A.shape)
   gm.update_fine_matrix_data(torch.tensor(A2.data, device='cuda'))
   Ac2 = (Ps[0].T @ A2.astype(np.float64) @ Ps[0]).tocsr()
   Ac2.sort_indices()
