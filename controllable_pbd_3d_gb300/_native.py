@@ -141,6 +141,8 @@ _SIGS = {
     'mgpbd_set_matrix': (C.c_int, [vp, i32, C.c_int64, vp, vp, vp]),
     'mgpbd_update_matrix': (C.c_int, [vp, vp]),
     'mgpbd_set_barrier_limit': (C.c_int, [vp, C.c_double]),
+    'mgpbd_set_bodies': (C.c_int, [vp, i32, vp, i32, vp]),
+    'mgpbd_body_stats': (C.c_int, [vp, i32, vp, vp, vp, vp]),
     'mgpbd_zone_proximity': (C.c_int, [vp, vp, f32, f32, f32, f32]),
     'mgpbd_zone_strain': (C.c_int, [vp, vp, vp, f32, f32]),
     'mgpbd_zone_expand': (C.c_int, [vp, vp, i32]),

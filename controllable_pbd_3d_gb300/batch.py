@@ -5,11 +5,15 @@ b shifted by the vertices before it) makes the system matrix block diagonal:
 one persistent-kernel CG solve fills the GPU with bodies that would each
 occupy a few SMs.  Each body keeps its own compliance (alpha~ per tet).
 
-The packed bodies share one Newton loop: one residual norm, one stopping
-test and one line-search step per Newton iteration for the whole batch.
-The linear solve of each Newton iteration is the same block-diagonal system
-as solving every body on its own (tested); the Newton path can differ from
-separate per-body steps by the shared step length.
+With the FAST persistent Chebyshev CG (`per_body=True`, the default for
+that mode) every body runs its own Newton loop: its residual norm, its
+stopping test and its line-search step, so a stiff body does not set the
+iteration count or the step of the others (`mgpbd_set_bodies`).  Each
+Newton iteration solves the block-diagonal system once, and the solve is
+verified per body (each active body's residual below the relative
+tolerance times its own right-hand side).  A packed substep therefore
+lands where separate per-body substeps land (tested).  Other modes share
+one Newton loop (one residual, test and step for the whole batch).
 """
 
 from __future__ import annotations
@@ -76,7 +80,7 @@ class BodyBatch:
   """One MGPBDSolverGPU over the packed bodies; `positions(b)` is a view of
   body b's rows of the shared positions tensor."""
 
-  def __init__(self, bodies, gravity, dt, device='cuda', **solver_kw):
+  def __init__(self, bodies, gravity, dt, device='cuda', per_body=None, **solver_kw):
     if 'compliance' in solver_kw:
       raise ValueError('compliance is per body (Body.compliance)')
     self.bodies = list(bodies)
@@ -89,6 +93,11 @@ class BodyBatch:
                                  torch.tensor(t_i, device=device), None, gravity, dt,
                                  compliance=self.bodies[0].compliance, **solver_kw)
     self.dt = float(dt)
+    fast_cheb = (solver_kw.get('mode') == 'fast' and solver_kw.get('precond') == 'cheb' and
+                 solver_kw.get('persistent', True))
+    self.per_body = fast_cheb if per_body is None else bool(per_body)
+    if self.per_body:
+      self.solver.set_bodies(self.vert_off, self.segments())
 
   def constraint_body(self) -> np.ndarray:
     """Body id of every constraint: one per tet (ARAP), or the volume
@@ -99,6 +108,17 @@ class BodyBatch:
       return tet_body
     edge_body = np.searchsorted(self.vert_off, self.solver.edges[:, 0], side='right') - 1
     return np.concatenate([tet_body, edge_body])
+
+  def segments(self) -> np.ndarray:
+    """(k, 3) constraint ranges (begin, end, body) in constraint order:
+    each body's volume (or ARAP) constraints, then, with
+    constraints='edge_volume', each body's edges (the edges are sorted by
+    vertex id, so every body's edges are contiguous)."""
+    cb = self.constraint_body()
+    cut = np.flatnonzero(np.diff(cb)) + 1
+    begin = np.concatenate([[0], cut])
+    end = np.concatenate([cut, [len(cb)]])
+    return np.stack([begin, end, cb[begin]], axis=1).astype(np.int32)
 
   def init(self):
     self.solver.init()

@@ -176,6 +176,18 @@ int mgpbd_update_matrix(mgpbd_handle h, const float* data) {
   return guarded([&] { h->impl.update_matrix(data); });
 }
 
+int mgpbd_set_bodies(mgpbd_handle h, int32_t n_bodies, const int32_t* vert_off, int32_t n_segs,
+                     const int32_t* segs) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.set_bodies(n_bodies, vert_off, n_segs, segs); });
+}
+
+int mgpbd_body_stats(mgpbd_handle h, int32_t n, int32_t* newton_iters, double* residual0,
+                     double* residual, double* omega) {
+  if (!h) return MGPBD_EINVAL;
+  return guarded([&] { h->impl.body_stats(n, newton_iters, residual0, residual, omega); });
+}
+
 int mgpbd_set_barrier_limit(mgpbd_handle h, double seconds) {
   if (!h) return MGPBD_EINVAL;
   return guarded([&] { h->impl.set_barrier_limit(seconds); });

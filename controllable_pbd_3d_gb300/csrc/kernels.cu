@@ -294,6 +294,54 @@ __global__ void k_rhs(const float* __restrict__ C, const float* __restrict__ alp
   if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
 
+constexpr int kMaxOmega = 16;
+
+// Adds constraint t's squared dual residual at x + omega_k dpos, for the
+// n_omega trial steps, to acc[k] (_calc_dual_norm_at, cons/mgpbd_gpu.py:
+// 360-377).
+__device__ __forceinline__ void add_trials(int64_t t, const float* __restrict__ x,
+                                           const float* __restrict__ dpos,
+                                           const double* __restrict__ omegas, int n_omega,
+                                           const int4* __restrict__ t_i,
+                                           const int32_t* __restrict__ ctype,
+                                           const float* __restrict__ dm_inv,
+                                           const float* __restrict__ rest,
+                                           const float* __restrict__ alpha,
+                                           const float* __restrict__ lambda,
+                                           double (&acc)[kMaxOmega]) {
+  int4 q = t_i[t];
+  const int ty = ctype ? ctype[t] : MGPBD_CONS_ARAP;
+  float al = alpha[t] * lambda[t];
+  if (ty == MGPBD_CONS_LENGTH) {
+    const float L0 = rest[t];
+#pragma unroll 1
+    for (int k = 0; k < n_omega; ++k) {
+      float r = -(length_c(x, dpos, (float)omegas[k], q, L0, nullptr) + al);
+      acc[k] += (double)r * (double)r;
+    }
+    return;
+  }
+  float B[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) B[k] = dm_inv[9 * t + k];
+#pragma unroll 1
+  for (int k = 0; k < n_omega; ++k) {
+    float F[3][3];
+    deformation(x, dpos, (float)omegas[k], q, B, F);
+    float c;
+    if (ty == MGPBD_CONS_VOLUME) {
+      float P[3][3];
+      c = volume_c(F, P);
+    } else {
+      float U[3][3], s[3], V[3][3];
+      svd3_rv(F, U, s, V);
+      c = arap_c(s);
+    }
+    float r = -(c + al);
+    acc[k] += (double)r * (double)r;
+  }
+}
+
 // _calc_dual_norm_at (cons/mgpbd_gpu.py:360-377) at x + omega_k dpos for
 // several omega_k in one pass
 __global__ void k_dual_trial(const float* __restrict__ x, const float* __restrict__ dpos,
@@ -302,48 +350,80 @@ __global__ void k_dual_trial(const float* __restrict__ x, const float* __restric
                              const float* __restrict__ dm_inv, const float* __restrict__ rest,
                              const float* __restrict__ alpha, const float* __restrict__ lambda,
                              int32_t nt, double* __restrict__ partials) {
-  constexpr int kMaxOmega = 16;
   double acc[kMaxOmega];
 #pragma unroll
   for (int k = 0; k < kMaxOmega; ++k) acc[k] = 0.0;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    int4 q = t_i[t];
-    const int ty = ctype ? ctype[t] : MGPBD_CONS_ARAP;
-    float al = alpha[t] * lambda[t];
-    if (ty == MGPBD_CONS_LENGTH) {
-      const float L0 = rest[t];
-#pragma unroll 1
-      for (int k = 0; k < n_omega; ++k) {
-        float r = -(length_c(x, dpos, (float)omegas[k], q, L0, nullptr) + al);
-        acc[k] += (double)r * (double)r;
-      }
-      continue;
-    }
-    float B[9];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) B[k] = dm_inv[9 * t + k];
-#pragma unroll 1
-    for (int k = 0; k < n_omega; ++k) {
-      float F[3][3];
-      deformation(x, dpos, (float)omegas[k], q, B, F);
-      float c;
-      if (ty == MGPBD_CONS_VOLUME) {
-        float P[3][3];
-        c = volume_c(F, P);
-      } else {
-        float U[3][3], s[3], V[3][3];
-        svd3_rv(F, U, s, V);
-        c = arap_c(s);
-      }
-      float r = -(c + al);
-      acc[k] += (double)r * (double)r;
-    }
-  }
+       t += (int64_t)gridDim.x * blockDim.x)
+    add_trials(t, x, dpos, omegas, n_omega, t_i, ctype, dm_inv, rest, alpha, lambda, acc);
 #pragma unroll 1
   for (int k = 0; k < n_omega; ++k) {
     double v = block_sum(acc[k]);
     if (threadIdx.x == 0) partials[k * gridDim.x + blockIdx.x] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Per-body reductions of a packed batch.  The constraints are cut into
+// chunks (contiguous ranges, each inside one body's range); block c sums
+// its chunk in a fixed order, so the per-body sums the host forms from the
+// chunk partials (in chunk order) repeat bit for bit.
+
+// partials[c] = sum over chunk c of (C + alpha lambda)^2 (alpha = null: C^2)
+__global__ void k_chunk_dual_sq(const float* __restrict__ C, const float* __restrict__ alpha,
+                                const float* __restrict__ lambda,
+                                const int2* __restrict__ chunks, double* __restrict__ partials) {
+  const int2 ch = chunks[blockIdx.x];
+  double acc = 0.0;
+  for (int64_t t = ch.x + threadIdx.x; t < ch.y; t += blockDim.x) {
+    float r = alpha ? C[t] + alpha[t] * lambda[t] : C[t];
+    acc += (double)r * (double)r;
+  }
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+}
+
+// partials[k * n_chunks + c]: the dual residual squares of chunk c at the
+// trial step omega_k
+__global__ void k_chunk_trial(const float* __restrict__ x, const float* __restrict__ dpos,
+                              const double* __restrict__ omegas, int n_omega,
+                              const int4* __restrict__ t_i, const int32_t* __restrict__ ctype,
+                              const float* __restrict__ dm_inv, const float* __restrict__ rest,
+                              const float* __restrict__ alpha, const float* __restrict__ lambda,
+                              const int2* __restrict__ chunks, double* __restrict__ partials) {
+  double acc[kMaxOmega];
+#pragma unroll
+  for (int k = 0; k < kMaxOmega; ++k) acc[k] = 0.0;
+  const int2 ch = chunks[blockIdx.x];
+  for (int64_t t = ch.x + threadIdx.x; t < ch.y; t += blockDim.x)
+    add_trials(t, x, dpos, omegas, n_omega, t_i, ctype, dm_inv, rest, alpha, lambda, acc);
+#pragma unroll 1
+  for (int k = 0; k < n_omega; ++k) {
+    double v = block_sum(acc[k]);
+    if (threadIdx.x == 0) partials[k * gridDim.x + blockIdx.x] = v;
+  }
+}
+
+// b_t = 0 for the constraints of bodies whose Newton loop has ended
+__global__ void k_mask_rhs(float* __restrict__ b, const int32_t* __restrict__ cons_body,
+                           const int32_t* __restrict__ active, int32_t nt) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt;
+       t += (int64_t)gridDim.x * blockDim.x)
+    if (!active[cons_body[t]]) b[t] = 0.0f;
+}
+
+// _apply_dpos with each body's own line-search step
+__global__ void k_apply_bodies(float* __restrict__ x, const float* __restrict__ dpos,
+                               const float* __restrict__ invm,
+                               const int32_t* __restrict__ vert_body,
+                               const float* __restrict__ omega, int32_t nv) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nv;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    if (invm[k] > 0.0f) {
+      const float w = omega[vert_body[k]];
+      float3 p = ld3(x, k), d = ld3(dpos, k);
+      st3(x, k, make_float3(p.x + w * d.x, p.y + w * d.y, p.z + w * d.z));
+    }
   }
 }
 
@@ -956,10 +1036,47 @@ void launch_dual_trial(const float* x, const float* dpos, const double* omegas, 
                        const int32_t* t_i, const int32_t* ctype, const float* dm_inv,
                        const float* rest, const float* alpha, const float* lambda, int32_t nt,
                        double* partials, cudaStream_t s) {
-  require(n_omega >= 1 && n_omega <= 16, MGPBD_EINVAL, "n_omega out of range");
+  require(n_omega >= 1 && n_omega <= kMaxOmega, MGPBD_EINVAL, "n_omega out of range");
   k_dual_trial<<<reduce_blocks(nt), kThreads, 0, s>>>(x, dpos, omegas, n_omega,
                                                       reinterpret_cast<const int4*>(t_i), ctype,
                                                       dm_inv, rest, alpha, lambda, nt, partials);
+  MGPBD_CHECK_LAUNCH();
+}
+
+void launch_chunk_dual_sq(const float* C, const float* alpha, const float* lambda,
+                          const int32_t* chunks, int32_t n_chunks, double* partials,
+                          cudaStream_t s) {
+  if (n_chunks <= 0) return;
+  k_chunk_dual_sq<<<n_chunks, kThreads, 0, s>>>(C, alpha, lambda,
+                                                reinterpret_cast<const int2*>(chunks), partials);
+  MGPBD_CHECK_LAUNCH();
+}
+
+void launch_chunk_trial(const float* x, const float* dpos, const double* omegas, int n_omega,
+                        const int32_t* t_i, const int32_t* ctype, const float* dm_inv,
+                        const float* rest, const float* alpha, const float* lambda,
+                        const int32_t* chunks, int32_t n_chunks, double* partials,
+                        cudaStream_t s) {
+  require(n_omega >= 1 && n_omega <= kMaxOmega, MGPBD_EINVAL, "n_omega out of range");
+  if (n_chunks <= 0) return;
+  k_chunk_trial<<<n_chunks, kThreads, 0, s>>>(x, dpos, omegas, n_omega,
+                                              reinterpret_cast<const int4*>(t_i), ctype, dm_inv,
+                                              rest, alpha, lambda,
+                                              reinterpret_cast<const int2*>(chunks), partials);
+  MGPBD_CHECK_LAUNCH();
+}
+
+void launch_mask_rhs(float* b, const int32_t* cons_body, const int32_t* active, int32_t nt,
+                     cudaStream_t s) {
+  if (nt <= 0) return;
+  k_mask_rhs<<<grid_for(nt, kThreads), kThreads, 0, s>>>(b, cons_body, active, nt);
+  MGPBD_CHECK_LAUNCH();
+}
+
+void launch_apply_bodies(float* x, const float* dpos, const float* invm, const int32_t* vert_body,
+                         const float* omega, int32_t nv, cudaStream_t s) {
+  if (nv <= 0) return;
+  k_apply_bodies<<<grid_for(nv, kThreads), kThreads, 0, s>>>(x, dpos, invm, vert_body, omega, nv);
   MGPBD_CHECK_LAUNCH();
 }
 

@@ -45,6 +45,24 @@ void launch_lambda_update(float* lambda, const float* dlam, int32_t nt, cudaStre
 void launch_scatter(const int32_t* inc_ptr, const int32_t* inc_ent, const float* invm,
                     const float* dlam, const float* gradC, float* dpos, int32_t nv,
                     cudaStream_t s);
+// per-body reductions of a packed batch over constraint chunks (int2 begin,
+// end; each inside one body): partials[c] = sum of (C + alpha lambda)^2
+// over chunk c (alpha = null: sum of C^2)
+void launch_chunk_dual_sq(const float* C, const float* alpha, const float* lambda,
+                          const int32_t* chunks, int32_t n_chunks, double* partials,
+                          cudaStream_t s);
+// partials[k * n_chunks + c]: chunk c's squared dual residual at x + omega_k dpos
+void launch_chunk_trial(const float* x, const float* dpos, const double* omegas, int n_omega,
+                        const int32_t* t_i, const int32_t* ctype, const float* dm_inv,
+                        const float* rest, const float* alpha, const float* lambda,
+                        const int32_t* chunks, int32_t n_chunks, double* partials,
+                        cudaStream_t s);
+// b_t = 0 where active[cons_body[t]] == 0
+void launch_mask_rhs(float* b, const int32_t* cons_body, const int32_t* active, int32_t nt,
+                     cudaStream_t s);
+// x += omega[vert_body[v]] dpos for free vertices
+void launch_apply_bodies(float* x, const float* dpos, const float* invm, const int32_t* vert_body,
+                         const float* omega, int32_t nv, cudaStream_t s);
 void launch_apply(float* x, const float* dpos, const float* invm, int32_t nv, float omega,
                   cudaStream_t s);
 

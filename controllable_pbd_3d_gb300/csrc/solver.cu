@@ -292,6 +292,7 @@ void Solver::set_mesh(const float* x_ref, const float* invm, const int32_t* t_i,
   x_ = x;
   v_ = v;
   matrix_mode_ = false;
+  nb_ = 0;
   inited_ = false;
   user_sizes_.clear();
   user_aggs_.clear();
@@ -465,6 +466,11 @@ void Solver::init() {
   for (int32_t l = 0; l < n_levels() && l < 8; ++l) {
     stats_.rows[l] = levels_[l].n;
     stats_.nnz[l] = levels_[l].nnz;
+  }
+  if (nb_ > 0) {
+    inited_ = false;
+    init_bodies(t_host);
+    inited_ = true;
   }
 }
 
@@ -808,32 +814,10 @@ int32_t Solver::pcg_cheb(const float* b, float* x) {
       }
     }
     // one cooperative kernel for the (rest of the) solve
-    JcgVecs v;
-    v.b = b;
-    v.x = x;
-    v.xc = jxc_.p;
-    v.r = jrf_.p;
-    v.z = jz_.p;
-    v.d = jd_.p;
-    v.p = jp_.p;
-    v.ap = jap_.p;
-    v.partials = partials_.p;
-    v.partials_capacity = static_cast<int64_t>(kMaxReduceBlocks) * 16;
-    v.gs = jgs_.p;
-    v.ulo = primal() ? pv_[6].p : nullptr;  // the primal Kp vector, free by now
-    MGPBD_CUDA(cudaEventRecord(ev_[0], outer));
-    launch_jcg_persistent(jview(), v, jplan_, jpart_.p, jst_.p, cg_state_.p, p_.tol_cg,
-                          p_.rel_tol_cg, left, p_.cheb_degree, warm, barrier_limit_s_, outer);
-    MGPBD_CUDA(cudaEventRecord(ev_[1], outer));
-    sync_read(h_state_, cg_state_.p, sizeof(CgState));
-    stats_.ms_dual += event_ms(ev_[0], ev_[1]);
-    stats_.cg_launches += 1;
-    if (static_cast<uint32_t>(h_state_->status) & MGPBD_STATUS_SYNC_TIMEOUT) {
-      status_ |= MGPBD_STATUS_SYNC_TIMEOUT;
-      throw Error(MGPBD_ECUDA, "persistent CG kernel: a grid barrier wait timed out");
-    }
-    status_ |= static_cast<uint32_t>(h_state_->status);
-    return its + h_state_->iters;
+    // (the primal Kp vector, free by now, holds the warm start's low parts)
+    const int32_t dual = run_dual(b, x, p_.tol_cg, p_.rel_tol_cg, left, warm,
+                                  primal() ? pv_[6].p : nullptr);
+    return its + dual;
   }
   if (!p_.use_graph) {
     // same kernels from the host; every kernel is a no-op once done is set
@@ -1442,6 +1426,10 @@ void Solver::apply_dpos(double omega) {
 void Solver::solve(int32_t frame) {
   (void)frame;
   require_mesh();
+  if (nb_ > 0) {
+    solve_bodies();
+    return;
+  }
   status_ = 0;
   MGPBD_CUDA(cudaMemsetAsync(lambda_.p, 0, sizeof(float) * nt_, stream_));
   double r0 = 0.0;
@@ -1493,6 +1481,292 @@ void Solver::solve(int32_t frame) {
     if (ite + 1 == p_.maxiter) status_ |= MGPBD_STATUS_NEWTON_MAXITER;
   }
   stats_.status = status_;
+}
+
+// One cooperative dual CG kernel from x (warm) or 0 to |r| <= max(tol_abs,
+// tol_rel |b|) or maxit iterations; returns its iterations.
+int32_t Solver::run_dual(const float* b, float* x, double tol_abs, double tol_rel, int32_t maxit,
+                         bool warm, float4* ulo) {
+  cudaStream_t outer = stream_;
+  JcgVecs v;
+  v.b = b;
+  v.x = x;
+  v.xc = jxc_.p;
+  v.r = jrf_.p;
+  v.z = jz_.p;
+  v.d = jd_.p;
+  v.p = jp_.p;
+  v.ap = jap_.p;
+  v.partials = partials_.p;
+  v.partials_capacity = static_cast<int64_t>(kMaxReduceBlocks) * 16;
+  v.gs = jgs_.p;
+  v.ulo = ulo;
+  MGPBD_CUDA(cudaEventRecord(ev_[0], outer));
+  launch_jcg_persistent(jview(), v, jplan_, jpart_.p, jst_.p, cg_state_.p, tol_abs, tol_rel, maxit,
+                        p_.cheb_degree, warm, barrier_limit_s_, outer);
+  MGPBD_CUDA(cudaEventRecord(ev_[1], outer));
+  sync_read(h_state_, cg_state_.p, sizeof(CgState));
+  stats_.ms_dual += event_ms(ev_[0], ev_[1]);
+  stats_.cg_launches += 1;
+  if (static_cast<uint32_t>(h_state_->status) & MGPBD_STATUS_SYNC_TIMEOUT) {
+    status_ |= MGPBD_STATUS_SYNC_TIMEOUT;
+    throw Error(MGPBD_ECUDA, "persistent CG kernel: a grid barrier wait timed out");
+  }
+  status_ |= static_cast<uint32_t>(h_state_->status);
+  return h_state_->iters;
+}
+
+// ---------------------------------------------------------------------------
+// Packed independent bodies
+
+namespace {
+constexpr int32_t kBodyChunk = 4096;  // constraints per reduction chunk
+constexpr int kBodyTrials = 10;       // line-search steps 1, 1/2, ..., 1/512
+}  // namespace
+
+void Solver::set_bodies(int32_t n_bodies, const int32_t* vert_off, int32_t n_segs,
+                        const int32_t* segs) {
+  require(x_ && t_i_ && !matrix_mode_, MGPBD_ESTATE, "mgpbd_set_mesh must come before mgpbd_set_bodies");
+  if (n_bodies == 0) {
+    nb_ = 0;
+    inited_ = false;
+    return;
+  }
+  require(n_bodies > 0 && vert_off && segs && n_segs >= n_bodies, MGPBD_EINVAL,
+          "bodies: null array or fewer constraint ranges than bodies");
+  require(vert_off[0] == 0 && vert_off[n_bodies] == nv_, MGPBD_EINVAL,
+          "bodies: vert_off must run from 0 to nv");
+  for (int32_t b = 0; b < n_bodies; ++b)
+    require(vert_off[b + 1] > vert_off[b], MGPBD_EINVAL, "bodies: every body needs vertices");
+  std::vector<uint8_t> seen(n_bodies, 0);
+  int32_t at = 0;
+  for (int32_t k = 0; k < n_segs; ++k) {
+    const int32_t lo = segs[3 * k], hi = segs[3 * k + 1], body = segs[3 * k + 2];
+    require(lo == at && hi > lo && hi <= nt_, MGPBD_EINVAL,
+            "bodies: constraint ranges must cover [0, nt) in order, each non-empty");
+    require(body >= 0 && body < n_bodies, MGPBD_EINVAL, "bodies: body id out of range");
+    seen[body] = 1;
+    at = hi;
+  }
+  require(at == nt_, MGPBD_EINVAL, "bodies: constraint ranges must end at nt");
+  for (uint8_t u : seen) require(u != 0, MGPBD_EINVAL, "bodies: a body without constraints");
+  nb_ = n_bodies;
+  body_vert_off_.assign(vert_off, vert_off + n_bodies + 1);
+  body_segs_.assign(segs, segs + 3LL * n_segs);
+  inited_ = false;
+}
+
+void Solver::init_bodies(const std::vector<int32_t>& t_host) {
+  require(cheb() && p_.persistent && p_.mode == MGPBD_MODE_FAST, MGPBD_ENOTSUP,
+          "packed bodies run the FAST persistent Chebyshev CG (mode fast, precond cheb)");
+  cudaStream_t s = stream_;
+  std::vector<int32_t> cb(nt_), vb(nv_), ch;
+  chunk_body_.clear();
+  for (size_t k = 0; k < body_segs_.size(); k += 3) {
+    const int32_t lo = body_segs_[k], hi = body_segs_[k + 1], body = body_segs_[k + 2];
+    for (int32_t t = lo; t < hi; ++t) cb[t] = body;
+    for (int32_t c = lo; c < hi; c += kBodyChunk) {
+      ch.push_back(c);
+      ch.push_back(std::min(hi, c + kBodyChunk));
+      chunk_body_.push_back(body);
+    }
+  }
+  for (int32_t b = 0; b < nb_; ++b)
+    for (int32_t v = body_vert_off_[b]; v < body_vert_off_[b + 1]; ++v) vb[v] = b;
+  // a constraint may only touch its own body's vertices (the bodies are
+  // independent: block-diagonal A)
+  for (int32_t t = 0; t < nt_; ++t)
+    for (int l = 0; l < 4; ++l)
+      require(vb[t_host[4LL * t + l]] == cb[t], MGPBD_EINVAL,
+              "bodies: a constraint touches another body's vertices");
+  upload(chunks_, ch, s);
+  upload(cons_body_, cb, s);
+  upload(vert_body_, vb, s);
+  body_active_.alloc(nb_);
+  body_omega_.alloc(nb_);
+  chunk_partials_.alloc(static_cast<int64_t>(kBodyTrials) * static_cast<int64_t>(chunk_body_.size()));
+  body_ulo_.alloc(nv_);
+  MGPBD_CUDA(cudaMemsetAsync(body_ulo_.p, 0, sizeof(float4) * nv_, s));
+  body_newton_.assign(nb_, 0);
+  body_r0_.assign(nb_, 0.0);
+  body_r_.assign(nb_, 0.0);
+  body_omega_h_.assign(nb_, 1.0);
+  MGPBD_CUDA(cudaStreamSynchronize(s));
+}
+
+// out[k * nb + b] = sum of the chunk partials k of body b, in chunk order
+void Solver::chunk_body_sums(int count, std::vector<double>& out) {
+  const int64_t nc = static_cast<int64_t>(chunk_body_.size());
+  std::vector<double> h(count * nc);
+  MGPBD_CUDA(cudaMemcpyAsync(h.data(), chunk_partials_.p, sizeof(double) * h.size(),
+                             cudaMemcpyDeviceToHost, stream_));
+  MGPBD_CUDA(cudaStreamSynchronize(stream_));
+  out.assign(static_cast<size_t>(count) * nb_, 0.0);
+  for (int k = 0; k < count; ++k)
+    for (int64_t c = 0; c < nc; ++c) out[static_cast<size_t>(k) * nb_ + chunk_body_[c]] += h[k * nc + c];
+}
+
+// The block-diagonal CG solve of one Newton iteration, verified per body:
+// CG to |r| <= rel |b| over the batch, then each body's own residual
+// |r_b| <= rel |b_b| is checked; while some body misses it, CG continues
+// from its iterate (float64 restart residual) to the smallest missing
+// body's bound.  bnorm[b] = |b_b| (0 for bodies whose loop has ended).
+int32_t Solver::pcg_bodies(const float* b, float* x, const std::vector<double>& bnorm) {
+  const double rel = p_.rel_tol_cg;
+  const int32_t n_ch = static_cast<int32_t>(chunk_body_.size());
+  double bn2 = 0.0;
+  for (double v : bnorm) bn2 += v * v;
+  double tol = std::max<double>(p_.tol_cg, rel * std::sqrt(bn2));
+  int32_t total = 0, left = p_.maxiter_cg;
+  bool warm = false;
+  std::vector<double> rb2;
+  for (int pass = 0; pass < 6 && left > 0; ++pass) {
+    const int32_t its = run_dual(b, x, tol, 0.0, left, warm, body_ulo_.p);
+    total += its;
+    left -= its;
+    if (status_ & (MGPBD_STATUS_NAN | MGPBD_STATUS_PAP_NONPOS)) break;
+    launch_chunk_dual_sq(jrf_.p, nullptr, nullptr, chunks_.p, n_ch, chunk_partials_.p, stream_);
+    chunk_body_sums(1, rb2);
+    double need = std::numeric_limits<double>::infinity();
+    for (int32_t k = 0; k < nb_; ++k) {
+      const double bound = std::max<double>(p_.tol_cg, rel * bnorm[k]);
+      if (bnorm[k] > 0.0 && std::sqrt(rb2[k]) > bound) need = std::min(need, bound);
+    }
+    if (!std::isfinite(need)) return total;
+    tol = need;
+    warm = true;
+  }
+  status_ |= MGPBD_STATUS_CG_MAXITER;
+  return total;
+}
+
+// The Newton loop of cons/mgpbd_gpu.py:397-446 run per body: each body's
+// residual, stopping test and line-search step are its own; bodies whose
+// test holds keep their positions (zero right-hand side) while the others
+// go on.
+void Solver::solve_bodies() {
+  cudaStream_t s = stream_;
+  status_ = 0;
+  MGPBD_CUDA(cudaMemsetAsync(lambda_.p, 0, sizeof(float) * nt_, s));
+  stats_.newton_iters = 0;
+  stats_.cg_iters_total = 0;
+  stats_.cg_iters_last = 0;
+  stats_.omega_last = 1.0;
+  stats_.cg_iters_warm = 0;
+  stats_.cg_launches = 0;
+  stats_.ms_warm = 0.0;
+  stats_.ms_dual = 0.0;
+  stats_.warm_amp = 0.0;
+  stats_.warm_declined = 0;
+  log_.clear();
+  auto now = [] {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+  };
+  const int32_t n_ch = static_cast<int32_t>(chunk_body_.size());
+  std::vector<int32_t> active(nb_, 1);
+  std::vector<double> r2, bnorm(nb_), cur, trial;
+  std::vector<float> om(nb_);
+  std::fill(body_newton_.begin(), body_newton_.end(), 0);
+  std::fill(body_omega_h_.begin(), body_omega_h_.end(), 1.0);
+  for (int32_t ite = 0; ite < p_.maxiter; ++ite) {
+    compute_constraints();
+    launch_rhs(C_.p, alpha_.p, lambda_.p, nt_, rhs_.p, partials_.p, s);
+    launch_chunk_dual_sq(C_.p, alpha_.p, lambda_.p, chunks_.p, n_ch, chunk_partials_.p, s);
+    chunk_body_sums(1, r2);
+    double rg2 = 0.0;
+    for (double v : r2) rg2 += v;
+    const double r = std::sqrt(rg2);
+    if (ite == 0) {
+      stats_.residual0 = r;
+      for (int32_t k = 0; k < nb_; ++k) body_r0_[k] = std::sqrt(r2[k]);
+    }
+    stats_.residual = r;
+    if (!std::isfinite(r)) {
+      status_ |= MGPBD_STATUS_NAN;
+      break;
+    }
+    int32_t n_active = 0;
+    for (int32_t k = 0; k < nb_; ++k) {
+      bnorm[k] = 0.0;
+      if (!active[k]) continue;
+      const double rk = std::sqrt(r2[k]);
+      body_r_[k] = rk;
+      if (rk < p_.atol || (body_r0_[k] > 1e-12 && rk < p_.rtol * body_r0_[k])) {
+        active[k] = 0;
+      } else {
+        bnorm[k] = rk;
+        ++n_active;
+      }
+    }
+    if (n_active == 0) {
+      log_.push_back({double(ite), r, 0.0, 1.0, now()});
+      break;
+    }
+    MGPBD_CUDA(cudaMemcpyAsync(body_active_.p, active.data(), sizeof(int32_t) * nb_,
+                               cudaMemcpyHostToDevice, s));
+    launch_mask_rhs(rhs_.p, cons_body_.p, body_active_.p, nt_, s);
+    fill_matrices();
+    const int32_t it = pcg_bodies(rhs_.p, dlam_.p, bnorm);
+    scatter(dlam_.p);
+    // per-body line search (cons/mgpbd_gpu.py:379-391): the first of 1,
+    // 1/2, ..., 1/512 whose dual norm (updated lambda) beats the current one
+    launch_chunk_dual_sq(C_.p, alpha_.p, lambda_.p, chunks_.p, n_ch, chunk_partials_.p, s);
+    chunk_body_sums(1, cur);
+    double steps[kBodyTrials];
+    for (int k = 0; k < kBodyTrials; ++k) steps[k] = std::ldexp(1.0, -k);
+    std::memcpy(h_buf_, steps, sizeof(steps));
+    MGPBD_CUDA(cudaMemcpyAsync(omegas_.p, h_buf_, sizeof(steps), cudaMemcpyHostToDevice, s));
+    launch_chunk_trial(x_, dpos_.p, omegas_.p, 1, t_i_, ctype_.p, dm_inv_.p, rest_vol_.p,
+                       alpha_.p, lambda_.p, chunks_.p, n_ch, chunk_partials_.p, s);
+    chunk_body_sums(1, trial);
+    bool more = false;
+    for (int32_t k = 0; k < nb_; ++k) {
+      om[k] = 1.0f;
+      if (active[k] && !(std::sqrt(trial[k]) < std::sqrt(cur[k]))) more = true;
+    }
+    if (more) {
+      launch_chunk_trial(x_, dpos_.p, omegas_.p, kBodyTrials, t_i_, ctype_.p, dm_inv_.p,
+                         rest_vol_.p, alpha_.p, lambda_.p, chunks_.p, n_ch, chunk_partials_.p, s);
+      chunk_body_sums(kBodyTrials, trial);
+      for (int32_t k = 0; k < nb_; ++k) {
+        if (!active[k]) continue;
+        double w = std::ldexp(1.0, -kBodyTrials);
+        for (int q = 0; q < kBodyTrials; ++q)
+          if (std::sqrt(trial[static_cast<size_t>(q) * nb_ + k]) < std::sqrt(cur[k])) {
+            w = steps[q];
+            break;
+          }
+        om[k] = static_cast<float>(w);
+      }
+    }
+    MGPBD_CUDA(cudaMemcpyAsync(body_omega_.p, om.data(), sizeof(float) * nb_,
+                               cudaMemcpyHostToDevice, s));
+    launch_apply_bodies(x_, dpos_.p, invm_, vert_body_.p, body_omega_.p, nv_, s);
+    double om_min = 1.0;
+    for (int32_t k = 0; k < nb_; ++k)
+      if (active[k]) {
+        body_newton_[k] += 1;
+        body_omega_h_[k] = om[k];
+        om_min = std::min<double>(om_min, om[k]);
+      }
+    log_.push_back({double(ite), r, double(it), om_min, now()});
+    stats_.newton_iters = ite + 1;
+    stats_.cg_iters_total += it;
+    stats_.cg_iters_last = it;
+    stats_.omega_last = om_min;
+    if (ite + 1 == p_.maxiter) status_ |= MGPBD_STATUS_NEWTON_MAXITER;
+  }
+  stats_.status = status_;
+}
+
+void Solver::body_stats(int32_t n, int32_t* newton, double* r0, double* r, double* omega) const {
+  require(n == nb_ && nb_ > 0, MGPBD_EINVAL, "body_stats: n must equal the number of bodies");
+  for (int32_t k = 0; k < nb_; ++k) {
+    if (newton) newton[k] = body_newton_[k];
+    if (r0) r0[k] = body_r0_[k];
+    if (r) r[k] = body_r_[k];
+    if (omega) omega[k] = body_omega_h_[k];
+  }
 }
 
 void* Solver::field(int32_t id, int64_t* count) {

@@ -66,6 +66,16 @@ class Solver {
   // update_fine_matrix_data + update_all_coarse_matrices (cons/mgpcg_gpu.py:
   // 175-212): new level-0 values (device, nnz), 1/diag and coarse refill
   void update_matrix(const float* data);
+  // Independent bodies packed into the mesh (vertex ranges vert_off[b] ..
+  // vert_off[b+1]; constraint ranges segs[3k] .. segs[3k+1] of body
+  // segs[3k+2], covering [0, nt) in order): each body gets its own Newton
+  // loop (residual, stopping test, line-search step) over one shared
+  // block-diagonal CG solve per Newton iteration.  FAST Chebyshev only.
+  void set_bodies(int32_t n_bodies, const int32_t* vert_off, int32_t n_segs, const int32_t* segs);
+  int32_t n_bodies() const { return nb_; }
+  // per body: Newton iterations, first and last residual, last line-search
+  // step of the last solve
+  void body_stats(int32_t n, int32_t* newton, double* r0, double* r, double* omega) const;
   // wait limit of the persistent CG kernels' grid barriers (seconds)
   void set_barrier_limit(double seconds) {
     require(seconds >= 0.0 && seconds <= 60.0, MGPBD_EINVAL, "barrier limit must be in [0, 60] s");
@@ -124,6 +134,14 @@ class Solver {
 
  private:
   void require_init() const;
+  // packed bodies: per-body Newton loop, verified block-diagonal CG solve,
+  // per-body sums over the constraint chunks
+  void init_bodies(const std::vector<int32_t>& t_host);
+  void solve_bodies();
+  int32_t pcg_bodies(const float* b, float* x, const std::vector<double>& bnorm);
+  void chunk_body_sums(int count, std::vector<double>& out);
+  int32_t run_dual(const float* b, float* x, double tol_abs, double tol_rel, int32_t maxit,
+                   bool warm, float4* ulo);
   // the per-mesh stages need set_mesh (not a caller's matrix)
   void require_mesh() const;
   void init_matrix();
@@ -169,6 +187,15 @@ class Solver {
   bool inited_ = false;
   bool matrix_mode_ = false;     // set_matrix: a caller's level-0 matrix, no mesh
   double barrier_limit_s_ = 4.0; // grid-barrier wait limit of the persistent kernels
+  // packed bodies (set_bodies)
+  int32_t nb_ = 0;
+  std::vector<int32_t> body_vert_off_, body_segs_, chunk_body_;
+  DevBuf<int32_t> chunks_, cons_body_, vert_body_, body_active_;
+  DevBuf<float> body_omega_;
+  DevBuf<double> chunk_partials_;
+  DevBuf<float4> body_ulo_;  // warm restarts of the verified CG solve
+  std::vector<int32_t> body_newton_;
+  std::vector<double> body_r0_, body_r_, body_omega_h_;
   Csr mat_csr_;                  // its structure and values (host)
   std::vector<float> mat_vals_;
 

@@ -263,6 +263,28 @@ class MGPBDSolverGPU:
             'mgpbd_set_hierarchy')
     self._inited = False
 
+  def set_bodies(self, vert_off, segments):
+    """Independent bodies packed in this mesh, each with its own Newton loop
+    (residual, stopping test, line-search step) over a shared, per-body
+    verified block-diagonal CG solve.  vert_off: (n_bodies + 1,) vertex
+    offsets; segments: (k, 3) rows (begin, end, body) of constraint ranges
+    covering all constraints in order.  Before init(); FAST Chebyshev only."""
+    vo = np.ascontiguousarray(vert_off, np.int32)
+    sg = np.ascontiguousarray(np.asarray(segments, np.int32).reshape(-1, 3))
+    N.check(self._lib.mgpbd_set_bodies(self._h, len(vo) - 1, vo.ctypes.data, len(sg),
+                                       sg.ctypes.data), 'mgpbd_set_bodies')
+    self.n_bodies = len(vo) - 1
+    self._inited = False
+
+  def body_stats(self) -> dict:
+    """Per body: Newton iterations, first / last residual, last step."""
+    n = self.n_bodies
+    it = np.zeros(n, np.int32)
+    r0, r, om = np.zeros(n), np.zeros(n), np.zeros(n)
+    N.check(self._lib.mgpbd_body_stats(self._h, n, it.ctypes.data, r0.ctypes.data, r.ctypes.data,
+                                       om.ctypes.data), 'mgpbd_body_stats')
+    return {'newton_iters': it, 'residual0': r0, 'residual': r, 'omega': om}
+
   def init(self):
     self._stream()
     N.check(self._lib.mgpbd_init(self._h), 'mgpbd_init')

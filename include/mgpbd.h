@@ -294,6 +294,28 @@ int mgpbd_update_matrix(mgpbd_handle h, const float* data);
  * mgpbd_init validates it.  No counterpart in the reference. */
 int mgpbd_set_constraint_types(mgpbd_handle h, const int32_t* types);
 
+/* Independent bodies packed into one mesh (vertex ids shifted per body, so
+ * A is block diagonal), each with its own Newton loop: per body the
+ * residual norm, the stopping test (atol / rtol of its own first residual)
+ * and the line-search step of cons/mgpbd_gpu.py:379-446, over one shared
+ * block-diagonal CG solve per Newton iteration that is verified per body
+ * (each active body's residual <= rel_tol_cg times its right-hand side; CG
+ * continues from its iterate while one is not).  A body whose test holds
+ * keeps its positions while the others go on.  Host arrays, between
+ * mgpbd_set_mesh (or mgpbd_set_constraint_types) and mgpbd_init:
+ * vert_off[n_bodies + 1] (body b owns vertices vert_off[b] ..
+ * vert_off[b+1]-1, from 0 to nv); segs[3 * n_segs]: constraint ranges
+ * (begin, end, body) covering [0, nt) in order.  A constraint may only
+ * touch its body's vertices (checked at init).  FAST mode with the
+ * persistent Chebyshev CG only.  n_bodies = 0 returns to one Newton loop.
+ * No counterpart in the reference. */
+int mgpbd_set_bodies(mgpbd_handle h, int32_t n_bodies, const int32_t* vert_off, int32_t n_segs,
+                     const int32_t* segs);
+/* Per body (n = n_bodies entries each, NULL to skip): Newton iterations,
+ * first and last residual norm, last line-search step of the last solve. */
+int mgpbd_body_stats(mgpbd_handle h, int32_t n, int32_t* newton_iters, double* residual0,
+                     double* residual, double* omega);
+
 /* Wait limit, in seconds [0, 60], of every grid-barrier wait of the
  * persistent CG kernels (default 4).  A wait that reaches it ends the
  * kernel on every block, marks MGPBD_STATUS_SYNC_TIMEOUT and makes the call
