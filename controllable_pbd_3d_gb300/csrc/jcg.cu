@@ -433,7 +433,7 @@ __global__ void __launch_bounds__(kPT, STAGED ? 1 : 2) k_jcg(PArgs a) {
     if (!grid_sync(a, gen)) return;
   }
   {
-    float bb = 0.0f, bz = 0.0f;
+    float bb = 0.0f, bz = 0.0f, br = 0.0f;
     for (int64_t t = o.tbeg; t < o.tend; t += o.tstep) {
       const float bt = a.b[t];
       float rt = bt;
@@ -450,20 +450,27 @@ __global__ void __launch_bounds__(kPT, STAGED ? 1 : 2) k_jcg(PArgs a) {
       a.d[t] = zt;
       bb += bt * bt;
       bz += rt * zt;
+      br += rt * rt;
     }
     put_partial(bb, P0);
     put_partial(bz, P1);
+    // a warm start may already meet the tolerance (a float64 residual
+    // replacement after a converged solve): its r.r decides below; P2 is
+    // first rewritten after the next grid barrier
+    if (a.warm) put_partial(br, P2);
   }
   if (!grid_sync(a, gen)) return;
   if (threadIdx.x < 32) {
     const double sb = warp_sum_partials(P0, G);
     const double sz = warp_sum_partials(P1, G);
+    const double s0 = a.warm ? warp_sum_partials(P2, G) : sb;
     if (threadIdx.x == 0) {
       bbs = sb;
       rz = sz;
+      rr = s0;
       const double t2 = a.tol_abs * a.tol_abs, r2 = a.tol_rel * a.tol_rel * bbs;
       tol2 = r2 > t2 ? r2 : t2;
-      int stop = a.maxiter <= 0;
+      int stop = a.maxiter <= 0 || (a.warm && rr < tol2);
       if (!isfinite(bbs)) {
         status |= MGPBD_STATUS_NAN;
         stop = 1;

@@ -613,7 +613,11 @@ void Solver::alloc_work() {
     jxc_.alloc(nt_);
     jrf_.alloc(nt_);
     jgs_.alloc(1);
-    if (p_.persistent) gT_.alloc(3LL * nt_);
+    if (p_.persistent) {
+      gT_.alloc(3LL * nt_);
+      ulo_.alloc(nv_);
+      MGPBD_CUDA(cudaMemsetAsync(ulo_.p, 0, sizeof(float4) * nv_, s));
+    }
     if (primal()) {
       for (auto& b : pv_) {
         b.alloc(nv_);
@@ -814,10 +818,18 @@ int32_t Solver::pcg_cheb(const float* b, float* x) {
       }
     }
     // one cooperative kernel for the (rest of the) solve
-    // (the primal Kp vector, free by now, holds the warm start's low parts)
-    const int32_t dual = run_dual(b, x, p_.tol_cg, p_.rel_tol_cg, left, warm,
-                                  primal() ? pv_[6].p : nullptr);
-    return its + dual;
+    int32_t total = its + run_dual(b, x, p_.tol_cg, p_.rel_tol_cg, left, warm, ulo_.p);
+    left = p_.maxiter_cg - total;
+    // float64 residual replacement: restart from the iterate with r = b - A x
+    // formed in float64 while that residual misses the tolerance
+    for (int32_t k = 0; k < p_.cg_refine && left > 0; ++k) {
+      if (status_ & (MGPBD_STATUS_NAN | MGPBD_STATUS_PAP_NONPOS)) break;
+      const int32_t more = run_dual(b, x, p_.tol_cg, p_.rel_tol_cg, left, true, ulo_.p);
+      total += more;
+      left -= more;
+      if (more == 0) break;
+    }
+    return total;
   }
   if (!p_.use_graph) {
     // same kernels from the host; every kernel is a no-op once done is set
@@ -1585,8 +1597,6 @@ void Solver::init_bodies(const std::vector<int32_t>& t_host) {
   body_active_.alloc(nb_);
   body_omega_.alloc(nb_);
   chunk_partials_.alloc(static_cast<int64_t>(kBodyTrials) * static_cast<int64_t>(chunk_body_.size()));
-  body_ulo_.alloc(nv_);
-  MGPBD_CUDA(cudaMemsetAsync(body_ulo_.p, 0, sizeof(float4) * nv_, s));
   body_newton_.assign(nb_, 0);
   body_r0_.assign(nb_, 0.0);
   body_r_.assign(nb_, 0.0);
@@ -1617,11 +1627,11 @@ int32_t Solver::pcg_bodies(const float* b, float* x, const std::vector<double>& 
   double bn2 = 0.0;
   for (double v : bnorm) bn2 += v * v;
   double tol = std::max<double>(p_.tol_cg, rel * std::sqrt(bn2));
-  int32_t total = 0, left = p_.maxiter_cg;
+  int32_t total = 0, left = p_.maxiter_cg, refine = 0;
   bool warm = false;
   std::vector<double> rb2;
-  for (int pass = 0; pass < 6 && left > 0; ++pass) {
-    const int32_t its = run_dual(b, x, tol, 0.0, left, warm, body_ulo_.p);
+  for (int pass = 0; pass < 6 + p_.cg_refine && left > 0; ++pass) {
+    const int32_t its = run_dual(b, x, tol, 0.0, left, warm, ulo_.p);
     total += its;
     left -= its;
     if (status_ & (MGPBD_STATUS_NAN | MGPBD_STATUS_PAP_NONPOS)) break;
@@ -1632,7 +1642,16 @@ int32_t Solver::pcg_bodies(const float* b, float* x, const std::vector<double>& 
       const double bound = std::max<double>(p_.tol_cg, rel * bnorm[k]);
       if (bnorm[k] > 0.0 && std::sqrt(rb2[k]) > bound) need = std::min(need, bound);
     }
-    if (!std::isfinite(need)) return total;
+    if (!std::isfinite(need)) {
+      // every body meets its bound on the residual the kernel ended with;
+      // with cg_refine, check that against the residual formed in float64
+      // (a warm restart that meets the bound at once runs no iteration and
+      // leaves that residual behind)
+      if ((warm && its == 0) || refine >= p_.cg_refine) return total;
+      ++refine;
+      warm = true;
+      continue;
+    }
     tol = need;
     warm = true;
   }

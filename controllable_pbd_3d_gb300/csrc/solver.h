@@ -193,7 +193,7 @@ class Solver {
   DevBuf<int32_t> chunks_, cons_body_, vert_body_, body_active_;
   DevBuf<float> body_omega_;
   DevBuf<double> chunk_partials_;
-  DevBuf<float4> body_ulo_;  // warm restarts of the verified CG solve
+  DevBuf<float4> ulo_;  // warm restarts of the dual CG: low parts of u (float64 residual)
   std::vector<int32_t> body_newton_;
   std::vector<double> body_r0_, body_r_, body_omega_h_;
   Csr mat_csr_;                  // its structure and values (host)

@@ -35,6 +35,7 @@ struct Lvl {
   std::vector<int32_t> mptr, mrows;          // next level members
   std::vector<int32_t> coff, cidx;           // refill from previous level
   std::vector<float> b, x, x2, r;
+  std::vector<float> pw;  // power-iteration vector, kept across Newton iterations
 };
 
 struct Cpu {
@@ -300,9 +301,13 @@ void fill(Cpu& c) {
       Cl.dinv[i] = std::fabs(d) > 1e-30f ? 1.0f / d : 0.0f;
     }
   }
-  // smoother weights: power iteration on D^-1 A
+  // smoother weights: power iteration on D^-1 A, six steps per Newton
+  // iteration continuing from the previous iteration's vector (as the GPU
+  // plain path does: restarting from a smooth vector every time would
+  // underestimate lambda_max and make the smoother diverge)
   for (Lvl& l : c.L) {
-    std::vector<float> v(l.n, 1.0f), w(l.n);
+    std::vector<float>& v = l.pw;
+    std::vector<float> w(l.n);
     double lam = 1;
     for (int it = 0; it < 6; ++it) {
       double nn = 0;
@@ -516,6 +521,12 @@ int cpu_add_level(void* h, int n, const int32_t* ip, const int32_t* ix, int64_t 
   l.x.assign(n, 0.0f);
   l.x2.assign(n, 0.0f);
   l.r.assign(n, 0.0f);
+  l.pw.resize(n);
+  for (int i = 0; i < n; ++i) {  // the GPU's pseudo-random start vector
+    uint32_t hsh = static_cast<uint32_t>(i) * 2654435761u;
+    hsh ^= hsh >> 15;
+    l.pw[i] = 0.5f + (hsh & 0xffff) * (1.0f / 65536.0f);
+  }
   if (!c.L.empty()) {
     Lvl& F = c.L.back();
     F.agg.assign(agg_prev, agg_prev + F.n);

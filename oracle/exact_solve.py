@@ -147,3 +147,62 @@ class ExactDualSolve:
       if rel <= tol:
         break
     return dlam, rel
+
+
+# ----------------------------------------------------------------------------
+# the FAST step's linear solve, restated in float64
+# ----------------------------------------------------------------------------
+
+
+def chebyshev_pcg(apply_A, b, degree=8, lo=1e-3, scale=None, rel_tol=1e-6, tol_abs=0.0,
+                  maxiter=6000, lmax=None):
+  """CG preconditioned by a degree-`degree` Chebyshev polynomial in S A
+  (S = diag(scale), or the identity) on [lo * 1.02 lmax, 1.02 lmax], lmax
+  the largest eigenvalue of S A (Lanczos to 1e-10 unless given), from
+  x = 0, until |r| < max(tol_abs, rel_tol |b|): the linear solve of the
+  library's FAST mode in float64.  Returns (x, iterations)."""
+  b = np.asarray(b, np.float64)
+  n = len(b)
+  sc = np.ones(n) if scale is None else np.asarray(scale, np.float64)
+  if lmax is None:
+    op = sla.LinearOperator((n, n), matvec=lambda v: np.sqrt(sc) * apply_A(np.sqrt(sc) * v),
+                            dtype=np.float64)
+    lmax = float(sla.eigsh(op, k=1, which='LA', tol=1e-10, return_eigenvectors=False)[0])
+  hi = 1.02 * lmax
+  a_ = lo * hi
+  theta, delta = 0.5 * (hi + a_), 0.5 * (hi - a_)
+  sigma = theta / delta
+
+  def precond(r):
+    x = np.zeros_like(r)
+    rr = r.copy()
+    d = sc * rr / theta
+    rho = 1.0 / sigma
+    for _ in range(degree):
+      x += d
+      rr -= apply_A(d)
+      rho_n = 1.0 / (2.0 * sigma - rho)
+      d = rho_n * rho * d + 2.0 * rho_n / delta * (sc * rr)
+      rho = rho_n
+    return x
+
+  x = np.zeros(n)
+  r = b.copy()
+  tol = max(tol_abs, rel_tol * np.linalg.norm(b))
+  if np.linalg.norm(r) < tol:
+    return x, 0
+  z = precond(r)
+  p = z.copy()
+  rz = r @ z
+  for k in range(maxiter):
+    ap = apply_A(p)
+    alpha = rz / (p @ ap)
+    x += alpha * p
+    r -= alpha * ap
+    if np.linalg.norm(r) < tol:
+      return x, k + 1
+    z = precond(r)
+    rz_new = r @ z
+    p = z + (rz_new / rz) * p
+    rz = rz_new
+  return x, maxiter

@@ -479,11 +479,14 @@ class MGPBDOracle:
     """linear='pcg': the reference's V-cycle PCG; 'exact': each Newton
     system solved to a float64 dual residual of exact_tol |b|
     (oracle/exact_solve.py), for checking positions against the step with
-    an exact linear solve (float64 only)."""
-    if linear not in ('pcg', 'exact'):
-      raise ValueError("linear must be 'pcg' or 'exact'")
-    if linear == 'exact' and dtype != np.float64:
-      raise ValueError("linear='exact' is a float64 oracle")
+    an exact linear solve; 'cheb': the library's FAST linear solve (CG
+    with a Chebyshev-8 polynomial in A, lo 1e-3, to rel_tol_cg) in float64,
+    the same algorithm as the CUDA path in exact arithmetic's stead (both
+    float64 only)."""
+    if linear not in ('pcg', 'exact', 'cheb'):
+      raise ValueError("linear must be 'pcg', 'exact' or 'cheb'")
+    if linear != 'pcg' and dtype != np.float64:
+      raise ValueError(f"linear='{linear}' is a float64 oracle")
     self.linear = linear
     self.exact_tol = exact_tol
     self.exact_log = []
@@ -530,8 +533,8 @@ class MGPBDOracle:
                                                         self.compliance, self.ctype)
     self.lam = np.zeros(self.nt, f)
     self.C, self.gradC = constraints(self.x, self.t_i, self.dm_inv, f, self.ctype, self.rest_vol)
-    if self.linear == 'exact':
-      self.levels = []  # no assembled matrix: the exact solve is matrix-free in A
+    if self.linear != 'pcg':
+      self.levels = []  # no assembled matrix: these solves are matrix-free in A
       return
     ip, ix = sparsity_pattern(self.t_i, self.nt)
     L0 = Level(ip, ix, f)
@@ -755,6 +758,15 @@ class MGPBDOracle:
         dlam, rel = ex.solve(b, self.exact_tol)
         self.exact_log.append((ite, rel, list(ex.iters)))
         it = 0
+      elif self.linear == 'cheb':
+        from .exact_solve import chebyshev_pcg, constraint_jacobian
+        J = constraint_jacobian(self.t_i, self.gradC, self.nv)
+        Jt = J.T.tocsr()
+        w3 = np.repeat(np.asarray(self.invm, np.float64), 3)
+        al = np.asarray(self.alpha, np.float64)
+        dlam, it = chebyshev_pcg(lambda v: al * v + J @ (w3 * (Jt @ v)), b,
+                                 rel_tol=self.rel_tol_cg, tol_abs=self.tol_cg,
+                                 maxiter=self.maxiter_cg)
       else:
         self.fill_matrices()
         dlam, it = self.pcg(b)

@@ -2,7 +2,8 @@
 linear solves): run here on the CPU, the fixtures are committed.
 
     python tests/golden/make_headline.py c1            # -> headline_c1.npz
-    python tests/golden/make_headline.py cube N S K    # -> headline_N_seedS.npz
+    python tests/golden/make_headline.py cube N S K [cheb]
+                              # -> headline_N_seedS.npz (headline_N_seedS_cheb.npz)
 
 * c1: the 10 x 10 x 10 hex cube (1,331 vertices, 5,000 tets; length +
   volume constraints), compliance 1e-6, 100 frames x 5 substeps (dt 1/300),
@@ -16,7 +17,9 @@ linear solves): run here on the CPU, the fixtures are committed.
 
 Newton settings are the benchmark's (maxiter 20, atol 1e-4, rtol 1e-2, no
 damping, pinned vertices kinematic).  Each Newton system is solved to a
-float64 dual residual of 1e-11 |b| (oracle/exact_solve.py).  The Newton log
+float64 dual residual of 1e-11 |b| (oracle/exact_solve.py), or, with
+`cheb`, by the library's FAST linear solve restated in float64 (Chebyshev-8
+CG on A to relative residual 1e-6): the same algorithm as the CUDA path.  The Newton log
 of every substep (residual per iteration) is stored with the positions, so
 a test can see how far each substep's Newton test was from its threshold.
 """
@@ -49,12 +52,13 @@ def cube(n, seed):
   return xr, x0, t, invm, compliance
 
 
-def run(n, seed, compliance, substeps, keep):
+def run(n, seed, compliance, substeps, keep, linear='exact'):
   xr, x0, t, invm, drawn = cube(n, seed)
   comp = drawn if compliance is None else compliance
   c, ty, _, _ = MO.edge_volume_system(t)
   o = MO.MGPBDOracle(x0, xr, invm, c, [0.0, -9.8, 0.0], DT, dtype=np.float64, compliance=comp,
-                     ctype=ty, linear='exact', **NEWTON)
+                     ctype=ty, linear=linear, rel_tol_cg=1e-6, tol_cg=1e-12, maxiter_cg=6000,
+                     **NEWTON)
   o.init()
   snaps, idx, logs = [], [], []
   t0 = time.perf_counter()
@@ -83,9 +87,11 @@ def main():
                         compliance=d['compliance'])
   elif case == 'cube':
     n, seed, k = int(sys.argv[2]), int(sys.argv[3]), int(sys.argv[4])
-    d = run(n, seed, None, k, lambda k: True)
+    linear = sys.argv[5] if len(sys.argv) > 5 else 'exact'
+    d = run(n, seed, None, k, lambda k: True, linear)
     disp = (d['snaps'] - d['x0'][None].astype(np.float64)).astype(np.float32)
-    np.savez_compressed(os.path.join(HERE, f'headline_{n}_seed{seed}.npz'), disp=disp,
+    tag = '' if linear == 'exact' else f'_{linear}'
+    np.savez_compressed(os.path.join(HERE, f'headline_{n}_seed{seed}{tag}.npz'), disp=disp,
                         substeps=d['substeps'], newton_residuals=d['newton_residuals'],
                         compliance=d['compliance'])
   else:

@@ -107,7 +107,8 @@ def test_reference_arm_prints_one_contract_line():
   # whole substeps actually timed, the workload described as the GPU arm does
   assert d['steps'] >= 1 and d['steps_requested'] == 1 and cb['cpu_model']
   assert 'whole substep' in cb['sample']
-  assert set(d['config']) == {'workload', 'n_verts', 'n_tets', 'constraints', 'n_constraints',
+  assert d["cg_iters_per_step"] < 20000  # the CPU port converges (no cap)
+  assert set(d["config"]) == {'workload', 'n_verts', 'n_tets', 'constraints', 'n_constraints',
                               'nnz_level0', 'compliance', 'dt', 'rel_res_cg', 'l2',
                               'parallelism'}
   assert d['config']['n_tets'] == 5000 and d['config']['n_constraints'] == 11930

@@ -200,3 +200,17 @@ def test_fast_and_plain_reach_the_same_positions_at_40(cuda):
   a = xf.cpu().numpy().astype(np.float64)
   b = xp.cpu().numpy().astype(np.float64)
   assert np.abs(a - b).max() <= POS_TOL * np.abs(b).max()
+
+
+def test_the_fast_algorithm_in_float64_is_the_exact_step():
+  """The library's FAST linear solve restated in float64 (Chebyshev-8 CG on
+  A to relative residual 1e-6, `linear='cheb'`) lands within 1e-8 of the
+  exact-solve oracle on the stiffest draw (20^3, compliance 2.7e-9): the
+  solve tolerance is not what separates a float32 run from float64 there."""
+  z = golden('headline_20_seed3.npz')
+  c = golden('headline_20_seed3_cheb.npz')
+  _, x0, _, _, _ = scenarios.cube_body(20, 3)
+  for i in range(len(z['disp'])):
+    a = x0 + z['disp'][i].astype(np.float64)
+    b = x0 + c['disp'][i].astype(np.float64)
+    assert np.abs(a - b).max() <= 1e-8 * np.abs(a).max(), i
