@@ -62,7 +62,6 @@ class Params(C.Structure):
       ('compliance', f32), ('precond', i32), ('cheb_degree', i32), ('cheb_lo', f32),
       ('use_graph', i32), ('persistent', i32), ('primal', i32), ('primal_tol', f32),
       ('learned_accept', f32), ('learned_stall', i32), ('cheb_scale', i32),
-      ('cg_refine', i32),
   ]
 
 

@@ -117,7 +117,6 @@ void mgpbd_default_params(mgpbd_params* p) {
   p->learned_accept = 0.1f;
   p->learned_stall = 1000;
   p->cheb_scale = MGPBD_CHEB_JACOBI;
-  p->cg_refine = 0;
 }
 
 const char* mgpbd_strerror(int code) {

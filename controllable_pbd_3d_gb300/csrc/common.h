@@ -18,12 +18,17 @@ struct Error : std::runtime_error {
   Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
 };
 
+// A failed call also leaves its error as the runtime's "last error"; it is
+// read back (cleared) here so the next launch check does not report it
+// again (sticky errors of a lost context stay, as they must).
 #define MGPBD_CUDA(call)                                                           \
   do {                                                                             \
     cudaError_t err_ = (call);                                                     \
-    if (err_ != cudaSuccess)                                                       \
+    if (err_ != cudaSuccess) {                                                     \
+      (void)cudaGetLastError();                                                    \
       throw ::mgpbd::Error(MGPBD_ECUDA, std::string(#call) + ": " +                \
                                             cudaGetErrorString(err_));             \
+    }                                                                              \
   } while (0)
 
 // Every kernel launch of the library goes through this macro, which also

@@ -606,8 +606,14 @@ __global__ void __launch_bounds__(kPT, STAGED ? 1 : 2) k_jcg(PArgs a) {
     bf = s_scal;
   }
 
-  // the compensated sum, rounded once
-  for (int64_t t = o.tbeg; t < o.tend; t += o.tstep) a.x[t] = a.x[t] - a.xc[t];
+  // the compensated sum, rounded once; xc keeps what the rounding dropped
+  // (x + xc is the solution as a float pair, for the float64 scatter)
+  for (int64_t t = o.tbeg; t < o.tend; t += o.tstep) {
+    const float s = a.x[t], c = a.xc[t];
+    const float hi = s - c;
+    a.xc[t] = (s - hi) - c;
+    a.x[t] = hi;
+  }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     CgState* st = a.st;
     st->rz = rz;
@@ -749,6 +755,11 @@ void launch_jcg_persistent(const JView& j, const JcgVecs& v, const JcgPlan& plan
   void* args[] = {&a};
   const void* fn = plan.staged ? reinterpret_cast<const void*>(k_jcg<true>)
                                : reinterpret_cast<const void*>(k_jcg<false>);
+  // the dynamic shared-memory limit is a per-function attribute shared by
+  // every handle in the process: set this plan's before each staged launch
+  if (plan.staged)
+    MGPBD_CUDA(cudaFuncSetAttribute(k_jcg<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    plan.smem));
   MGPBD_CUDA(cudaLaunchCooperativeKernel(fn, dim3(plan.grid), dim3(kPT), args,
                                          static_cast<size_t>(plan.smem), s));
   MGPBD_CHECK_LAUNCH();

@@ -437,12 +437,30 @@ __global__ void k_lambda_update(float* __restrict__ lambda, const float* __restr
 // _zero_dpos + _scatter_dlam_gpu (cons/mgpbd_gpu.py:330-355): gathered per
 // vertex over its incident (tet, slot) pairs in ascending tet order, so the
 // float32 sum has the order of a serial run of the reference loop.
+// With dlam_lo (the low part of a float-pair solution) the sum runs in
+// float64 over dlam + dlam_lo: on stiff bodies dpos is a small difference
+// of large terms w dlam g, whose float32 rounding would otherwise reach the
+// 1e-5 level in positions.
 __global__ void k_scatter(const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc_ent,
                           const float* __restrict__ invm, const float* __restrict__ dlam,
-                          const float* __restrict__ gradC, float* __restrict__ dpos, int32_t nv) {
+                          const float* __restrict__ dlam_lo, const float* __restrict__ gradC,
+                          float* __restrict__ dpos, int32_t nv) {
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv;
        v += (int64_t)gridDim.x * blockDim.x) {
     float w = invm[v];
+    if (dlam_lo) {
+      double ax = 0.0, ay = 0.0, az = 0.0;
+      for (int32_t k = inc_ptr[v]; k < inc_ptr[v + 1]; ++k) {
+        int32_t e = inc_ent[k];  // 4 * tet + slot
+        const double sc = (double)w * ((double)dlam[e >> 2] + (double)dlam_lo[e >> 2]);
+        const float* g = gradC + 3 * (int64_t)e;
+        ax += sc * (double)g[0];
+        ay += sc * (double)g[1];
+        az += sc * (double)g[2];
+      }
+      st3(dpos, v, make_float3((float)ax, (float)ay, (float)az));
+      continue;
+    }
     float3 acc = make_float3(0.0f, 0.0f, 0.0f);
     for (int32_t k = inc_ptr[v]; k < inc_ptr[v + 1]; ++k) {
       int32_t e = inc_ent[k];  // 4 * tet + slot
@@ -1087,9 +1105,11 @@ void launch_lambda_update(float* lambda, const float* dlam, int32_t nt, cudaStre
 }
 
 void launch_scatter(const int32_t* inc_ptr, const int32_t* inc_ent, const float* invm,
-                    const float* dlam, const float* gradC, float* dpos, int32_t nv, cudaStream_t s) {
+                    const float* dlam, const float* gradC, float* dpos, int32_t nv, cudaStream_t s,
+                    const float* dlam_lo) {
   if (nv <= 0) return;
-  k_scatter<<<grid_for(nv, kThreads), kThreads, 0, s>>>(inc_ptr, inc_ent, invm, dlam, gradC, dpos, nv);
+  k_scatter<<<grid_for(nv, kThreads), kThreads, 0, s>>>(inc_ptr, inc_ent, invm, dlam, dlam_lo,
+                                                        gradC, dpos, nv);
   MGPBD_CHECK_LAUNCH();
 }
 

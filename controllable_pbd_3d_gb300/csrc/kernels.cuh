@@ -40,11 +40,12 @@ void launch_dual_trial(const float* x, const float* dpos, const double* omegas, 
                        const float* rest, const float* alpha, const float* lambda, int32_t nt,
                        double* partials, cudaStream_t s);
 // lambda += dlam; dpos[v] = sum over incident (t,l) ascending of
-// w_v * dlam_t * gradC[t,l]
+// w_v * dlam_t * gradC[t,l] (float32; with dlam_lo, the low part of a
+// float-pair dlam, in float64 over dlam + dlam_lo)
 void launch_lambda_update(float* lambda, const float* dlam, int32_t nt, cudaStream_t s);
 void launch_scatter(const int32_t* inc_ptr, const int32_t* inc_ent, const float* invm,
-                    const float* dlam, const float* gradC, float* dpos, int32_t nv,
-                    cudaStream_t s);
+                    const float* dlam, const float* gradC, float* dpos, int32_t nv, cudaStream_t s,
+                    const float* dlam_lo = nullptr);
 // per-body reductions of a packed batch over constraint chunks (int2 begin,
 // end; each inside one body): partials[c] = sum of (C + alpha lambda)^2
 // over chunk c (alpha = null: sum of C^2)

@@ -868,6 +868,10 @@ void launch_pcg_primal(const JView& j, const PcgVecs& v, const JcgPlan& plan,
   const size_t smem = plan.staged ? static_cast<size_t>(staged_smem_bytes(plan.emax, plan.tmax,
                                                                            plan.vmax))
                                   : 0;
+  // per-function attribute shared by every handle: set this plan's limit
+  if (plan.staged)
+    MGPBD_CUDA(cudaFuncSetAttribute(k_pcg<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(smem)));
   MGPBD_CUDA(cudaLaunchCooperativeKernel(fn, dim3(plan.grid), dim3(kPT), args, smem, s));
   MGPBD_CHECK_LAUNCH();
 }

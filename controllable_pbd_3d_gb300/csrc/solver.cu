@@ -818,18 +818,7 @@ int32_t Solver::pcg_cheb(const float* b, float* x) {
       }
     }
     // one cooperative kernel for the (rest of the) solve
-    int32_t total = its + run_dual(b, x, p_.tol_cg, p_.rel_tol_cg, left, warm, ulo_.p);
-    left = p_.maxiter_cg - total;
-    // float64 residual replacement: restart from the iterate with r = b - A x
-    // formed in float64 while that residual misses the tolerance
-    for (int32_t k = 0; k < p_.cg_refine && left > 0; ++k) {
-      if (status_ & (MGPBD_STATUS_NAN | MGPBD_STATUS_PAP_NONPOS)) break;
-      const int32_t more = run_dual(b, x, p_.tol_cg, p_.rel_tol_cg, left, true, ulo_.p);
-      total += more;
-      left -= more;
-      if (more == 0) break;
-    }
-    return total;
+    return its + run_dual(b, x, p_.tol_cg, p_.rel_tol_cg, left, warm, ulo_.p);
   }
   if (!p_.use_graph) {
     // same kernels from the host; every kernel is a no-op once done is set
@@ -1278,6 +1267,7 @@ int32_t Solver::pcg_learned(const float* b, float* x) {
 // GPUMultigridSolver.solve (cons/mgpcg_gpu.py:261-329)
 int32_t Solver::pcg(const float* b, float* x) {
   require_init();
+  dual_x_ = nullptr;
   if (cheb()) return pcg_cheb(b, x);
   if (learned()) return pcg_learned(b, x);
   if (p_.mode == MGPBD_MODE_FAST && p_.use_graph && b == rhs_.p && x == dlam_.p &&
@@ -1393,7 +1383,10 @@ int32_t Solver::pcg_graph(const float* b, float* x) {
 void Solver::scatter(const float* dlam) {
   require_mesh();
   launch_lambda_update(lambda_.p, dlam, nt_, stream_);
-  launch_scatter(inc_ptr_.p, inc_ent_.p, invm_, dlam, gradC_.p, dpos_.p, nv_, stream_);
+  // after a persistent dual solve into this dlam, its low part (jxc_) joins
+  // a float64 scatter
+  const float* lo = (dual_x_ != nullptr && dual_x_ == dlam) ? jxc_.p : nullptr;
+  launch_scatter(inc_ptr_.p, inc_ent_.p, invm_, dlam, gradC_.p, dpos_.p, nv_, stream_, lo);
 }
 
 // _line_search (cons/mgpbd_gpu.py:379-391): backtracking from omega = 1 by
@@ -1514,8 +1507,10 @@ int32_t Solver::run_dual(const float* b, float* x, double tol_abs, double tol_re
   v.gs = jgs_.p;
   v.ulo = ulo;
   MGPBD_CUDA(cudaEventRecord(ev_[0], outer));
+  dual_x_ = nullptr;
   launch_jcg_persistent(jview(), v, jplan_, jpart_.p, jst_.p, cg_state_.p, tol_abs, tol_rel, maxit,
                         p_.cheb_degree, warm, barrier_limit_s_, outer);
+  dual_x_ = x;
   MGPBD_CUDA(cudaEventRecord(ev_[1], outer));
   sync_read(h_state_, cg_state_.p, sizeof(CgState));
   stats_.ms_dual += event_ms(ev_[0], ev_[1]);
@@ -1627,10 +1622,10 @@ int32_t Solver::pcg_bodies(const float* b, float* x, const std::vector<double>& 
   double bn2 = 0.0;
   for (double v : bnorm) bn2 += v * v;
   double tol = std::max<double>(p_.tol_cg, rel * std::sqrt(bn2));
-  int32_t total = 0, left = p_.maxiter_cg, refine = 0;
+  int32_t total = 0, left = p_.maxiter_cg;
   bool warm = false;
   std::vector<double> rb2;
-  for (int pass = 0; pass < 6 + p_.cg_refine && left > 0; ++pass) {
+  for (int pass = 0; pass < 6 && left > 0; ++pass) {
     const int32_t its = run_dual(b, x, tol, 0.0, left, warm, ulo_.p);
     total += its;
     left -= its;
@@ -1642,16 +1637,7 @@ int32_t Solver::pcg_bodies(const float* b, float* x, const std::vector<double>& 
       const double bound = std::max<double>(p_.tol_cg, rel * bnorm[k]);
       if (bnorm[k] > 0.0 && std::sqrt(rb2[k]) > bound) need = std::min(need, bound);
     }
-    if (!std::isfinite(need)) {
-      // every body meets its bound on the residual the kernel ended with;
-      // with cg_refine, check that against the residual formed in float64
-      // (a warm restart that meets the bound at once runs no iteration and
-      // leaves that residual behind)
-      if ((warm && its == 0) || refine >= p_.cg_refine) return total;
-      ++refine;
-      warm = true;
-      continue;
-    }
+    if (!std::isfinite(need)) return total;
     tol = need;
     warm = true;
   }
@@ -1725,6 +1711,7 @@ void Solver::solve_bodies() {
                                cudaMemcpyHostToDevice, s));
     launch_mask_rhs(rhs_.p, cons_body_.p, body_active_.p, nt_, s);
     fill_matrices();
+    dual_x_ = nullptr;
     const int32_t it = pcg_bodies(rhs_.p, dlam_.p, bnorm);
     scatter(dlam_.p);
     // per-body line search (cons/mgpbd_gpu.py:379-391): the first of 1,

@@ -187,6 +187,7 @@ class Solver {
   bool inited_ = false;
   bool matrix_mode_ = false;     // set_matrix: a caller's level-0 matrix, no mesh
   double barrier_limit_s_ = 4.0; // grid-barrier wait limit of the persistent kernels
+  const float* dual_x_ = nullptr;  // x of the last persistent dual solve (its low part in jxc_)
   // packed bodies (set_bodies)
   int32_t nb_ = 0;
   std::vector<int32_t> body_vert_off_, body_segs_, chunk_body_;

@@ -116,7 +116,7 @@ class MGPBDSolverGPU:
                aggregation='tet', benchmark=None, *, mode='parity', rel_tol_cg=0.0,
                coarse_solver='jacobi', smoother='jacobi', max_levels=0, max_coarse=400,
                kinematic_pins=False, coarse_sweeps=0, cg_alias=False, compliance=0.0,
-               precond='vcycle', cheb_degree=8, cheb_lo=0.01, cheb_scale='jacobi', cg_refine=0,
+               precond='vcycle', cheb_degree=8, cheb_lo=0.01, cheb_scale='jacobi',
                use_graph=True,
                persistent=True, primal=False, primal_tol=1e-2, learned_accept=0.1, learned_stall=1000,
                constraints='arap', check_finite=True):
@@ -205,7 +205,6 @@ class MGPBDSolverGPU:
     p.cheb_degree = int(cheb_degree)
     p.cheb_lo = float(cheb_lo)
     p.cheb_scale = {'jacobi': 0, 'none': 1}[cheb_scale]
-    p.cg_refine = int(cg_refine)
     p.use_graph = int(bool(use_graph))
     p.persistent = int(persistent)  # True / 1, 2 (unstaged) or False / 0
     p.primal = int(bool(primal))

@@ -160,15 +160,6 @@ typedef struct mgpbd_params {
    * band sits at the bottom of the spectrum, where CG pays for it.  No
    * counterpart in the reference. */
   int32_t cheb_scale;
-  /* MGPBD_PRECOND_CHEB, persistent: after the CG solve meets its tolerance
-   * on the float32 recurrence residual, up to this many restarts from its
-   * iterate with the residual b - A dlam formed in float64 (residual
-   * replacement), until the recomputed residual meets the tolerance (a
-   * restart that meets it at once costs no iteration).  The float32
-   * recurrence drifts from the true residual; at very small compliance the
-   * drift moves positions by more than 1e-5.  0 (default): none.  No
-   * counterpart in the reference. */
-  int32_t cg_refine;
 } mgpbd_params;
 
 #define MGPBD_CHEB_JACOBI 0
