@@ -32,6 +32,8 @@ from typing import Optional
 import numpy as np
 
 _FILE_KEYS = ('solver_name', 'mesh_name', 'params', 'frames')
+_FRAME_KEYS = ('frame_id', 'iterations', 't_start', 't_end')
+_ITER_KEYS = ('iteration', 'residual', 'cg_iters', 'omega', 't')
 
 
 def _device_sync():
@@ -56,6 +58,13 @@ class IterationRecord:
   def as_layout(self) -> dict:
     return {'iteration': self.iteration, 'residual': self.residual, 'cg_iters': self.cg_iters,
             'omega': self.omega, 't': self.t}
+
+  def __getitem__(self, key):
+    """Read access by the layout's key, as code written against the
+    reference recorder's dicts does (`it['residual']`)."""
+    if key not in _ITER_KEYS:
+      raise KeyError(key)
+    return getattr(self, key)
 
   @classmethod
   def from_layout(cls, d: dict) -> 'IterationRecord':
@@ -85,6 +94,13 @@ class FrameRecord:
   def as_layout(self) -> dict:
     return {'frame_id': self.frame_id, 'iterations': [it.as_layout() for it in self.iterations],
             't_start': self.t_start, 't_end': self.t_end}
+
+  def __getitem__(self, key):
+    """Read access by the layout's key (`frame['iterations']`), as on the
+    reference recorder's frame dicts."""
+    if key not in _FRAME_KEYS:
+      raise KeyError(key)
+    return getattr(self, key)
 
   @classmethod
   def from_layout(cls, d: dict) -> 'FrameRecord':

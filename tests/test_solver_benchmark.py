@@ -53,6 +53,11 @@ def test_new_record_has_the_reference_layout(tmp_path):
   assert list(fr) == list(rf)
   assert list(fr['iterations'][0]) == list(rf['iterations'][0])
   assert fr['iterations'][1]['t'] == 123.0
+  # frames read like the reference recorder's dicts
+  f0 = b.frames[0]
+  assert f0['frame_id'] == 0 and f0['iterations'][0]['cg_iters'] == 12
+  with pytest.raises(KeyError):
+    f0['nope']
   assert fr['t_start'] <= fr['iterations'][0]['t'] <= fr['t_end']
   s = SolverBenchmark.load(str(path)).summary()
   assert s['n_frames'] == 1 and s['avg_iterations'] == 2.0 and s['avg_final_residual'] == 0.25
