@@ -306,20 +306,16 @@ def operator_shape(s):
   return 4 * (s.n_tets - n2) + 2 * n2, n2
 
 
-# DRAM bytes (read + write: dram__bytes_read.sum + dram__bytes_write.sum) of
-# one launch of each persistent kernel on the 40^3 workload, from one ncu
-# capture each.  Length + volume: the timed substep's two launches of
-# `bench.py --no-cpu-baseline --no-plain --no-learned --no-arap --steps 1
-# --warmup 3` (-k regex:"k_pcg|k_jcg" -s 10 -c 2; 56 primal and 714 dual CG
-# iterations).  ARAP: `bench.py --profile-solve --size 40 --constraints arap`.
-TRAFFIC_40 = {'arap': {'k_pcg': 44874752, 'k_jcg': 46275840},
-              'edge_volume': {'k_pcg': 729190400, 'k_jcg': 81323029760}}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per CG iteration
+# of the dual persistent kernel on the 40^3 length + volume workload, from one
+# ncu capture of one launch of `bench.py --profile-solve --size 40` (461 CG
+# iterations, 56.87 GB; the unscaled Chebyshev-8 polynomial of the headline).
+# A launch's traffic is this times its iterations.
+TRAFFIC_PER_IT_40 = {'edge_volume': {'k_jcg': 56.87e9 / 461}}
 TRAFFIC_SOURCE = {
-    'arap': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of bench.py '
-            '--profile-solve --size 40 --constraints arap (same workload)',
-    'edge_volume': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of the timed substep\'s '
-                   'launches of bench.py --no-cpu-baseline --no-plain --no-learned --no-arap '
-                   '--steps 1 --warmup 3 (56 primal, 714 dual CG iterations)'}
+    'edge_volume': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of bench.py '
+                   '--profile-solve --size 40 (461 CG iterations, 56.87 GB), per iteration x '
+                   'this launch\'s iterations'}
 
 
 def roofline_from_steps(st, nt, nv, degree, hbm_peak, peak_kind, size=40, constraints='arap',
@@ -359,7 +355,8 @@ def roofline_from_steps(st, nt, nv, degree, hbm_peak, peak_kind, size=40, constr
                 'cg_iterations_per_launch': round(its / n, 1), 'launch_us': round(dt * 1e6, 1),
                 'us_per_cg_iteration': round(ms * 1e3 / max(its, 1), 2),
                 'share_of_step_gpu_time': None,
-                'traffic': (TRAFFIC_40.get(constraints, {}).get(name[:5]) if size == 40
+                'traffic': (int(TRAFFIC_PER_IT_40[constraints][name[:5]] * its / n)
+                            if size == 40 and name[:5] in TRAFFIC_PER_IT_40.get(constraints, {})
                             else None)})
   out.sort(key=lambda r: -r['launch_us'] * r['launches'])
   total = sum(r['launch_us'] * r['launches'] for r in out)
