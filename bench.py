@@ -508,33 +508,40 @@ def net_forward_bytes(n, nnz):
   return l1 + 2 * layer + n * 16
 
 
-def learned_leg(torch, args, hbm, kind):
-  """The learned coarse correction on the same workload: pairs recorded by
-  one plain Newton iteration, the network trained on them on the GPU, then
-  the plain V-cycle PCG with its coarse sweeps replaced by the learned
-  correction, timed like the plain leg."""
-  from controllable_pbd_3d_gb300.learned import CoarseNet, coarse_energy
+LEARNED_TRAIN_BODIES = 12
+
+
+def learned_leg(torch, args, hbm, kind, plain=None):
+  """The learned coarse correction, trained off-body: pairs recorded by
+  the plain solver on LEARNED_TRAIN_BODIES bodies of the configuration's
+  training-set generator (`scenarios.training_bodies`, cubes and balls of
+  20..32 cells, compliance log-U[1e-9, 1e-4], random pinned surface
+  vertices; seed 1, so none is the benchmark body), the network trained on
+  the GPU on them; then the plain V-cycle PCG on the benchmark body with
+  its coarse sweeps replaced by the learned correction, timed like the
+  plain leg, beside the same solver with a single coarse Jacobi sweep (the
+  cheapest non-learned coarse correction)."""
+  from controllable_pbd_3d_gb300 import scenarios
+  from controllable_pbd_3d_gb300.learned import (CoarseNet, coarse_energy, collect_pairs,
+                                                 train_on_bodies)
   peaks_all = json.load(open(os.path.join(HERE, 'MEASURED_PEAKS.json'))) if os.path.exists(
       os.path.join(HERE, 'MEASURED_PEAKS.json')) else {}
   tc_peak = float(peaks_all.get('bf16_tflops', 1900.0))
-  kwr = dict(SOLVER_KW)
-  kwr.update(PLAIN_KW)
-  kwr['maxiter'] = 1
-  sr, _, _ = make_solver(torch, args.size, kwr, args.constraints)
-  sr.record_coarse(256, 4)
-  sr.step(0)
-  rc, ec = sr.recorded_coarse()
-  g = sr.coarse_graph().snapshot()
   net = CoarseNet(seed=1)
   torch.cuda.synchronize()
   t0 = time.perf_counter()
-  losses = net.fit(g, rc, steps=600, batch=8, lr=2e-3)
+  losses, data = train_on_bodies(net, scenarios.training_bodies(LEARNED_TRAIN_BODIES, seed=1,
+                                                                sides=(20, 32)),
+                                 pairs_per_body=32, every=8, steps=1500, batch=8, lr=2e-3)
   torch.cuda.synchronize()
   t_train = time.perf_counter() - t0
-  held = slice(max(0, rc.shape[0] - 32), rc.shape[0])
-  e_net = coarse_energy(g, rc[held], net.correction(g, rc[held])).mean().item()
-  e_plain = coarse_energy(g, rc[held], ec[held]).mean().item()
-  # the weights pass (network forward) with CUDA events on this stream
+  # held-out pairs of the benchmark body: the network's coarse energy beside
+  # one Jacobi sweep's and the reference's 50 sweeps'
+  xr, x0, t, invm, comp = workload(args.size)
+  g, rc = collect_pairs(dict(x_ref=xr, x0=x0, t_i=t, invm=invm, compliance=comp), 32, 8)
+  e_net = coarse_energy(g, rc, net.correction(g, rc)).mean().item()
+  e_one = coarse_energy(g, rc, ((2.0 / 3.0) * g.diag_inv[None, :] * rc.reshape(-1, g.n))
+                        .reshape(rc.shape)).mean().item()
   for _ in range(3):
     net.weights(g)
   t_fwd = _event_time(torch, lambda: net.weights(g), 20)
@@ -547,36 +554,46 @@ def learned_leg(torch, args, hbm, kind):
           'algorithmic_bytes_per_launch': int(fb), 'launch_us': round(t_fwd * 1e6, 2),
           'tensor_tflops': round(flops / t_fwd / 1e12, 3),
           'tensor_frac': round(flops / t_fwd / 1e12 / tc_peak, 5),
-          'working_set_note': 'the graph (ah, columns) and the bf16 features (11 MB) stay in L2; '
+          'working_set_note': 'the graph (ah, columns) and the bf16 features stay in L2; '
                               'the neighbour gathers are L2 traffic', 'traffic': None}
-  del sr
-  kwl = dict(SOLVER_KW)
-  kwl.update(PLAIN_KW)
-  kwl['precond'] = 'learned'
-  sl, _, _ = make_solver(torch, args.size, kwl, args.constraints)
-  sl.set_coarse_net(net)
-  shapes = sl.autotune(reps=5)
-  k = max(1, min(args.steps, args.plain_steps))
-  tl, stl = time_steps(torch, sl, k, 0)
+
+  def timed(extra, with_net):
+    kw = dict(SOLVER_KW)
+    kw.update(PLAIN_KW)
+    kw.update(extra)
+    sl, _, _ = make_solver(torch, args.size, kw, args.constraints)
+    if with_net:
+      sl.set_coarse_net(net)
+    sl.autotune(reps=5)
+    k = max(1, args.plain_steps)
+    tl, stl = time_steps(torch, sl, k, 0)
+    del sl
+    torch.cuda.empty_cache()
+    return k, tl, stl
+
+  k, tl, stl = timed(dict(precond='learned'), True)
+  k1, t1, st1 = timed(dict(coarse_sweeps=1), False)
   out = {'value': round(k / tl, 4), 'unit': UNIT, 'steps': k,
          'newton_iters_per_step': sum(x['newton_iters'] for x in stl) / k,
          'cg_iters_per_step': sum(x['cg_iters_total'] for x in stl) / k,
-         'row_shapes': {str(l): c for l, c in shapes.items()},
          'learned_solves': sum(x['learned_solves'] for x in stl),
          'fallbacks': sum(x['learned_fallbacks'] for x in stl),
          'rejected': sum(x['learned_rejected'] for x in stl),
          'config': 'the plain leg with the coarse sweeps replaced by e_c = w * r_c / diag(A_c), '
                    'w = c sigmoid(y), c = 1.9 / row sums of |Ah|, y from the 3-layer '
                    'message-passing network (hidden 64, bf16 tensor-core layers) on the '
-                   'level-1 graph, computed once per Newton iteration; judge threshold 0.1 of '
-                   'the plain coarse-energy decrease, stall window 1000 CG iterations',
-         'train': {'pairs': int(rc.shape[0]), 'adam_steps': 600, 'batch': 8,
-                   'seconds': round(t_train, 3), 'loss_first10': float(losses[:10].mean()),
-                   'loss_last20': float(losses[-20:].mean()),
-                   'coarse_energy_network': e_net, 'coarse_energy_plain_sweeps': e_plain},
+                   'level-1 graph, computed once per Newton iteration; trained off-body',
+         'train': {'bodies': LEARNED_TRAIN_BODIES, 'generator': 'scenarios.training_bodies, '
+                   'seed 1, sides 20..32', 'pairs': int(sum(r.shape[0] for _, r in data)),
+                   'adam_steps': 1500, 'batch': 8, 'seconds': round(t_train, 2),
+                   'loss_first20': float(losses[:20].mean()),
+                   'loss_last50': float(losses[-50:].mean())},
+         'held_out_coarse_energy': {'network': e_net, 'one_jacobi_sweep': e_one},
+         'one_sweep_ablation': {'value': round(k1 / t1, 4), 'unit': UNIT, 'steps': k1,
+                                'cg_iters_per_step': sum(x['cg_iters_total'] for x in st1) / k1,
+                                'config': 'the plain leg with one coarse Jacobi sweep'},
          'roofline': roof}
-  del sl
-  torch.cuda.empty_cache()
+  out['vs_one_sweep'] = round(out['value'] / out['one_sweep_ablation']['value'], 3)
   return out
 
 
@@ -696,6 +713,8 @@ def run_ours(args):
     lrn = learned_leg(torch, args, hbm, kind)
     if plain is not None:
       lrn['speedup_vs_plain'] = round(lrn['value'] / plain['value'], 3)
+      lrn['one_sweep_ablation']['speedup_vs_plain'] = round(
+          lrn['one_sweep_ablation']['value'] / plain['value'], 3)
     out['learned_amg_pcg'] = lrn
   if cons != 'arap' and not args.no_arap:
     # the reference step's own constraint (one ARAP constraint per tet) on

@@ -281,11 +281,17 @@ def test_learned_pcg_solution_matches_direct_solve(cuda):
 @pytest.mark.gpu
 def test_learned_pcg_reports_the_gain(cuda):
   """Same Newton steps solved by the plain V-cycle PCG (the reference's
-  min(50, n) coarse sweeps) and by the learned one (network weights judged
-  by the plain V-cycle on each solve's first V-cycle): the network is kept
-  on every solve, no solve falls back or hits maxiter_cg, the Newton
-  iterations match, and the gain in solve time over the plain V-cycle is
-  reported (asserted to be a speed-up)."""
+  min(50, n) coarse sweeps), by the learned one (network weights judged by
+  the plain V-cycle on each solve's first V-cycle) and by the one-sweep
+  ablation (a single coarse Jacobi sweep, the cheapest non-learned coarse
+  correction): the network is kept on every solve, no solve falls back or
+  hits maxiter_cg, the Newton iterations match, and the gain in solve time
+  over the plain V-cycle is reported (asserted to be a speed-up).  Against
+  the one-sweep ablation the network is reported, not asserted: on this
+  system the coarse level carries a few percent of the CG iterations, and
+  measured off-body on the 40^3 benchmark body the network's held-out
+  coarse energy (-3.5e-5) does not reach one sweep's (-4.0e-5), 3.45 vs
+  3.24 s per substep."""
   torch = cuda
   _, _, net, _, _, _, _ = record_and_train(torch)
 
@@ -303,6 +309,14 @@ def test_learned_pcg_reports_the_gain(cuda):
 
   xp, sp_, tp = run('vcycle')
   xl, sl, tl = run('learned')
+  s1, x1 = cube_solver(torch, n=12, coarse_sweeps=1)
+  s1.make_prediction()
+  torch.cuda.synchronize()
+  t0 = time.perf_counter()
+  s1.solve(0)
+  torch.cuda.synchronize()
+  t1 = time.perf_counter() - t0
+  assert s1.stats()['newton_iters'] == sp_['newton_iters']
   assert sl['newton_iters'] == sp_['newton_iters']
   assert sl['learned_solves'] == sl['newton_iters'] and sl['learned_fallbacks'] == 0
   assert not (sl['status'] & 4)  # no CG solve hit maxiter_cg
@@ -310,7 +324,8 @@ def test_learned_pcg_reports_the_gain(cuda):
   print(f"\nplain V-cycle PCG: {sp_['cg_iters_total']} CG iterations, {tp * 1e3:.1f} ms; "
         f"learned: {sl['cg_iters_total']} CG iterations, {tl * 1e3:.1f} ms "
         f"({tp / tl:.2f}x); coarse energy of the first V-cycles: network "
-        f"{sl['coarse_energy_learned']:.3e}, plain {sl['coarse_energy_plain']:.3e}")
+        f"{sl['coarse_energy_learned']:.3e}, plain {sl['coarse_energy_plain']:.3e}; one-sweep "
+        f"ablation: {s1.stats()['cg_iters_total']} CG iterations, {t1 * 1e3:.1f} ms")
   assert tl < 0.8 * tp
 
 
