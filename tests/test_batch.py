@@ -150,8 +150,9 @@ def test_per_body_newton_equals_separate_substeps(cuda):
   and line-search step; the shared CG solve verified per body) land where
   each body's own substeps land: positions within 1e-5 relative after three
   substeps, and the same Newton iteration count per body.  The Newton loops
-  run to a tight test (rtol 1e-4: after one iteration r/r0 is ~1e-2, after
-  two ~1e-6) so every count is decided far from the test's threshold; the bodies differ in size
+  run to a test with margin on both sides (rtol 3e-3: after one iteration
+  r/r0 is ~1e-2, after two it sits at the float32 floor, 1e-5 .. 1e-4), so
+  every count is decided far from the threshold; the bodies differ in size
   and compliance, so they end their loops at different iterations.  (ARAP
   bodies are left out: the reference's ARAP step never meets its Newton
   test in 20 iterations, and a trajectory cut off mid-iteration is not a
@@ -161,7 +162,7 @@ def test_per_body_newton_equals_separate_substeps(cuda):
   from controllable_pbd_3d_gb300.mgpbd_gpu import MGPBDSolverGPU
   g, dt = [0.0, -9.8, 0.0], 1 / 300
   kw = dict(mode='fast', precond='cheb', cheb_scale='none', cheb_lo=1e-3, primal=False,
-            rel_tol_cg=1e-7, tol_cg=1e-14, maxiter_cg=6000, maxiter=10, atol=1e-9, rtol=1e-4,
+            rel_tol_cg=1e-7, tol_cg=1e-14, maxiter_cg=6000, maxiter=10, atol=1e-9, rtol=3e-3,
             kinematic_pins=True, constraints=constraints)
   bodies = random_bodies(4, seed=2, dims=(3, 7), compliance=(1e-8, 1e-5))
   batch = BodyBatch(bodies, g, dt, **kw)
