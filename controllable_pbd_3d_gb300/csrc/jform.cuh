@@ -55,6 +55,7 @@ struct JView {
   const float* invm = nullptr;       // (nv)
   const float* alpha = nullptr;      // (nt)
   const float* dinv = nullptr;       // (nt) 1 / diag(A)
+  bool unit_dinv = false;            // dinv is all ones (unscaled Chebyshev base)
   float4* u = nullptr;               // (nv) vertex scratch
   // compact length constraints (the persistent kernels' unstaged tet
   // phases): constraints n4 .. nt-1 are length constraints whose gradient n

@@ -714,6 +714,7 @@ JView Solver::jview() {
   j.invm = invm_;
   j.alpha = alpha_.p;
   j.dinv = jdinv_.p;
+  j.unit_dinv = p_.cheb_scale == MGPBD_CHEB_UNSCALED;
   j.u = u_.p;
   j.n4 = n4_;
   j.gE = gE_.p;
