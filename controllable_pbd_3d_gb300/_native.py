@@ -181,6 +181,8 @@ _SIGS = {
     'mgpbd_host_aggregate': (C.c_int, [vp, i32, i32, vp, P_i32]),
     'mgpbd_host_tet_hierarchy': (C.c_int, [vp, i32, i32, i32, P_i32, vp, vp]),
     'mgpbd_host_galerkin': (C.c_int, [i32, vp, vp, vp, vp, i32, P_i64, P_i64, vp, vp, vp, vp]),
+    'mgpbd_device_galerkin': (C.c_int, [i32, vp, vp, vp, vp, i32, P_i64, P_i64, vp, vp, vp, vp,
+                                        vp]),
     # include/mgpbd_local.h
     'mgpbd_color_elements': (C.c_int, [vp, i32, i32, i32, vp, vp, P_i32]),
     'mgpbd_color_vertices': (C.c_int, [vp, i32, i32, i32, vp, vp, P_i32]),

@@ -16,6 +16,7 @@
 #include "kernels.cuh"
 #include "local.cuh"
 #include "mpnn.cuh"
+#include "rap.cuh"
 #include "solver.h"
 #include "structure.h"
 
@@ -689,6 +690,72 @@ int mgpbd_host_galerkin(int32_t n, const int32_t* indptr, const int32_t* indices
       std::memcpy(c_indices, g.coarse.indices.data(), sizeof(int32_t) * g.coarse.indices.size());
       std::memcpy(contrib_idx, g.contrib_idx.data(), sizeof(int32_t) * g.contrib_idx.size());
       std::memcpy(contrib_off, g.contrib_off.data(), sizeof(int32_t) * g.contrib_off.size());
+    }
+  });
+}
+
+int mgpbd_device_galerkin(int32_t n, const int32_t* indptr, const int32_t* indices,
+                          const float* data, const int32_t* agg_ids, int32_t n_agg,
+                          int64_t* c_nnz, int64_t* n_contrib, int32_t* c_indptr,
+                          int32_t* c_indices, int32_t* contrib_idx, int32_t* contrib_off,
+                          int32_t* diag_pos) {
+  if (n <= 0 || !indptr || !indices || !agg_ids || n_agg <= 0 || !c_nnz || !n_contrib)
+    return MGPBD_EINVAL;
+  return guarded([&] {
+    using mgpbd::require;
+    require(indptr[0] == 0, MGPBD_EINVAL, "indptr must start at 0");
+    for (int32_t i = 0; i < n; ++i) {
+      require(indptr[i + 1] >= indptr[i], MGPBD_EINVAL, "indptr must not decrease");
+      for (int32_t k = indptr[i]; k < indptr[i + 1]; ++k)
+        require(indices[k] >= 0 && indices[k] < n, MGPBD_EINVAL, "column index outside [0, n)");
+      require(agg_ids[i] >= 0 && agg_ids[i] < n_agg, MGPBD_EINVAL, "aggregate id out of range");
+    }
+    const int64_t nnz = indptr[n];
+    require(nnz > 0, MGPBD_EINVAL, "empty matrix");
+    std::vector<int32_t> mp(n_agg + 1, 0), mr(n);
+    for (int32_t i = 0; i < n; ++i) mp[agg_ids[i] + 1]++;
+    for (int32_t a = 0; a < n_agg; ++a) mp[a + 1] += mp[a];
+    std::vector<int32_t> cur(mp.begin(), mp.end() - 1);
+    for (int32_t i = 0; i < n; ++i) mr[cur[agg_ids[i]]++] = i;
+    cudaStream_t s = nullptr;
+    MGPBD_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    struct StreamGuard {
+      cudaStream_t s;
+      ~StreamGuard() { cudaStreamDestroy(s); }
+    } guard{s};
+    auto put = [&](auto& d, const auto* h, int64_t count) {
+      d.alloc(std::max<int64_t>(count, 1));
+      MGPBD_CUDA(cudaMemcpyAsync(d.p, h, sizeof(*h) * count, cudaMemcpyHostToDevice, s));
+    };
+    mgpbd::DevBuf<int32_t> d_ip, d_ix, d_agg, d_mp, d_mr;
+    mgpbd::DevBuf<float> d_a;
+    put(d_ip, indptr, n + 1LL);
+    put(d_ix, indices, nnz);
+    put(d_agg, agg_ids, n);
+    put(d_mp, mp.data(), n_agg + 1LL);
+    put(d_mr, mr.data(), n);
+    if (data) put(d_a, data, nnz);
+    mgpbd::DeviceGalerkin g;
+    mgpbd::galerkin_device(n, nnz, d_ip.p, d_ix.p, data ? d_a.p : nullptr, d_agg.p, d_mp.p,
+                           d_mr.p, n_agg, g, s);
+    int32_t nmap = 0;
+    MGPBD_CUDA(cudaMemcpyAsync(&nmap, g.contrib_off.p + g.nnz, sizeof(int32_t),
+                               cudaMemcpyDeviceToHost, s));
+    MGPBD_CUDA(cudaStreamSynchronize(s));
+    *c_nnz = g.nnz;
+    *n_contrib = nmap;
+    if (c_indptr) {
+      require(c_indices && contrib_idx && contrib_off, MGPBD_EINVAL, "output buffer missing");
+      std::memcpy(c_indptr, g.host_indptr.data(), sizeof(int32_t) * (n_agg + 1LL));
+      std::memcpy(c_indices, g.host_indices.data(), sizeof(int32_t) * g.nnz);
+      MGPBD_CUDA(cudaMemcpyAsync(contrib_idx, g.contrib_idx.p, sizeof(int32_t) * nmap,
+                                 cudaMemcpyDeviceToHost, s));
+      MGPBD_CUDA(cudaMemcpyAsync(contrib_off, g.contrib_off.p, sizeof(int32_t) * (g.nnz + 1),
+                                 cudaMemcpyDeviceToHost, s));
+      if (diag_pos)
+        MGPBD_CUDA(cudaMemcpyAsync(diag_pos, g.diag_pos.p, sizeof(int32_t) * n_agg,
+                                   cudaMemcpyDeviceToHost, s));
+      MGPBD_CUDA(cudaStreamSynchronize(s));
     }
   });
 }

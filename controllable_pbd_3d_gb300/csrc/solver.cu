@@ -225,7 +225,7 @@ void Solver::init_matrix() {
   upload_padded(L0.data, mat_vals_, s);
   L0.diag_inv.alloc(nt_);
   launch_diag_inv_scan(L0.indptr.p, L0.indices.p, L0.data.p, L0.n, L0.diag_inv.p, s);
-  build_hierarchy({}, mat_vals_);
+  build_hierarchy({});
   alloc_work();
   inited_ = true;
   refill_coarse();
@@ -446,12 +446,7 @@ void Solver::init() {
   launch_constraints(x_, t_i_, ctype_.p, dm_inv_.p, rest_vol_.p, nt_, C_.p, gradC_.p, s);
   launch_fill_A(L0.indptr.p, L0.indices.p, t_i_, invm_, gradC_.p, alpha_.p, nt_, L0.data.p,
                 L0.diag_inv.p, s);
-  std::vector<float> a0(L0.nnz);
-  MGPBD_CUDA(cudaMemcpyAsync(a0.data(), L0.data.p, sizeof(float) * a0.size(),
-                             cudaMemcpyDeviceToHost, s));
-  MGPBD_CUDA(cudaStreamSynchronize(s));
-
-  build_hierarchy(t_host, a0);
+  build_hierarchy(t_host);
   alloc_work();
   MGPBD_CUDA(cudaStreamSynchronize(s));
   inited_ = true;
@@ -474,7 +469,40 @@ void Solver::init() {
   }
 }
 
-void Solver::build_hierarchy(const std::vector<int32_t>& t_host, const std::vector<float>& a0) {
+// Transfer maps of level l (aggregate id per row, the members of each
+// aggregate ascending) uploaded to the level.
+static void upload_transfer(Level& F, const std::vector<int32_t>& agg, int32_t n_agg,
+                            cudaStream_t s) {
+  std::vector<int32_t> mp(n_agg + 1, 0), mr(F.n);
+  for (int32_t i = 0; i < F.n; ++i) mp[agg[i] + 1]++;
+  for (int32_t a = 0; a < n_agg; ++a) mp[a + 1] += mp[a];
+  std::vector<int32_t> cur(mp.begin(), mp.end() - 1);
+  for (int32_t i = 0; i < F.n; ++i) mr[cur[agg[i]]++] = i;
+  upload(F.agg, agg, s);
+  upload(F.mem_ptr, mp, s);
+  upload(F.mem_rows, mr, s);
+}
+
+// The coarse level below levels_.back() from its device Galerkin build.
+void Solver::push_coarse(DeviceGalerkin& g, int32_t n_agg) {
+  cudaStream_t s = stream_;
+  levels_.emplace_back();
+  Level& C = levels_.back();
+  C.n = n_agg;
+  C.nnz = g.nnz;
+  C.indptr = std::move(g.indptr);
+  C.indices = std::move(g.indices);  // kCsrPad zeroed entries after the last
+  C.diag_pos = std::move(g.diag_pos);
+  C.contrib_off = std::move(g.contrib_off);
+  C.contrib_idx = std::move(g.contrib_idx);
+  alloc_padded(C.data, C.nnz, s);
+  C.diag_inv.alloc(C.n);
+  C.host.n_rows = C.host.n_cols = n_agg;
+  C.host.indptr = std::move(g.host_indptr);
+  C.host.indices = std::move(g.host_indices);
+}
+
+void Solver::build_hierarchy(const std::vector<int32_t>& t_host) {
   cudaStream_t s = stream_;
   int32_t max_coarse = p_.max_coarse > 0 ? p_.max_coarse : 400;
   // tet hierarchy (cons/tet_aggregation.py:145-211, max_levels = 4)
@@ -486,42 +514,18 @@ void Solver::build_hierarchy(const std::vector<int32_t>& t_host, const std::vect
   } else if (!matrix_mode_) {
     tet_hierarchy(t_host.data(), nt_, max_coarse, 4, sizes, aggs);
   }
-  std::vector<float> fine_vals = a0;
+  // Galerkin levels from the values on the device (level 0: the first A);
+  // each new level's values are refilled at once for the level after it
   for (size_t l = 0; l < aggs.size(); ++l) {
+    const int32_t n_agg = sizes[l + 1];
     Level& F = levels_[l];
-    int32_t n_agg = sizes[l + 1];
-    Galerkin g = galerkin(F.host, fine_vals.data(), aggs[l].data(), n_agg);
-    upload(F.agg, aggs[l], s);
-    std::vector<int32_t> mp(n_agg + 1, 0), mr(F.n);
-    for (int32_t i = 0; i < F.n; ++i) mp[aggs[l][i] + 1]++;
-    for (int32_t a = 0; a < n_agg; ++a) mp[a + 1] += mp[a];
-    {
-      std::vector<int32_t> cur(mp.begin(), mp.end() - 1);
-      for (int32_t i = 0; i < F.n; ++i) mr[cur[aggs[l][i]]++] = i;
-    }
-    upload(F.mem_ptr, mp, s);
-    upload(F.mem_rows, mr, s);
-    // host values of the coarse level (only needed if another value-based
-    // level follows; the tet hierarchy never has one)
-    std::vector<float> cv(g.coarse.nnz(), 0.0f);
-    for (int64_t c = 0; c < g.coarse.nnz(); ++c) {
-      float acc = 0.0f;
-      for (int32_t k = g.contrib_off[c]; k < g.contrib_off[c + 1]; ++k) acc += fine_vals[g.contrib_idx[k]];
-      cv[c] = acc;
-    }
-    levels_.emplace_back();
+    upload_transfer(F, aggs[l], n_agg, s);
+    DeviceGalerkin g;
+    galerkin_device(F.n, F.nnz, F.indptr.p, F.indices.p, F.data.p, F.agg.p, F.mem_ptr.p,
+                    F.mem_rows.p, n_agg, g, s);
+    push_coarse(g, n_agg);
     Level& C = levels_.back();
-    C.n = n_agg;
-    C.nnz = g.coarse.nnz();
-    upload(C.indptr, g.coarse.indptr, s);
-    upload_padded(C.indices, g.coarse.indices, s);
-    upload(C.diag_pos, g.diag_pos, s);
-    upload(C.contrib_off, g.contrib_off, s);
-    upload(C.contrib_idx, g.contrib_idx, s);
-    alloc_padded(C.data, C.nnz, s);
-    C.diag_inv.alloc(C.n);
-    C.host = std::move(g.coarse);
-    fine_vals.swap(cv);
+    launch_rap_refill(C.contrib_off.p, C.contrib_idx.p, levels_[l].data.p, C.nnz, C.data.p, s);
   }
   // optional extra levels by matrix-graph aggregation (not in the reference,
   // whose tet hierarchy stops at two levels)
@@ -531,29 +535,11 @@ void Solver::build_hierarchy(const std::vector<int32_t>& t_host, const std::vect
     std::vector<int32_t> agg;
     int32_t n_agg = graph_aggregate(F.host, 8, agg);
     if (n_agg >= F.n || n_agg <= 0) break;
-    Galerkin g = galerkin_structural(F.host, agg.data(), n_agg);
-    upload(F.agg, agg, s);
-    std::vector<int32_t> mp(n_agg + 1, 0), mr(F.n);
-    for (int32_t i = 0; i < F.n; ++i) mp[agg[i] + 1]++;
-    for (int32_t a = 0; a < n_agg; ++a) mp[a + 1] += mp[a];
-    {
-      std::vector<int32_t> cur(mp.begin(), mp.end() - 1);
-      for (int32_t i = 0; i < F.n; ++i) mr[cur[agg[i]]++] = i;
-    }
-    upload(F.mem_ptr, mp, s);
-    upload(F.mem_rows, mr, s);
-    levels_.emplace_back();
-    Level& C = levels_.back();
-    C.n = n_agg;
-    C.nnz = g.coarse.nnz();
-    upload(C.indptr, g.coarse.indptr, s);
-    upload_padded(C.indices, g.coarse.indices, s);
-    upload(C.diag_pos, g.diag_pos, s);
-    upload(C.contrib_off, g.contrib_off, s);
-    upload(C.contrib_idx, g.contrib_idx, s);
-    alloc_padded(C.data, C.nnz, s);
-    C.diag_inv.alloc(C.n);
-    C.host = std::move(g.coarse);
+    upload_transfer(F, agg, n_agg, s);
+    DeviceGalerkin g;
+    galerkin_device(F.n, F.nnz, F.indptr.p, F.indices.p, nullptr, F.agg.p, F.mem_ptr.p,
+                    F.mem_rows.p, n_agg, g, s);
+    push_coarse(g, n_agg);
     ++extra;
   }
   require(levels_.size() <= 8, MGPBD_ERANGE, "more than 8 multigrid levels");

@@ -12,6 +12,7 @@
 #include "jform.cuh"
 #include "kernels.cuh"
 #include "mpnn.cuh"
+#include "rap.cuh"
 #include "structure.h"
 
 namespace mgpbd {
@@ -145,7 +146,8 @@ class Solver {
   // the per-mesh stages need set_mesh (not a caller's matrix)
   void require_mesh() const;
   void init_matrix();
-  void build_hierarchy(const std::vector<int32_t>& t_i_host, const std::vector<float>& a0);
+  void build_hierarchy(const std::vector<int32_t>& t_i_host);
+  void push_coarse(DeviceGalerkin& g, int32_t n_agg);
   void alloc_work();
   // V-cycle on `l` with rhs b_l (device) and zero initial guess; the result
   // is left in levels_[l].xa.

@@ -138,3 +138,31 @@ def galerkin_structure(indptr, indices, data, agg_ids, n_agg):
                                       c_indptr.ctypes.data, c_indices.ctypes.data,
                                       cidx.ctypes.data, coff.ctypes.data), 'mgpbd_host_galerkin')
   return c_indptr, c_indices, cidx, coff
+
+
+def galerkin_structure_device(indptr, indices, data, agg_ids, n_agg):
+  """The same build on the GPU (`mgpbd_device_galerkin`; bit-identical to
+  `galerkin_structure`); data None gives the structural pattern.  Returns
+  (c_indptr, c_indices, contrib_idx, contrib_off, diag_pos)."""
+  ip = _as_i32(indptr)
+  ix = _as_i32(indices)
+  d = None if data is None else np.ascontiguousarray(data, dtype=np.float32)
+  dp = None if d is None else d.ctypes.data
+  ag = _as_i32(agg_ids)
+  n = len(ip) - 1
+  cn = C.c_int64(0)
+  nc = C.c_int64(0)
+  L = N.lib()
+  N.check(L.mgpbd_device_galerkin(n, ip.ctypes.data, ix.ctypes.data, dp, ag.ctypes.data,
+                                  int(n_agg), C.byref(cn), C.byref(nc), None, None, None, None,
+                                  None), 'mgpbd_device_galerkin')
+  c_indptr = np.empty(n_agg + 1, np.int32)
+  c_indices = np.empty(max(cn.value, 1), np.int32)
+  cidx = np.empty(max(nc.value, 1), np.int32)
+  coff = np.empty(cn.value + 1, np.int32)
+  diag = np.empty(n_agg, np.int32)
+  N.check(L.mgpbd_device_galerkin(n, ip.ctypes.data, ix.ctypes.data, dp, ag.ctypes.data,
+                                  int(n_agg), C.byref(cn), C.byref(nc), c_indptr.ctypes.data,
+                                  c_indices.ctypes.data, cidx.ctypes.data, coff.ctypes.data,
+                                  diag.ctypes.data), 'mgpbd_device_galerkin')
+  return c_indptr, c_indices[:cn.value], cidx[:nc.value], coff, diag

@@ -613,6 +613,20 @@ int mgpbd_host_galerkin(int32_t n, const int32_t* indptr, const int32_t* indices
                         int32_t* c_indices, int32_t* contrib_idx,
                         int32_t* contrib_off);
 
+/* The same Galerkin build on the GPU (one warp per coarse row, a float64
+ * hash accumulation in the host build's summation order): bit-identical
+ * outputs.  data == NULL gives the structural pattern (no value-based
+ * dropping), the build used below the tet hierarchy.  Host arrays in and
+ * out (copied to and from the device inside; the call blocks the host);
+ * diag_pos (n_agg, -1 where a coarse row has no diagonal) may be NULL.
+ * Replaces the host setup of cons/mgpcg_gpu.py:30-99; the solver's own
+ * hierarchy build (mgpbd_init) uses this builder on the device arrays. */
+int mgpbd_device_galerkin(int32_t n, const int32_t* indptr, const int32_t* indices,
+                          const float* data, const int32_t* agg_ids, int32_t n_agg,
+                          int64_t* c_nnz, int64_t* n_contrib, int32_t* c_indptr,
+                          int32_t* c_indices, int32_t* contrib_idx, int32_t* contrib_off,
+                          int32_t* diag_pos);
+
 #ifdef __cplusplus
 }
 #endif
