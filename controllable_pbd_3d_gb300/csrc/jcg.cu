@@ -85,6 +85,7 @@ struct PArgs {
   float4* ulo;   // warm start: low part of u (u = a.u + ulo, float64 sums)
   unsigned long long spin_ns;
   int32_t unit_dinv;  // 1: 1/diag is all ones (unscaled base): skip its loads
+  const JcgCtl* ctl;  // device-side tolerance / limit / start, or null
 };
 
 // (the staged kernel keeps the loads: the flag's test spills a register
@@ -364,6 +365,16 @@ __device__ __forceinline__ void tphase_ap(const PArgs& a, const Own& o, float bf
 
 template <bool STAGED>
 __global__ void __launch_bounds__(kPT, STAGED ? 1 : 2) k_jcg(PArgs a) {
+  // the control values (every block reads the same ones: a skipped launch
+  // leaves before its first barrier in every block)
+  int32_t warm = a.warm, maxiter = a.maxiter;
+  double tol_abs = a.tol_abs;
+  if (a.ctl) {
+    if (a.ctl->skip) return;
+    warm = a.ctl->warm;
+    maxiter = a.ctl->maxiter;
+    tol_abs = a.ctl->tol_abs;
+  }
   extern __shared__ __align__(16) unsigned char s_dyn[];
   __shared__ float s_c1[kMaxCheb], s_c2[kMaxCheb];
   __shared__ float s_scal;  // alpha or beta, broadcast from thread 0
@@ -436,7 +447,7 @@ __global__ void __launch_bounds__(kPT, STAGED ? 1 : 2) k_jcg(PArgs a) {
 
   // x = 0 (or the warm start x0), r = b - A x, p = 0, z = d = D^-1 r / theta;
   // partials of b.b and r.z
-  if (a.warm) {
+  if (warm) {
     vphase_warm<STAGED>(a, o);
     if (!grid_sync(a, gen)) return;
   }
@@ -445,7 +456,7 @@ __global__ void __launch_bounds__(kPT, STAGED ? 1 : 2) k_jcg(PArgs a) {
     for (int64_t t = o.tbeg; t < o.tend; t += o.tstep) {
       const float bt = a.b[t];
       float rt = bt;
-      if (a.warm) {
+      if (warm) {
         rt = (float)((double)bt - tdot_warm<STAGED>(a, o, t));
       } else {
         a.x[t] = 0.0f;
@@ -465,20 +476,20 @@ __global__ void __launch_bounds__(kPT, STAGED ? 1 : 2) k_jcg(PArgs a) {
     // a warm start may already meet the tolerance (a float64 residual
     // replacement after a converged solve): its r.r decides below; P2 is
     // first rewritten after the next grid barrier
-    if (a.warm) put_partial(br, P2);
+    if (warm) put_partial(br, P2);
   }
   if (!grid_sync(a, gen)) return;
   if (threadIdx.x < 32) {
     const double sb = warp_sum_partials(P0, G);
     const double sz = warp_sum_partials(P1, G);
-    const double s0 = a.warm ? warp_sum_partials(P2, G) : sb;
+    const double s0 = warm ? warp_sum_partials(P2, G) : sb;
     if (threadIdx.x == 0) {
       bbs = sb;
       rz = sz;
       rr = s0;
-      const double t2 = a.tol_abs * a.tol_abs, r2 = a.tol_rel * a.tol_rel * bbs;
+      const double t2 = tol_abs * tol_abs, r2 = a.tol_rel * a.tol_rel * bbs;
       tol2 = r2 > t2 ? r2 : t2;
-      int stop = a.maxiter <= 0 || (a.warm && rr < tol2);
+      int stop = maxiter <= 0 || (warm && rr < tol2);
       if (!isfinite(bbs)) {
         status |= MGPBD_STATUS_NAN;
         stop = 1;
@@ -601,7 +612,7 @@ __global__ void __launch_bounds__(kPT, STAGED ? 1 : 2) k_jcg(PArgs a) {
           beta = sz / rz;
           rz = sz;
           s_scal = (float)beta;
-          if (iters >= a.maxiter) {
+          if (iters >= maxiter) {
             status |= MGPBD_STATUS_CG_MAXITER;
             stop = 1;
           }
@@ -633,7 +644,7 @@ __global__ void __launch_bounds__(kPT, STAGED ? 1 : 2) k_jcg(PArgs a) {
     st->tol2 = tol2;
     st->iters = iters;
     st->done = 1;
-    st->maxiter = a.maxiter;
+    st->maxiter = maxiter;
     st->body_runs = 1;
     atomicOr(reinterpret_cast<unsigned int*>(&st->status), status);
   }
@@ -711,7 +722,7 @@ JcgPlan jcg_plan(const std::vector<int32_t>& inc_ptr, int32_t nv, int32_t nt, bo
 void launch_jcg_persistent(const JView& j, const JcgVecs& v, const JcgPlan& plan,
                            const int32_t* part_dev, const JState* js, CgState* st, double tol_abs,
                            double tol_rel, int maxiter, int degree, bool warm, double spin_limit_s,
-                           cudaStream_t s) {
+                           cudaStream_t s, const JcgCtl* ctl) {
   require(degree >= 1 && degree <= kMaxCheb, MGPBD_EINVAL, "Chebyshev degree out of range");
   require(plan.grid > 0, MGPBD_ESTATE, "persistent CG plan not built");
   require(3LL * plan.grid <= v.partials_capacity, MGPBD_ERANGE, "partials buffer too small");
@@ -757,7 +768,8 @@ void launch_jcg_persistent(const JView& j, const JcgVecs& v, const JcgPlan& plan
   a.degree = degree;
   a.warm = warm ? 1 : 0;
   a.ulo = v.ulo;
-  require(!warm || v.ulo != nullptr, MGPBD_EINVAL, "warm start needs the ulo scratch");
+  a.ctl = ctl;
+  require(!(warm || ctl) || v.ulo != nullptr, MGPBD_EINVAL, "warm start needs the ulo scratch");
   a.spin_ns = static_cast<unsigned long long>(spin_limit_s * 1e9);
   MGPBD_CUDA(cudaMemsetAsync(v.gs, 0, sizeof(GridSync), s));
   MGPBD_CUDA(cudaMemsetAsync(st, 0, sizeof(CgState), s));

@@ -468,30 +468,29 @@ void launch_jform_lanczos(const JView& j, float* q, float* qprev, float* w, doub
 }
 
 // Largest eigenvalue of the symmetric tridiagonal T (diagonal a, off-
-// diagonal b) by Sturm-sequence bisection on its Gershgorin interval.
-double lanczos_lmax(const double* a, const double* b, int k) {
+// diagonal b) by Sturm-sequence bisection on its Gershgorin interval.  Every
+// product that feeds a sum is rounded on its own (no fused multiply-add), so
+// the result does not depend on how the compiler contracts.
+__device__ double lanczos_lmax(const double* a, const double* b, int k) {
   double lo = 1e300, hi = -1e300;
   for (int i = 0; i < k; ++i) {
-    double r = (i > 0 ? std::fabs(b[i - 1]) : 0.0) + (i + 1 < k ? std::fabs(b[i]) : 0.0);
-    lo = std::fmin(lo, a[i] - r);
-    hi = std::fmax(hi, a[i] + r);
+    const double r = (i > 0 ? fabs(b[i - 1]) : 0.0) + (i + 1 < k ? fabs(b[i]) : 0.0);
+    lo = fmin(lo, a[i] - r);
+    hi = fmax(hi, a[i] + r);
   }
-  if (!(hi >= lo) || !std::isfinite(hi) || !std::isfinite(lo)) return NAN;
-  // count of eigenvalues < x
-  auto below = [&](double x) {
+  if (!(hi >= lo) || !isfinite(hi) || !isfinite(lo)) return NAN;
+  for (int it = 0; it < 200 && hi - lo > __dmul_rn(1e-12, fmax(1.0, fabs(hi))); ++it) {
+    const double mid = __dmul_rn(0.5, lo + hi);
+    // count of eigenvalues below mid
     int c = 0;
     double d = 1.0;
     for (int i = 0; i < k; ++i) {
-      double bb = i > 0 ? b[i - 1] * b[i - 1] : 0.0;
-      d = (a[i] - x) - (i > 0 ? bb / d : 0.0);
+      const double q = i > 0 ? __ddiv_rn(__dmul_rn(b[i - 1], b[i - 1]), d) : 0.0;
+      d = (a[i] - mid) - q;
       if (d == 0.0) d = -1e-300;
       if (d < 0.0) ++c;
     }
-    return c;
-  };
-  for (int it = 0; it < 200 && hi - lo > 1e-12 * std::fmax(1.0, std::fabs(hi)); ++it) {
-    double mid = 0.5 * (lo + hi);
-    if (below(mid) >= k) hi = mid;  // all eigenvalues below mid
+    if (c >= k) hi = mid;  // all eigenvalues below mid
     else lo = mid;
   }
   return hi;
@@ -500,25 +499,39 @@ double lanczos_lmax(const double* a, const double* b, int k) {
 // Chebyshev acceleration coefficients on [hi * lo_ratio, hi] (Saad,
 // "Iterative Methods for Sparse Linear Systems", 2nd ed., Alg. 12.1):
 // sigma = theta / delta, rho_0 = 1 / sigma, rho_i = 1 / (2 sigma - rho_{i-1}),
-// d_i = rho_i rho_{i-1} d_{i-1} + (2 rho_i / delta) r_i.
-ChebCoef chebyshev_coefficients(double lmax, int degree, double lo_ratio) {
-  ChebCoef c{};
-  double hi = lmax;
-  if (!(hi > 0.0) || !std::isfinite(hi)) hi = 2.0;
-  const double lo = hi * lo_ratio;
-  const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
-  double rho = 1.0 / sigma;
+// d_i = rho_i rho_{i-1} d_{i-1} + (2 rho_i / delta) r_i.  One thread.
+__global__ void k_cheb_coefficients(JState* js, int steps, int degree, double lo_ratio,
+                                    uint32_t* status) {
+  const double lmax = lanczos_lmax(js->lz_a, js->lz_b, steps);
+  const bool ok = isfinite(lmax) && lmax > 0.0;
+  if (!ok && status) atomicOr(reinterpret_cast<unsigned int*>(status), MGPBD_STATUS_NAN);
+  ChebCoef& c = js->cf;
+  const double hi = ok ? __dmul_rn(1.02, lmax) : 2.0;
+  const double lo = __dmul_rn(hi, lo_ratio);
+  const double theta = __dmul_rn(0.5, hi + lo), delta = __dmul_rn(0.5, hi - lo);
+  const double sigma = __ddiv_rn(theta, delta);
+  double rho = __ddiv_rn(1.0, sigma);
+  for (int i = 0; i < kMaxCheb; ++i) {
+    c.c1[i] = 0.0f;
+    c.c2[i] = 0.0f;
+  }
   for (int i = 1; i < degree && i < kMaxCheb; ++i) {
-    const double rn = 1.0 / (2.0 * sigma - rho);
-    c.c1[i] = static_cast<float>(rn * rho);
-    c.c2[i] = static_cast<float>(2.0 * rn / delta);
+    const double rn = __ddiv_rn(1.0, __dmul_rn(2.0, sigma) - rho);
+    c.c1[i] = static_cast<float>(__dmul_rn(rn, rho));
+    c.c2[i] = static_cast<float>(__ddiv_rn(__dmul_rn(2.0, rn), delta));
     rho = rn;
   }
   c.theta = theta;
-  c.lmax = lmax;
-  c.inv_theta = static_cast<float>(1.0 / theta);
+  c.lmax = ok ? lmax : (isfinite(lmax) ? lmax : NAN);
+  c.inv_theta = static_cast<float>(__ddiv_rn(1.0, theta));
   c.degree = degree;
-  return c;
+}
+
+void launch_cheb_coefficients(JState* js, int steps, int degree, double lo_ratio,
+                              uint32_t* status, cudaStream_t s) {
+  require(steps >= 1 && steps <= kMaxLanczos, MGPBD_EINVAL, "Lanczos steps out of range");
+  k_cheb_coefficients<<<1, 1, 0, s>>>(js, steps, degree, lo_ratio, status);
+  MGPBD_CHECK_LAUNCH();
 }
 
 void launch_jcg_init(const JView& j, const JVecs& v, JState* js, CgState* st, double tol_abs,

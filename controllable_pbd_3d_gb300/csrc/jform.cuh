@@ -79,10 +79,13 @@ void launch_jform_apply(const JView& j, const float* x, float* y, cudaStream_t s
 // nt floats of scratch)
 void launch_jform_lanczos(const JView& j, float* q, float* qprev, float* w, double* partials,
                           JState* js, int steps, cudaStream_t s);
-// host side: largest eigenvalue of the Lanczos tridiagonal (bisection) and
-// the Chebyshev coefficients of `degree` on [hi * lo_ratio, hi]
-double lanczos_lmax(const double* a, const double* b, int k);
-ChebCoef chebyshev_coefficients(double lmax, int degree, double lo_ratio);
+// On the device, from the `steps` Lanczos coefficients in js: the largest
+// eigenvalue of the tridiagonal (bisection), and js->cf = the Chebyshev
+// coefficients of `degree` on [1.02 lmax lo_ratio, 1.02 lmax]; a lmax that
+// is not finite and positive ORs MGPBD_STATUS_NAN into *status (if given)
+// and leaves js->cf.lmax NaN or <= 0 for the host to see.
+void launch_cheb_coefficients(JState* js, int steps, int degree, double lo_ratio,
+                              uint32_t* status, cudaStream_t s);
 
 // CG with the degree-k Chebyshev preconditioner (k >= 1; k = 1 is scaled
 // Jacobi), scalars on the device.  init: x = 0, r = b, z = M^-1 r, p = z.
@@ -151,10 +154,21 @@ JcgPlan jcg_plan(const std::vector<int32_t>& inc_ptr, int32_t nv, int32_t nt,
 // x on entry (r = b - A x) instead of 0; the tolerance stays relative to
 // |b|.  A barrier wait longer than spin_limit_s sets
 // MGPBD_STATUS_SYNC_TIMEOUT in st->status.
+// With ctl (device memory), a launch captured into a graph takes its
+// tolerance, iteration limit and start from there when it runs (tol_abs,
+// maxiter and warm are then ignored), or returns at once when ctl->skip is
+// set, writing nothing.
+struct JcgCtl {
+  double tol_abs;
+  int32_t maxiter;
+  int32_t warm;
+  int32_t skip;
+  int32_t pad;
+};
 void launch_jcg_persistent(const JView& j, const JcgVecs& v, const JcgPlan& plan,
                            const int32_t* part_dev, const JState* js, CgState* st, double tol_abs,
                            double tol_rel, int maxiter, int degree, bool warm, double spin_limit_s,
-                           cudaStream_t s);
+                           cudaStream_t s, const JcgCtl* ctl = nullptr);
 
 // Work vectors of the primal persistent CG (pcg.cu): vertex vectors are
 // float4 per vertex (xyz used), s is per tet.

@@ -130,6 +130,8 @@ Solver::Solver(const mgpbd_params& p) : p_(p) {
 Solver::~Solver() {
   if (cg_exec_) cudaGraphExecDestroy(cg_exec_);
   if (jcg_exec_) cudaGraphExecDestroy(jcg_exec_);
+  if (body_exec_) cudaGraphExecDestroy(body_exec_);
+  if (h_body_loop_) cudaFreeHost(h_body_loop_);
   if (h_buf_) cudaFreeHost(h_buf_);
   if (h_state_) cudaFreeHost(h_state_);
   if (h_cf_) cudaFreeHost(h_cf_);
@@ -305,6 +307,7 @@ void Solver::set_mesh(const float* x_ref, const float* invm, const int32_t* t_i,
     cudaGraphExecDestroy(jcg_exec_);
     jcg_exec_ = nullptr;
   }
+  drop_body_graph();
 }
 
 void Solver::sync_read(void* host, const void* dev, size_t bytes) {
@@ -726,20 +729,16 @@ JVecs Solver::jvecs(const float* b, float* x) {
 // unscaled base), lambda_max of D^-1 A by 24 Lanczos steps (upper end taken 2% above the Ritz value; a
 // Chebyshev interval that misses the top of the spectrum makes the
 // preconditioner indefinite) and the Chebyshev coefficients.
-void Solver::jform_setup() {
+void Solver::jform_setup(uint32_t* dev_status) {
   constexpr int kSteps = 24;
   JView j = jview();
   launch_jform_prepare(j, inc_ent_.p, gV_.p, jdinv_.p, gT_.p,
                        p_.cheb_scale == MGPBD_CHEB_UNSCALED, stream_);
   launch_jform_lanczos(j, pw_v_.p, jd_.p, pw_w_.p, partials_.p, jst_.p, kSteps, stream_);
-  static_assert(2 * kMaxLanczos <= 64, "h_buf_ holds the Lanczos coefficients");
-  MGPBD_CUDA(cudaMemcpyAsync(h_buf_, jst_.p->lz_a, sizeof(double) * kMaxLanczos,
-                             cudaMemcpyDeviceToHost, stream_));
-  sync_read(h_buf_ + kMaxLanczos, jst_.p->lz_b, sizeof(double) * kMaxLanczos);
-  double lmax = lanczos_lmax(h_buf_, h_buf_ + kMaxLanczos, kSteps);
-  if (!std::isfinite(lmax) || !(lmax > 0.0)) status_ |= MGPBD_STATUS_NAN;
-  *h_cf_ = chebyshev_coefficients(1.02 * lmax, p_.cheb_degree, p_.cheb_lo);
-  MGPBD_CUDA(cudaMemcpyAsync(&jst_.p->cf, h_cf_, sizeof(ChebCoef), cudaMemcpyHostToDevice, stream_));
+  launch_cheb_coefficients(jst_.p, kSteps, p_.cheb_degree, p_.cheb_lo, dev_status, stream_);
+  if (dev_status) return;  // captured: the status word is read after the graph
+  sync_read(h_buf_, &jst_.p->cf.lmax, sizeof(double));
+  if (!std::isfinite(h_buf_[0]) || !(h_buf_[0] > 0.0)) status_ |= MGPBD_STATUS_NAN;
 }
 
 // CG with the Chebyshev preconditioner as one CUDA graph: init, a device-side
@@ -1419,7 +1418,8 @@ void Solver::solve(int32_t frame) {
   (void)frame;
   require_mesh();
   if (nb_ > 0) {
-    solve_bodies();
+    if (p_.use_graph) solve_bodies_graph();
+    else solve_bodies();
     return;
   }
   status_ = 0;
@@ -1583,7 +1583,67 @@ void Solver::init_bodies(const std::vector<int32_t>& t_host) {
   body_r0_.assign(nb_, 0.0);
   body_r_.assign(nb_, 0.0);
   body_omega_h_.assign(nb_, 1.0);
+  // each body's chunks in ascending order (the host loop's summation order)
+  std::vector<int32_t> cp(nb_ + 1, 0), ci(chunk_body_.size());
+  for (int32_t b : chunk_body_) cp[b + 1]++;
+  for (int32_t b = 0; b < nb_; ++b) cp[b + 1] += cp[b];
+  {
+    std::vector<int32_t> cur(cp.begin(), cp.end() - 1);
+    for (size_t c = 0; c < chunk_body_.size(); ++c) ci[cur[chunk_body_[c]]++] = static_cast<int32_t>(c);
+  }
+  upload(body_chunk_ptr_, cp, s);
+  upload(body_chunk_idx_, ci, s);
+  body_newton_d_.alloc(nb_);
+  body_r0_d_.alloc(nb_);
+  body_r_d_.alloc(nb_);
+  body_bnorm_d_.alloc(nb_);
+  body_sq_d_.alloc(nb_);
+  body_cur_d_.alloc(nb_);
+  body_omh_d_.alloc(nb_);
+  body_loop_.alloc(1);
+  body_log_.alloc(std::max(1, p_.maxiter) + 1);
+  if (!h_body_loop_) MGPBD_CUDA(cudaMallocHost(&h_body_loop_, sizeof(BodyLoop)));
+  drop_body_graph();
   MGPBD_CUDA(cudaStreamSynchronize(s));
+}
+
+void Solver::drop_body_graph() {
+  if (body_exec_) {
+    cudaGraphExecDestroy(body_exec_);
+    body_exec_ = nullptr;
+  }
+}
+
+BodyArrays Solver::body_arrays() {
+  BodyArrays ba;
+  ba.nb = nb_;
+  ba.n_chunks = static_cast<int32_t>(chunk_body_.size());
+  ba.chunk_ptr = body_chunk_ptr_.p;
+  ba.chunk_idx = body_chunk_idx_.p;
+  ba.partials = chunk_partials_.p;
+  ba.active = body_active_.p;
+  ba.r0 = body_r0_d_.p;
+  ba.r = body_r_d_.p;
+  ba.bnorm = body_bnorm_d_.p;
+  ba.sq = body_sq_d_.p;
+  ba.cur = body_cur_d_.p;
+  ba.newton = body_newton_d_.p;
+  ba.omega = body_omega_.p;
+  ba.omega_h = body_omh_d_.p;
+  ba.log = body_log_.p;
+  ba.log_cap = static_cast<int32_t>(body_log_.n);
+  return ba;
+}
+
+BodyLimits Solver::body_limits() const {
+  BodyLimits lim;
+  lim.atol = p_.atol;
+  lim.rtol = p_.rtol;
+  lim.tol_cg = p_.tol_cg;
+  lim.rel_tol_cg = p_.rel_tol_cg;
+  lim.maxiter = p_.maxiter;
+  lim.maxiter_cg = p_.maxiter_cg;
+  return lim;
 }
 
 // out[k * nb + b] = sum of the chunk partials k of body b, in chunk order
@@ -1750,6 +1810,168 @@ void Solver::solve_bodies() {
     if (ite + 1 == p_.maxiter) status_ |= MGPBD_STATUS_NEWTON_MAXITER;
   }
   stats_.status = status_;
+}
+
+// The Newton loop of solve_bodies as one CUDA graph: the residual and
+// stopping tests before the loop, then a device-side while loop whose body
+// is one Newton iteration: masked right-hand side, Lanczos estimate and
+// Chebyshev coefficients, up to 6 verified CG passes (the persistent
+// kernel with its tolerance, limit and start read from the device; unused
+// passes return at once), scatter, the per-body line search over all 10
+// steps, the position update, and the next residual, which decides whether
+// the loop goes on.  Decisions are the host loop's (bodies.cu).
+void Solver::capture_body_graph() {
+  drop_body_graph();
+  cudaStream_t outer = stream_;
+  cudaStream_t cs, bs;
+  MGPBD_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  MGPBD_CUDA(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking));
+  cudaGraph_t graph = nullptr;
+  const int32_t n_ch = static_cast<int32_t>(chunk_body_.size());
+  const BodyArrays ba = body_arrays();
+  const BodyLimits lim = body_limits();
+  BodyLoop* L = body_loop_.p;
+  JcgVecs v;
+  v.b = rhs_.p;
+  v.x = dlam_.p;
+  v.xc = jxc_.p;
+  v.r = jrf_.p;
+  v.z = jz_.p;
+  v.d = jd_.p;
+  v.p = jp_.p;
+  v.ap = jap_.p;
+  v.partials = partials_.p;
+  v.partials_capacity = static_cast<int64_t>(kMaxReduceBlocks) * 16;
+  v.gs = jgs_.p;
+  v.ulo = ulo_.p;
+  try {
+    long long c0 = g_launches.load();
+    MGPBD_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    stream_ = cs;
+    MGPBD_CUDA(cudaMemsetAsync(lambda_.p, 0, sizeof(float) * nt_, cs));
+    launch_bodies_reset(ba, L, cs);
+    compute_constraints();
+    launch_rhs(C_.p, alpha_.p, lambda_.p, nt_, rhs_.p, partials_.p, cs);
+    launch_chunk_dual_sq(C_.p, alpha_.p, lambda_.p, chunks_.p, n_ch, chunk_partials_.p, cs);
+    cudaStreamCaptureStatus cst;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    MGPBD_CUDA(cudaStreamGetCaptureInfo(cs, &cst, nullptr, &graph, &deps, nullptr, &ndeps));
+    cudaGraphConditionalHandle handle;
+    MGPBD_CUDA(cudaGraphConditionalHandleCreate(&handle, graph, 0, cudaGraphCondAssignDefault));
+    launch_bodies_residual(ba, L, lim, handle, cs);
+    MGPBD_CUDA(cudaStreamGetCaptureInfo(cs, &cst, nullptr, &graph, &deps, nullptr, &ndeps));
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cond;
+    MGPBD_CUDA(cudaGraphAddNode(&cond, graph, deps, nullptr, ndeps, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    MGPBD_CUDA(cudaStreamUpdateCaptureDependencies(cs, &cond, nullptr, 1, cudaStreamSetCaptureDependencies));
+    long long c1 = g_launches.load();
+    MGPBD_CUDA(cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    stream_ = bs;
+    launch_mask_rhs(rhs_.p, cons_body_.p, body_active_.p, nt_, bs);
+    jform_setup(&L->status);
+    for (int pass = 0; pass < 6; ++pass) {
+      launch_jcg_persistent(jview(), v, jplan_, jpart_.p, jst_.p, cg_state_.p, p_.tol_cg, 0.0,
+                            p_.maxiter_cg, p_.cheb_degree, false, barrier_limit_s_, bs, &L->jc);
+      launch_chunk_dual_sq(jrf_.p, nullptr, nullptr, chunks_.p, n_ch, chunk_partials_.p, bs);
+      launch_bodies_verify(ba, L, cg_state_.p, lim, bs);
+    }
+    dual_x_ = dlam_.p;
+    scatter(dlam_.p);
+    launch_chunk_dual_sq(C_.p, alpha_.p, lambda_.p, chunks_.p, n_ch, chunk_partials_.p, bs);
+    launch_bodies_cur(ba, bs);
+    launch_chunk_trial(x_, dpos_.p, omegas_.p, kBodyTrials, t_i_, ctype_.p, dm_inv_.p,
+                       rest_vol_.p, alpha_.p, lambda_.p, chunks_.p, n_ch, chunk_partials_.p, bs);
+    launch_bodies_omega(ba, L, lim, kBodyTrials, bs);
+    launch_apply_bodies(x_, dpos_.p, invm_, vert_body_.p, body_omega_.p, nv_, bs);
+    compute_constraints();
+    launch_rhs(C_.p, alpha_.p, lambda_.p, nt_, rhs_.p, partials_.p, bs);
+    launch_chunk_dual_sq(C_.p, alpha_.p, lambda_.p, chunks_.p, n_ch, chunk_partials_.p, bs);
+    launch_bodies_residual(ba, L, lim, handle, bs);
+    long long c2 = g_launches.load();
+    MGPBD_CUDA(cudaStreamEndCapture(bs, &body));
+    stream_ = outer;
+    MGPBD_CUDA(cudaStreamEndCapture(cs, &graph));
+    g_launches.fetch_sub(c2 - c0);
+    body_graph_init_launches_ = c1 - c0;
+    body_graph_body_launches_ = c2 - c1;
+    MGPBD_CUDA(cudaGraphInstantiate(&body_exec_, graph, 0));
+    cudaGraphDestroy(graph);
+  } catch (...) {
+    stream_ = outer;
+    cudaStreamCaptureStatus cst;
+    if (cudaStreamIsCapturing(bs, &cst) == cudaSuccess && cst != cudaStreamCaptureStatusNone) {
+      cudaGraph_t g2;
+      cudaStreamEndCapture(bs, &g2);
+    }
+    if (cudaStreamIsCapturing(cs, &cst) == cudaSuccess && cst != cudaStreamCaptureStatusNone) {
+      cudaGraph_t g2 = nullptr;
+      cudaStreamEndCapture(cs, &g2);
+      if (g2) cudaGraphDestroy(g2);
+    }
+    cudaGetLastError();
+    cudaStreamDestroy(cs);
+    cudaStreamDestroy(bs);
+    throw;
+  }
+  cudaStreamDestroy(cs);
+  cudaStreamDestroy(bs);
+  body_exec_limit_ = barrier_limit_s_;
+}
+
+void Solver::solve_bodies_graph() {
+  cudaStream_t s = stream_;
+  require(p_.maxiter + 1 <= static_cast<int32_t>(body_log_.n), MGPBD_ESTATE,
+          "bodies: the loop log is smaller than maxiter + 1");
+  if (!body_exec_ || body_exec_limit_ != barrier_limit_s_) capture_body_graph();
+  // the line-search steps 1, 1/2, ..., 1/512 (the graph reads them)
+  double steps[kBodyTrials];
+  for (int k = 0; k < kBodyTrials; ++k) steps[k] = std::ldexp(1.0, -k);
+  std::memcpy(h_buf_, steps, sizeof(steps));
+  MGPBD_CUDA(cudaMemcpyAsync(omegas_.p, h_buf_, sizeof(steps), cudaMemcpyHostToDevice, s));
+  MGPBD_CUDA(cudaEventRecord(ev_[0], s));
+  MGPBD_CUDA(cudaGraphLaunch(body_exec_, s));
+  MGPBD_CUDA(cudaEventRecord(ev_[1], s));
+  MGPBD_CUDA(cudaMemcpyAsync(h_body_loop_, body_loop_.p, sizeof(BodyLoop), cudaMemcpyDeviceToHost, s));
+  std::vector<BodyLogEntry> lg(body_log_.n);
+  MGPBD_CUDA(cudaMemcpyAsync(lg.data(), body_log_.p, sizeof(BodyLogEntry) * lg.size(),
+                             cudaMemcpyDeviceToHost, s));
+  MGPBD_CUDA(cudaMemcpyAsync(body_newton_.data(), body_newton_d_.p, sizeof(int32_t) * nb_,
+                             cudaMemcpyDeviceToHost, s));
+  MGPBD_CUDA(cudaMemcpyAsync(body_r0_.data(), body_r0_d_.p, sizeof(double) * nb_,
+                             cudaMemcpyDeviceToHost, s));
+  MGPBD_CUDA(cudaMemcpyAsync(body_r_.data(), body_r_d_.p, sizeof(double) * nb_,
+                             cudaMemcpyDeviceToHost, s));
+  MGPBD_CUDA(cudaMemcpyAsync(body_omega_h_.data(), body_omh_d_.p, sizeof(double) * nb_,
+                             cudaMemcpyDeviceToHost, s));
+  MGPBD_CUDA(cudaStreamSynchronize(s));
+  const BodyLoop& L = *h_body_loop_;
+  g_launches.fetch_add(body_graph_init_launches_ + body_graph_body_launches_ * L.ite);
+  status_ = L.status;
+  stats_.newton_iters = L.ite;
+  stats_.cg_iters_total = L.cg_total;
+  stats_.cg_iters_last = L.ite > 0 ? static_cast<int32_t>(lg[L.ite - 1].cg) : 0;
+  stats_.omega_last = L.omega_min;
+  stats_.residual0 = L.residual0;
+  stats_.residual = L.residual;
+  stats_.cg_iters_warm = 0;
+  stats_.cg_launches = L.cg_launches;
+  stats_.ms_warm = 0.0;
+  stats_.ms_dual = event_ms(ev_[0], ev_[1]);
+  stats_.warm_amp = 0.0;
+  stats_.warm_declined = 0;
+  stats_.status = status_;
+  log_.clear();
+  const double t = std::chrono::duration<double>(
+                       std::chrono::steady_clock::now().time_since_epoch()).count();
+  for (int32_t i = 0; i < L.n_log && i < static_cast<int32_t>(lg.size()); ++i)
+    log_.push_back({double(i), lg[i].r, lg[i].cg, lg[i].omega, t});
+  if (status_ & MGPBD_STATUS_SYNC_TIMEOUT)
+    throw Error(MGPBD_ECUDA, "persistent CG kernel: a grid barrier wait timed out");
 }
 
 void Solver::body_stats(int32_t n, int32_t* newton, double* r0, double* r, double* omega) const {

@@ -8,6 +8,7 @@
 #include <memory>
 #include <vector>
 
+#include "bodies.cuh"
 #include "common.h"
 #include "jform.cuh"
 #include "kernels.cuh"
@@ -141,6 +142,12 @@ class Solver {
   void solve_bodies();
   int32_t pcg_bodies(const float* b, float* x, const std::vector<double>& bnorm);
   void chunk_body_sums(int count, std::vector<double>& out);
+  // the same loop as one captured CUDA graph per substep (use_graph)
+  void solve_bodies_graph();
+  void capture_body_graph();
+  void drop_body_graph();
+  BodyArrays body_arrays();
+  BodyLimits body_limits() const;
   int32_t run_dual(const float* b, float* x, double tol_abs, double tol_rel, int32_t maxit,
                    bool warm, float4* ulo);
   // the per-mesh stages need set_mesh (not a caller's matrix)
@@ -173,7 +180,7 @@ class Solver {
   bool cheb() const { return p_.precond == MGPBD_PRECOND_CHEB; }
   JView jview();
   JVecs jvecs(const float* b, float* x);
-  void jform_setup();
+  void jform_setup(uint32_t* dev_status = nullptr);
   int32_t pcg_cheb(const float* b, float* x);
   void sync_read(void* host, const void* dev, size_t bytes);
   double finalize_read(const double* partials, int blocks);
@@ -199,6 +206,15 @@ class Solver {
   DevBuf<float4> ulo_;  // warm restarts of the dual CG: low parts of u (float64 residual)
   std::vector<int32_t> body_newton_;
   std::vector<double> body_r0_, body_r_, body_omega_h_;
+  // device side of the loop for the captured substep (bodies.cuh)
+  DevBuf<int32_t> body_chunk_ptr_, body_chunk_idx_, body_newton_d_;
+  DevBuf<double> body_r0_d_, body_r_d_, body_bnorm_d_, body_sq_d_, body_cur_d_, body_omh_d_;
+  DevBuf<BodyLoop> body_loop_;
+  DevBuf<BodyLogEntry> body_log_;
+  BodyLoop* h_body_loop_ = nullptr;  // pinned
+  cudaGraphExec_t body_exec_ = nullptr;
+  double body_exec_limit_ = -1.0;  // barrier limit baked into the captured launches
+  long long body_graph_init_launches_ = 0, body_graph_body_launches_ = 0;
   Csr mat_csr_;                  // its structure and values (host)
   std::vector<float> mat_vals_;
 

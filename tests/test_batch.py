@@ -187,3 +187,39 @@ def test_per_body_newton_equals_separate_substeps(cuda):
     got = batch.positions(b).cpu().numpy().astype(np.float64)
     ref = x.cpu().numpy().astype(np.float64)
     assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max(), b
+
+
+@pytest.mark.gpu
+def test_captured_substep_equals_host_loop(cuda):
+  """The packed-body substep as one captured CUDA graph (use_graph: the
+  Newton loop a device-side while loop, every decision taken on the device)
+  and the same substep driven by the host loop take the same decisions in
+  the same arithmetic: positions, per-body Newton counts, residuals, steps
+  and the Newton log agree bit for bit over three substeps, and the graph
+  replays (one capture, three launches)."""
+  from controllable_pbd_3d_gb300.batch import BodyBatch
+  g, dt = [0.0, -9.8, 0.0], 1 / 300
+  kw = dict(mode='fast', precond='cheb', cheb_scale='none', cheb_lo=1e-3, primal=False,
+            rel_tol_cg=1e-7, tol_cg=1e-14, maxiter_cg=6000, maxiter=10, atol=1e-9, rtol=3e-3,
+            kinematic_pins=True, constraints='edge_volume')
+  bodies = random_bodies(5, seed=3, dims=(3, 7), compliance=(1e-8, 1e-5))
+  runs = {}
+  for graph in (True, False):
+    batch = BodyBatch(bodies, g, dt, use_graph=graph, **kw)
+    batch.init()
+    hist = []
+    for k in range(3):
+      batch.step(k)
+      st = batch.solver.stats()
+      hist.append((batch.x.cpu().numpy().copy(), batch.solver.body_stats(),
+                   {key: st[key] for key in ('newton_iters', 'cg_iters_total', 'residual',
+                                             'residual0', 'omega_last', 'status')},
+                   [tuple(e[1:4]) for e in batch.solver.newton_log()]))
+    runs[graph] = hist
+  for (xg, bg, sg, lg), (xh, bh, sh, lh) in zip(runs[True], runs[False]):
+    np.testing.assert_array_equal(xg, xh)
+    for key in bg:
+      np.testing.assert_array_equal(bg[key], bh[key])
+    assert sg == sh
+    assert lg == lh
+  assert runs[True][-1][2]['status'] == 0
