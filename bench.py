@@ -188,7 +188,11 @@ def make_solver(torch, n, kw, constraints='edge_volume'):
   s = MGPBDSolverGPU(x, torch.tensor(xr, device='cuda'), torch.tensor(invm, device='cuda'),
                      torch.tensor(t, device='cuda'), None, [0.0, -9.8, 0.0], DT,
                      compliance=compliance, constraints=constraints, **kw)
+  torch.cuda.synchronize()
+  t0 = time.perf_counter()
   s.init()
+  torch.cuda.synchronize()
+  s.init_s = time.perf_counter() - t0
   return s, x, compliance
 
 
@@ -689,6 +693,7 @@ def run_ours(args):
   st0 = st[-1]
   n_verts, n_cons = s.n_verts, s.n_tets
   n_tets = s.n_mesh_tets
+  init_s = s.init_s
   del s
   torch.cuda.empty_cache()
 
@@ -705,6 +710,7 @@ def run_ours(args):
       'newton_iters_per_step': newton / args.steps, 'cg_iters_per_step': cg / args.steps,
       'cg_iters_per_s': round(ws * cg / t_max, 1), 'gpu_launches': int(launches),
       'clocks': clk.summary(), 'e2e': e2e, 'roofline': roof,
+      'init_s': round(init_s, 3),
   }
   if plain is not None:
     out['plain_fp32_amg_pcg'] = plain
@@ -954,6 +960,63 @@ def run_batch(args):
   print(json.dumps(out), flush=True)
 
 
+TRAIN_SET_BODIES = 256  # the training-set configuration
+TRAIN_PAIRS, TRAIN_EVERY, TRAIN_STEPS = 4, 8, 4000
+
+
+def run_train(args):
+  """The learned correction's training-set configuration: 256 seeded
+  bodies (hex-grid cubes, side uniform in 20..40, half of them projected to
+  a ball, compliance log-uniform in [1e-9, 1e-4], 1-4 % of surface vertices
+  pinned; `scenarios.training_bodies(256, seed=0)`), TRAIN_PAIRS restricted
+  residuals per body from the plain solver's first V-cycles (its CG stopped
+  after TRAIN_PAIRS * TRAIN_EVERY + 1 iterations), the 3-layer network
+  (hidden 64) trained on the GPU on all of them; then its coarse energy on
+  held-out pairs of the benchmark body beside one Jacobi sweep's.  One JSON
+  line; nothing here is a timed substep."""
+  import torch
+  from controllable_pbd_3d_gb300 import scenarios
+  from controllable_pbd_3d_gb300.learned import CoarseNet, coarse_energy, collect_pairs
+  torch.cuda.set_device(0)
+  limit = TRAIN_PAIRS * TRAIN_EVERY + 1
+  data, sides, comps = [], [], []
+  torch.cuda.synchronize()
+  t0 = time.perf_counter()
+  for b in scenarios.training_bodies(TRAIN_SET_BODIES, seed=0):
+    g, rc = collect_pairs(b, TRAIN_PAIRS, TRAIN_EVERY, cg_limit=limit)
+    sides.append(int(b['side']))
+    comps.append(float(b['compliance']))
+    if rc.shape[0] > 0:
+      data.append((g, rc))
+  torch.cuda.synchronize()
+  t_collect = time.perf_counter() - t0
+  net = CoarseNet(seed=1)
+  t0 = time.perf_counter()
+  losses = net.fit_many(data, steps=TRAIN_STEPS, batch=TRAIN_PAIRS, lr=2e-3)
+  torch.cuda.synchronize()
+  t_train = time.perf_counter() - t0
+  xr, x0, t, invm, comp = workload(args.size)
+  g, rc = collect_pairs(dict(x_ref=xr, x0=x0, t_i=t, invm=invm, compliance=comp), 32, 8)
+  e_net = coarse_energy(g, rc, net.correction(g, rc)).mean().item()
+  e_one = coarse_energy(g, rc, ((2.0 / 3.0) * g.diag_inv[None, :] * rc.reshape(-1, g.n))
+                        .reshape(rc.shape)).mean().item()
+  out = {'metric': 'learned coarse correction: training set', 'workload': 'train',
+         'data': 'synthetic (seeded training bodies)',
+         'config': {'bodies': TRAIN_SET_BODIES, 'generator': 'scenarios.training_bodies(256, seed=0)',
+                    'sides': [min(sides), max(sides)],
+                    'compliance': [min(comps), max(comps)],
+                    'pairs_per_body': TRAIN_PAIRS, 'every': TRAIN_EVERY,
+                    'network': '3 message-passing layers, hidden 64, bf16 tensor-core layers'},
+         'bodies_with_pairs': len(data), 'pairs': int(sum(r.shape[0] for _, r in data)),
+         'collect_s': round(t_collect, 1), 'train_s': round(t_train, 1),
+         'adam_steps': TRAIN_STEPS, 'loss_first50': float(losses[:50].mean()),
+         'loss_last200': float(losses[-200:].mean()),
+         'held_out': f'{args.size}^3 benchmark body, 32 pairs',
+         'held_out_coarse_energy': {'network': e_net, 'one_jacobi_sweep': e_one},
+         'network_over_one_sweep': round(e_net / e_one, 4) if e_one else None}
+  print(json.dumps(out), flush=True)
+
+
 def run_reference(args):
   """The reference algorithm on the host cores (the reference itself needs
   Taichi, absent here): whole substeps of the OpenMP CPU port of the plain
@@ -1012,7 +1075,8 @@ def main():
   ap.add_argument('--profile-net', action='store_true')
   ap.add_argument('--profile-reps', type=int, default=5)
   # the 40^3 cube (headline) or the stiff-drag slab (one line, fast step only)
-  ap.add_argument('--workload', default='cube', choices=['cube', 'slab', 'batch'])
+  # C3: the learned correction's training set (one line, no timed substeps)
+  ap.add_argument('--workload', default='cube', choices=['cube', 'slab', 'batch', 'train'])
   args = ap.parse_args()
   if args.profile_net:
     run_profile_net(args)
@@ -1020,6 +1084,8 @@ def main():
     run_slab(args)
   elif args.workload == 'batch' and args.impl == 'ours':
     run_batch(args)
+  elif args.workload == 'train' and args.impl == 'ours':
+    run_train(args)
   elif args.profile_solve:
     run_profile_solve(args)
   elif args.impl == 'reference':

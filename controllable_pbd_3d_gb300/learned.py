@@ -224,18 +224,21 @@ PAIR_SOLVER_KW = dict(mode='parity', smoother='safe', precond='vcycle', damp=1.0
 
 
 def collect_pairs(body, n_pairs=64, every=4, constraints='edge_volume', dt=1.0 / 300.0,
-                  device='cuda'):
+                  device='cuda', cg_limit=None):
   """Training pairs of one body (a dict of `scenarios.training_body`): one
   Newton iteration of the plain solver, recording up to `n_pairs`
   restricted residuals r_c (every `every`-th V-cycle); returns the level-1
-  graph (a snapshot that outlives the solver) and the (k, n1) residuals."""
+  graph (a snapshot that outlives the solver) and the (k, n1) residuals.
+  cg_limit: stop the solve after that many CG iterations (the pairs come
+  from its first n_pairs * every V-cycles)."""
   from .mgpbd_gpu import MGPBDSolverGPU
   x = torch.tensor(body['x0'], device=device)
   s = MGPBDSolverGPU(x, torch.tensor(body['x_ref'], device=device),
                      torch.tensor(body['invm'], device=device),
                      torch.tensor(body['t_i'], device=device), None, [0.0, -9.8, 0.0], dt,
                      compliance=float(body['compliance']), constraints=constraints,
-                     **PAIR_SOLVER_KW)
+                     **dict(PAIR_SOLVER_KW, **({} if cg_limit is None else
+                                               {'maxiter_cg': int(cg_limit)})))
   s.init()
   s.record_coarse(int(n_pairs), int(every))
   s.step(0)
@@ -247,14 +250,14 @@ def collect_pairs(body, n_pairs=64, every=4, constraints='edge_volume', dt=1.0 /
 
 
 def train_on_bodies(net: CoarseNet, bodies, pairs_per_body=64, every=4, steps=600, batch=8,
-                    lr=2e-3, constraints='edge_volume'):
+                    lr=2e-3, constraints='edge_volume', cg_limit=None):
   """Train `net` on pairs from several bodies (an iterable of
   `scenarios.training_body` dicts): pairs are collected body by body, then
   `fit_many` alternates Adam steps over the bodies.  Returns
   (losses, [(graph, residuals)])."""
   data = []
   for b in bodies:
-    g, rc = collect_pairs(b, pairs_per_body, every, constraints)
+    g, rc = collect_pairs(b, pairs_per_body, every, constraints, cg_limit=cg_limit)
     if rc.shape[0] > 0:
       data.append((g, rc))
   if not data:
