@@ -365,16 +365,9 @@ __device__ __forceinline__ void tphase_ap(const PArgs& a, const Own& o, float bf
 
 template <bool STAGED>
 __global__ void __launch_bounds__(kPT, STAGED ? 1 : 2) k_jcg(PArgs a) {
-  // the control values (every block reads the same ones: a skipped launch
-  // leaves before its first barrier in every block)
-  int32_t warm = a.warm, maxiter = a.maxiter;
-  double tol_abs = a.tol_abs;
-  if (a.ctl) {
-    if (a.ctl->skip) return;
-    warm = a.ctl->warm;
-    maxiter = a.ctl->maxiter;
-    tol_abs = a.ctl->tol_abs;
-  }
+  // a skipped launch leaves before its first barrier in every block (every
+  // thread reads the same flag)
+  if (a.ctl && a.ctl->skip) return;
   extern __shared__ __align__(16) unsigned char s_dyn[];
   __shared__ float s_c1[kMaxCheb], s_c2[kMaxCheb];
   __shared__ float s_scal;  // alpha or beta, broadcast from thread 0
@@ -388,10 +381,17 @@ __global__ void __launch_bounds__(kPT, STAGED ? 1 : 2) k_jcg(PArgs a) {
     s_c1[threadIdx.x] = a.js->cf.c1[threadIdx.x];
     s_c2[threadIdx.x] = a.js->cf.c2[threadIdx.x];
   }
+  // the control values, in shared memory (kept out of the registers of the
+  // iteration loop): from ctl when given, else the launch arguments
+  __shared__ int32_t warm, maxiter;
+  __shared__ double tol_abs;
   if (threadIdx.x == 0) {
     bbs = tol2 = rz = rr = pap = alpha = beta = 0.0;
     iters = 0;
     status = 0;
+    warm = a.ctl ? a.ctl->warm : a.warm;
+    maxiter = a.ctl ? a.ctl->maxiter : a.maxiter;
+    tol_abs = a.ctl ? a.ctl->tol_abs : a.tol_abs;
   }
   const float it = a.js->cf.inv_theta;
   const int m = a.degree;
