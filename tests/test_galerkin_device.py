@@ -149,14 +149,15 @@ def test_structural_build_equals_positive_values(cuda):
 
 
 @pytest.mark.gpu
-def test_solver_levels_are_built_on_the_device(cuda):
+@pytest.mark.parametrize('n', [10, 20])
+def test_solver_levels_are_built_on_the_device(cuda, n):
   """The coarse levels of a live edge + volume solver (its own hierarchy
   build) equal the host build on the solver's level-0 values, and the
   values refilled from them match the float64 Galerkin product."""
   from controllable_pbd_3d_gb300.mgpbd_gpu import MGPBDSolverGPU
   from controllable_pbd_3d_gb300.scenarios import cube_body
   torch = cuda
-  xr, x0, t, invm, compliance = cube_body(10, 0)
+  xr, x0, t, invm, compliance = cube_body(n, 0)
   x = torch.tensor(x0, device='cuda')
   s = MGPBDSolverGPU(x, torch.tensor(xr, device='cuda'), torch.tensor(invm, device='cuda'),
                      torch.tensor(t, device='cuda'), None, [0.0, -9.8, 0.0], 1.0 / 300,
