@@ -93,3 +93,48 @@ def test_barrier_timeout_is_an_error_and_the_handle_recovers(cuda, variant):
   s.step(2)
   ref.step(2)
   assert float((x - xr).abs().max()) <= 1e-5 * float(xr.abs().max())
+
+
+@pytest.mark.gpu
+def test_barrier_timeout_in_the_captured_body_substep(cuda):
+  """Packed bodies, substep as one captured graph: a persistent CG launch
+  inside the graph whose barrier wait runs out ends the device-side Newton
+  loop, the call returns MGPBD_ECUDA with MGPBD_STATUS_SYNC_TIMEOUT, and
+  with the limit back the graph is captured again and the same solve lands
+  where an untouched batch does."""
+  from controllable_pbd_3d_gb300._native import MGPBDError
+  from controllable_pbd_3d_gb300.batch import BodyBatch, random_bodies
+  torch = cuda
+  L = N.lib()
+  kw = dict(mode='fast', precond='cheb', cheb_scale='none', cheb_lo=1e-3, primal=False,
+            rel_tol_cg=1e-7, tol_cg=1e-14, maxiter_cg=3000, maxiter=5, atol=1e-9, rtol=3e-3,
+            kinematic_pins=True, constraints='edge_volume')
+  bodies = random_bodies(3, seed=5, dims=(3, 6), compliance=(1e-7, 1e-5))
+  g, dt = [0.0, -9.8, 0.0], 1.0 / 300
+  a = BodyBatch(bodies, g, dt, **kw)
+  b = BodyBatch(bodies, g, dt, **kw)
+  a.init()
+  b.init()
+  a.step(0)
+  b.step(0)
+  s = a.solver
+  assert L.mgpbd_set_barrier_limit(s._h, 0.0) == 0
+  s.make_prediction()
+  x_before = a.x.clone()
+  with pytest.raises(MGPBDError) as e:
+    s.solve(1)
+  assert e.value.code == ECUDA
+  assert 'timed out' in str(e.value)
+  st = C.c_uint32()
+  N.check(L.mgpbd_get_status(s._h, C.byref(st)), 'mgpbd_get_status')
+  assert st.value & SYNC_TIMEOUT
+  torch.cuda.synchronize()
+  assert L.mgpbd_set_barrier_limit(s._h, 4.0) == 0
+  with torch.no_grad():
+    a.x.copy_(x_before)
+  s.solve(1)
+  s.update_vel()
+  b.step(1)
+  assert s.stats()['status'] & SYNC_TIMEOUT == 0
+  assert torch.isfinite(a.x).all()
+  assert float((a.x - b.x).abs().max()) <= 1e-5 * float(b.x.abs().max())
