@@ -781,6 +781,39 @@ def run_profile_solve(args):
                     'status': s.stats()['status']}), flush=True)
 
 
+def run_profile_rap(args):
+  """The Galerkin coarse level of the length + volume level-0 matrix of a
+  `--size`^3 cube, built on the device (`mgpbd_device_galerkin`: copies in,
+  the k_rap_* kernels, copies out) and on the host, for profilers and the
+  setup figures: one JSON line with both times and whether they agree."""
+  import torch
+  from controllable_pbd_3d_gb300.tet_aggregation import (galerkin_structure,
+                                                         galerkin_structure_device)
+  kw = dict(SOLVER_KW)
+  kw.update(PLAIN_KW)
+  s, x, _ = make_solver(torch, args.size, kw, 'edge_volume')
+  g = s._gpu_solver
+  A0 = g._gpu_As[0]
+  ip = A0.indptr.cpu().numpy()
+  ix = A0.indices.cpu().numpy()[:A0.nnz]
+  a = A0.data.cpu().numpy()[:A0.nnz]
+  agg = g._agg[0].cpu().numpy()
+  n_agg = g._gpu_As[1].n_rows
+  del s, g
+  torch.cuda.empty_cache()
+  t0 = time.perf_counter()
+  dev = galerkin_structure_device(ip, ix, a, agg, n_agg)
+  t_dev = time.perf_counter() - t0
+  t0 = time.perf_counter()
+  host = galerkin_structure(ip, ix, a, agg, n_agg)
+  t_host = time.perf_counter() - t0
+  same = all(np.array_equal(u, v) for u, v in zip(host, dev[:4]))
+  print(json.dumps({'profile_rap': args.size, 'rows': int(len(ip) - 1), 'nnz': int(A0.nnz),
+                    'aggregates': int(n_agg), 'coarse_nnz': int(len(host[1])),
+                    'device_s_with_copies': round(t_dev, 4), 'host_s': round(t_host, 4),
+                    'bit_identical': bool(same)}), flush=True)
+
+
 def run_profile_net(args):
   """The coarse network's weights pass on the level-1 graph of a
   `--size`^3 cube (pairs from one plain Newton iteration, 100 Adam steps),
@@ -1065,6 +1098,7 @@ def main():
   # CG solve (ncu cannot profile kernels inside conditional graphs)
   ap.add_argument('--no-graph', action='store_true')
   ap.add_argument('--profile-solve', action='store_true')
+  ap.add_argument('--profile-rap', action='store_true')
   ap.add_argument('--profile-precond', default='cheb', choices=['cheb', 'vcycle'])
   ap.add_argument('--profile-maxiter', type=int, default=6000)
   # 1/0: with / without the primal (Woodbury) warm start of each CG solve
@@ -1088,6 +1122,8 @@ def main():
     run_train(args)
   elif args.profile_solve:
     run_profile_solve(args)
+  elif args.profile_rap:
+    run_profile_rap(args)
   elif args.impl == 'reference':
     run_reference(args)
   else:
