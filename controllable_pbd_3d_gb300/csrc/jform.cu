@@ -467,11 +467,29 @@ void launch_jform_lanczos(const JView& j, float* q, float* qprev, float* w, doub
   }
 }
 
-// Largest eigenvalue of the symmetric tridiagonal T (diagonal a, off-
-// diagonal b) by Sturm-sequence bisection on its Gershgorin interval.  Every
-// product that feeds a sum is rounded on its own (no fused multiply-add), so
-// the result does not depend on how the compiler contracts.
+// Number of eigenvalues of the symmetric tridiagonal T (diagonal a,
+// off-diagonal b, k rows) below x: the sign changes of the Sturm sequence.
+__device__ int sturm_below(const double* a, const double* b, int k, double x) {
+  int c = 0;
+  double d = 1.0;
+  for (int i = 0; i < k; ++i) {
+    const double q = i > 0 ? __ddiv_rn(__dmul_rn(b[i - 1], b[i - 1]), d) : 0.0;
+    d = (a[i] - x) - q;
+    if (d == 0.0) d = -1e-300;
+    if (d < 0.0) ++c;
+  }
+  return c;
+}
+
+// Largest eigenvalue of T by Sturm multisection on its Gershgorin interval,
+// one warp: each round the 32 lanes count the eigenvalues below 32 points
+// that split the interval into 33 parts, and the interval shrinks to the
+// part that holds the largest eigenvalue (the first point with all k below
+// it is the new upper end), until its width is below 1e-12 of the upper
+// end.  Every product that feeds a sum is rounded on its own (no fused
+// multiply-add).  The result is the upper end, in all lanes.
 __device__ double lanczos_lmax(const double* a, const double* b, int k) {
+  const int lane = threadIdx.x & 31;
   double lo = 1e300, hi = -1e300;
   for (int i = 0; i < k; ++i) {
     const double r = (i > 0 ? fabs(b[i - 1]) : 0.0) + (i + 1 < k ? fabs(b[i]) : 0.0);
@@ -479,19 +497,17 @@ __device__ double lanczos_lmax(const double* a, const double* b, int k) {
     hi = fmax(hi, a[i] + r);
   }
   if (!(hi >= lo) || !isfinite(hi) || !isfinite(lo)) return NAN;
-  for (int it = 0; it < 200 && hi - lo > __dmul_rn(1e-12, fmax(1.0, fabs(hi))); ++it) {
-    const double mid = __dmul_rn(0.5, lo + hi);
-    // count of eigenvalues below mid
-    int c = 0;
-    double d = 1.0;
-    for (int i = 0; i < k; ++i) {
-      const double q = i > 0 ? __ddiv_rn(__dmul_rn(b[i - 1], b[i - 1]), d) : 0.0;
-      d = (a[i] - mid) - q;
-      if (d == 0.0) d = -1e-300;
-      if (d < 0.0) ++c;
-    }
-    if (c >= k) hi = mid;  // all eigenvalues below mid
-    else lo = mid;
+  for (int it = 0; it < 60 && hi - lo > __dmul_rn(1e-12, fmax(1.0, fabs(hi))); ++it) {
+    const double step = __ddiv_rn(hi - lo, 33.0);
+    const double x = lane == 31 ? hi - step : lo + __dmul_rn(step, static_cast<double>(lane + 1));
+    const unsigned all = __ballot_sync(0xffffffffu, sturm_below(a, b, k, x) >= k);
+    // the first point with every eigenvalue below it bounds the largest;
+    // none: the largest lies above the last point
+    const int f = all ? __ffs(all) - 1 : 32;
+    const double nlo = f == 0 ? lo : __shfl_sync(0xffffffffu, x, f > 0 ? f - 1 : 0);
+    const double nhi = f == 32 ? hi : __shfl_sync(0xffffffffu, x, f < 32 ? f : 31);
+    lo = nlo;
+    hi = nhi;
   }
   return hi;
 }
@@ -499,10 +515,12 @@ __device__ double lanczos_lmax(const double* a, const double* b, int k) {
 // Chebyshev acceleration coefficients on [hi * lo_ratio, hi] (Saad,
 // "Iterative Methods for Sparse Linear Systems", 2nd ed., Alg. 12.1):
 // sigma = theta / delta, rho_0 = 1 / sigma, rho_i = 1 / (2 sigma - rho_{i-1}),
-// d_i = rho_i rho_{i-1} d_{i-1} + (2 rho_i / delta) r_i.  One thread.
+// d_i = rho_i rho_{i-1} d_{i-1} + (2 rho_i / delta) r_i.  One warp finds
+// lmax; its lane 0 writes the coefficients.
 __global__ void k_cheb_coefficients(JState* js, int steps, int degree, double lo_ratio,
                                     uint32_t* status) {
   const double lmax = lanczos_lmax(js->lz_a, js->lz_b, steps);
+  if (threadIdx.x != 0) return;
   const bool ok = isfinite(lmax) && lmax > 0.0;
   if (!ok && status) atomicOr(reinterpret_cast<unsigned int*>(status), MGPBD_STATUS_NAN);
   ChebCoef& c = js->cf;
@@ -530,7 +548,7 @@ __global__ void k_cheb_coefficients(JState* js, int steps, int degree, double lo
 void launch_cheb_coefficients(JState* js, int steps, int degree, double lo_ratio,
                               uint32_t* status, cudaStream_t s) {
   require(steps >= 1 && steps <= kMaxLanczos, MGPBD_EINVAL, "Lanczos steps out of range");
-  k_cheb_coefficients<<<1, 1, 0, s>>>(js, steps, degree, lo_ratio, status);
+  k_cheb_coefficients<<<1, 32, 0, s>>>(js, steps, degree, lo_ratio, status);
   MGPBD_CHECK_LAUNCH();
 }
 
