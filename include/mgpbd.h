@@ -112,7 +112,11 @@ typedef struct mgpbd_params {
   /* FAST mode: 1 (default) runs each CG solve as one CUDA graph with a
    * device-side while loop; 0 launches the same kernels from a host loop
    * that checks the device state every 8 iterations (for profilers that
-   * cannot look inside conditional graphs). */
+   * cannot look inside conditional graphs).  With packed bodies
+   * (mgpbd_set_bodies), 1 runs each whole substep's Newton loop as one
+   * captured graph (decisions taken on the device; captured at the first
+   * solve and again when the barrier limit changes), 0 drives the same
+   * kernels from the host loop; both give the same results bit for bit. */
   int32_t use_graph;
   /* FAST mode with MGPBD_PRECOND_CHEB: 1 (default) runs each CG solve as ONE
    * cooperative persistent kernel (grid barriers between its phases, float32
