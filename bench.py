@@ -642,6 +642,40 @@ def plain_leg(torch, args, hbm, kind, constraints):
   return plain
 
 
+# the benchmark configuration's mixed-precision multilevel variant of the
+# plain solver: 4-5 levels (the tet aggregation, then matrix-graph
+# aggregation down to at most 400 rows), float32 smoothing and transfers,
+# float64 CG scalars and a float64 dense Cholesky solve of the coarsest level
+MIXED_KW = dict(max_levels=3, max_coarse=400, coarse_solver='dense')
+
+
+def mixed_leg(torch, args, constraints):
+  """The plain AMG-PCG with the mixed-precision multilevel hierarchy
+  (MIXED_KW), timed like the plain leg."""
+  kw = dict(SOLVER_KW)
+  kw.update(PLAIN_KW)
+  kw.update(MIXED_KW)
+  sm, _, _ = make_solver(torch, args.size, kw, constraints)
+  sm.autotune(reps=5)
+  warm = min(args.warmup, 3)
+  for i in range(warm):
+    sm.step(i)
+  k = max(1, args.plain_steps)
+  tm, stm = time_steps(torch, sm, k, warm)
+  out = {'value': round(k / tm, 4), 'unit': UNIT, 'steps': k, 'warmup': warm,
+         'levels': [int(r) for r in stm[-1]['rows'] if r],
+         'newton_iters_per_step': sum(x['newton_iters'] for x in stm) / k,
+         'cg_iters_per_step': sum(x['cg_iters_total'] for x in stm) / k,
+         'status': stm[-1]['status'],
+         'config': 'CSR V-cycle PCG over the tet aggregation plus matrix-graph aggregation '
+                   '(aggregates of 8) to <= 400 rows, float32 smoothing and transfers, '
+                   'float64 CG scalars, float64 dense Cholesky on the coarsest level; each '
+                   'CG solve one CUDA graph'}
+  del sm
+  torch.cuda.empty_cache()
+  return out
+
+
 def run_ours(args):
   import torch
   ws, rank, local = dist_init(args)
@@ -715,6 +749,8 @@ def run_ours(args):
   if plain is not None:
     out['plain_fp32_amg_pcg'] = plain
     out['speedup_vs_plain'] = round(value / ws / plain['value'], 2)
+  if not args.no_mixed and cons == 'edge_volume':
+    out['mixed_multilevel_amg_pcg'] = mixed_leg(torch, args, cons)
   if not args.no_learned:
     lrn = learned_leg(torch, args, hbm, kind)
     if plain is not None:
@@ -1088,6 +1124,7 @@ def main():
   ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
   ap.add_argument('--size', type=int, default=40)
   ap.add_argument('--no-cpu-baseline', action='store_true')
+  ap.add_argument('--no-mixed', action='store_true')
   ap.add_argument('--no-plain', action='store_true')
   ap.add_argument('--plain-steps', type=int, default=3)
   ap.add_argument('--no-learned', action='store_true')
