@@ -214,3 +214,25 @@ def test_the_fast_algorithm_in_float64_is_the_exact_step():
     a = x0 + z['disp'][i].astype(np.float64)
     b = x0 + c['disp'][i].astype(np.float64)
     assert np.abs(a - b).max() <= 1e-8 * np.abs(a).max(), i
+
+
+@pytest.mark.gpu
+def test_mixed_multilevel_variant_matches_float64_oracle_at_40(cuda):
+  """The benchmark configuration's mixed-precision multilevel solver (the
+  plain AMG-PCG over 4-5 levels: tet aggregation, then matrix-graph
+  aggregation to <= 400 rows, float64 dense Cholesky on the coarsest,
+  float64 CG scalars; `bench.MIXED_KW`) on the 40^3 benchmark body: within
+  1e-5 relative of the exact float64 oracle after both fixture substeps,
+  with no CG cap reached."""
+  torch = cuda
+  z = golden('headline_40_seed0.npz')
+  kw = {**bench.SOLVER_KW, **bench.PLAIN_KW, **bench.MIXED_KW}
+  s, x, x0 = gpu_body(torch, 40, 0, kw=kw)
+  levels = [int(r) for r in s.stats()['rows'] if r]
+  assert 4 <= len(levels) <= 5 and levels[-1] <= 400, levels
+  for i in range(len(z['disp'])):
+    s.step(0)
+    assert s.stats()['status'] == 0, (i + 1, s.stats())
+    ref = x0.astype(np.float64) + z['disp'][i].astype(np.float64)
+    err = float(np.abs(x.cpu().numpy() - ref).max()) / float(np.abs(ref).max())
+    assert err <= POS_TOL, (i + 1, err)
