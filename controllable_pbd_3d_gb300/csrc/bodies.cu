@@ -100,7 +100,9 @@ __global__ void __launch_bounds__(kBT)
       L->pass = 0;
       L->cg_newton = 0;
       L->left = lim.maxiter_cg;
-      L->jc.tol_abs = tol;
+      // per-body CG: each body's bound is max(tol_cg, rel_tol_cg |b_b|), the
+      // kernel's own test
+      L->jc.tol_abs = lim.per_body_cg ? static_cast<double>(lim.tol_cg) : tol;
       L->jc.maxiter = lim.maxiter_cg;
       L->jc.warm = 0;
       L->jc.skip = 0;
@@ -139,6 +141,10 @@ __global__ void __launch_bounds__(kBT)
   }
   __syncthreads();
   if (s_skip) return;
+  if (lim.per_body_cg) {  // the kernel tested every body against its own bound
+    if (threadIdx.x == 0) L->jc.skip = 1;
+    return;
+  }
   double need = INFINITY;
   for (int32_t k = threadIdx.x; k < ba.nb; k += blockDim.x) {
     const double bound = fmax(static_cast<double>(lim.tol_cg),

@@ -58,6 +58,7 @@ struct BodyArrays {
 struct BodyLimits {
   float atol, rtol, tol_cg, rel_tol_cg;
   int32_t maxiter, maxiter_cg;
+  int32_t per_body_cg;  // 1: the CG is per body (its own bounds); one pass
 };
 
 // Loop state reset for a new substep (all bodies active)

@@ -650,6 +650,397 @@ __global__ void __launch_bounds__(kPT, STAGED ? 1 : 2) k_jcg(PArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Per-body CG of packed bodies (block-diagonal A): one CG per body, run in
+// lockstep inside one persistent launch.  Every dot product is summed per
+// body (chunks of at most kCgChunk constraints, each inside one body, one
+// warp per chunk; then one warp per body over its chunks, in order), and
+// alpha, beta and the stopping test are the body's own, so a stiff body no
+// longer holds the others to its iteration count, nor they it to theirs:
+// each converges as its own CG would.  A body that meets its bound keeps
+// its x and r (its chunks are skipped); the launch ends when every body has
+// stopped.  The Chebyshev preconditioner (one polynomial) and the vertex
+// and tet phases are those of k_jcg, unstaged.
+//
+// Per iteration: vertex phase, A p (chunked), body alphas, update
+// (chunked), body residuals, the Chebyshev steps (the last chunked), body
+// betas: 2k + 4 barriers for degree k.
+
+// chunk c of the per-warp loop: its constraint range and body
+__device__ __forceinline__ int64_t gwarp() {
+  return (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+}
+__device__ __forceinline__ int64_t nwarps() { return ((int64_t)gridDim.x * blockDim.x) >> 5; }
+
+// sum over body k's chunks (ascending) of plane q of the chunk partials;
+// all lanes of the warp get it
+__device__ __forceinline__ double body_total(const BodyCg& b, int q, int32_t k) {
+  const int lane = threadIdx.x & 31;
+  const double* cp = b.cp + (int64_t)q * b.nch;
+  double acc = 0.0;
+  for (int32_t i = b.bptr[k] + lane; i < b.bptr[k + 1]; i += 32) acc += __ldcg(cp + b.bidx[i]);
+  return warp_sum_d(acc);
+}
+
+// Vertex phase with a per-body beta: u_v = w_v sum (z_t + beta_b(t) p_t) g_{t,l}
+__device__ __forceinline__ void vphase_body_zbp(const PArgs& a, const BodyCg& b) {
+  const int lane = threadIdx.x % kVG;
+  constexpr int kPerWarp = 32 / kVG;
+  const int64_t warp = gwarp();
+  const int64_t stride = nwarps() * kPerWarp;
+  for (int64_t base = warp * kPerWarp; base < a.nv; base += stride) {
+    const int64_t v = base + (threadIdx.x & 31) / kVG;
+    const bool valid = v < a.nv;
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    const float wv = valid ? a.invm[v] : 0.0f;
+    if (valid && wv != 0.0f) {
+      const int32_t k0 = a.inc_ptr[v], k1 = a.inc_ptr[v + 1];
+      for (int32_t k = k0 + lane; k < k1; k += kVG) {
+        const float4 e = __ldg(a.gV + k);
+        const int32_t t = __float_as_int(e.w);
+        const float xt = a.z[t] + b.fb[__ldg(b.cbody + t)] * a.p[t];
+        ax += xt * e.x;
+        ay += xt * e.y;
+        az += xt * e.z;
+      }
+    }
+#pragma unroll
+    for (int o = kVG / 2; o > 0; o >>= 1) {
+      ax += __shfl_xor_sync(0xffffffffu, ax, o, kVG);
+      ay += __shfl_xor_sync(0xffffffffu, ay, o, kVG);
+      az += __shfl_xor_sync(0xffffffffu, az, o, kVG);
+    }
+    if (valid && lane == 0) a.u[v] = make_float4(wv * ax, wv * ay, wv * az, 0.0f);
+  }
+}
+
+__global__ void __launch_bounds__(kPT, 2) k_jcg_bodies(PArgs a, BodyCg b) {
+  if (a.ctl && a.ctl->skip) return;
+  __shared__ float s_c1[kMaxCheb], s_c2[kMaxCheb];
+  __shared__ int32_t warm, maxiter;
+  __shared__ double tol_abs;
+  __shared__ uint32_t status;  // this block's status bits
+  __shared__ int s_all;        // every body has stopped
+  if (threadIdx.x < kMaxCheb) {
+    s_c1[threadIdx.x] = a.js->cf.c1[threadIdx.x];
+    s_c2[threadIdx.x] = a.js->cf.c2[threadIdx.x];
+  }
+  if (threadIdx.x == 0) {
+    status = 0;
+    warm = a.ctl ? a.ctl->warm : a.warm;
+    maxiter = a.ctl ? a.ctl->maxiter : a.maxiter;
+    tol_abs = a.ctl ? a.ctl->tol_abs : a.tol_abs;
+  }
+  const float it = a.js->cf.inv_theta;
+  const int m = a.degree;
+  const int lane = threadIdx.x & 31;
+  unsigned long long gen = 0;
+  Own o;
+  o.tbeg = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  o.tend = a.ta.nt;
+  o.tstep = (int64_t)gridDim.x * blockDim.x;
+  o.tb0 = 0;
+  o.vb0 = 0;
+  o.nvb = 0;
+  o.e = nullptr;
+  o.q = nullptr;
+  o.off = nullptr;
+  o.w = nullptr;
+  __syncthreads();
+  // every block reads whether all bodies have stopped after a barrier
+  auto all_stopped = [&]() {
+    if (threadIdx.x == 0) s_all = ld_relaxed(b.ndone) >= (unsigned int)b.nb;
+    __syncthreads();
+    return s_all != 0;
+  };
+
+  // x = 0 (or the warm start), r = b - A x, p = 0, z = d = D^-1 r / theta;
+  // chunk partials of b.b, r.z and r.r
+  if (warm) {
+    vphase_warm<false>(a, o);
+    if (!grid_sync(a, gen)) return;
+  }
+  for (int64_t c = gwarp(); c < b.nch; c += nwarps()) {
+    const int2 r = __ldg(b.ch + c);
+    float bb = 0.0f, bz = 0.0f, br = 0.0f;
+    for (int64_t t = r.x + lane; t < r.y; t += 32) {
+      const float bt = a.b[t];
+      float rt = bt;
+      if (warm) {
+        rt = (float)((double)bt - tdot_warm<false>(a, o, t));
+      } else {
+        a.x[t] = 0.0f;
+      }
+      a.xc[t] = 0.0f;
+      a.r[t] = rt;
+      a.p[t] = 0.0f;
+      const float zt = dinv_of<false>(a, t) * rt * it;
+      a.z[t] = zt;
+      a.d[t] = zt;
+      bb += bt * bt;
+      bz += rt * zt;
+      br += rt * rt;
+    }
+    const double sb = warp_sum_d(bb), sz = warp_sum_d(bz), sr = warp_sum_d(br);
+    if (lane == 0) {
+      b.cp[c] = sb;
+      b.cp[b.nch + c] = sz;
+      b.cp[2LL * b.nch + c] = sr;
+    }
+  }
+  if (!grid_sync(a, gen)) return;
+  // per body: |b|^2, r.z, the bound, whether it starts stopped
+  for (int64_t k = gwarp(); k < b.nb; k += nwarps()) {
+    const double sb = body_total(b, 0, k), sz = body_total(b, 1, k), sr = body_total(b, 2, k);
+    if (lane == 0) {
+      double* sc = b.sc;
+      const double t2 = tol_abs * tol_abs, r2 = a.tol_rel * a.tol_rel * sb;
+      const double tol2 = r2 > t2 ? r2 : t2;
+      const double rr = warm ? sr : sb;
+      // a body with b = 0 (its Newton loop has ended) has x = 0 exactly
+      int stop = maxiter <= 0 || (warm && rr < tol2) || sb == 0.0;
+      if (!isfinite(sb)) {
+        atomicOr(&status, (uint32_t)MGPBD_STATUS_NAN);
+        stop = 1;
+      }
+      sc[0 * b.nb + k] = sb;   // |b|^2
+      sc[1 * b.nb + k] = sz;   // r.z
+      sc[2 * b.nb + k] = rr;   // r.r
+      sc[4 * b.nb + k] = tol2;
+      b.fa[k] = 0.0f;
+      b.fb[k] = 0.0f;
+      b.iters[k] = 0;
+      b.done[k] = stop;
+      if (stop) atomicAdd(b.ndone, 1u);
+    }
+  }
+  if (!grid_sync(a, gen)) return;
+  bool finished = all_stopped();
+
+  // the Chebyshev steps of z = M^-1 r, the last one with chunked partials
+  // of r.z into plane 2
+  auto cheb_steps = [&]() -> bool {
+    for (int i = 1; i < m; ++i) {
+      vphase<kSrcX, false>(a, o, 0.0f, a.z);
+      if (!grid_sync(a, gen)) return false;
+      if (i < m - 1) {
+        tphase_cheb<false, false>(a, o, s_c1[i], s_c2[i], nullptr);
+      } else {
+        const float c1 = s_c1[i], c2 = s_c2[i];
+        for (int64_t c = gwarp(); c < b.nch; c += nwarps()) {
+          const int2 r = __ldg(b.ch + c);
+          float acc = 0.0f;
+          for (int64_t tb = r.x + lane; tb < r.y; tb += 32 * kTB) {
+            float y[kTB];
+#pragma unroll
+            for (int q = 0; q < kTB; ++q) {
+              const int64_t t = tb + 32 * q;
+              y[q] = t < r.y ? tdot_any<false>(a, o, t) : 0.0f;
+            }
+#pragma unroll
+            for (int q = 0; q < kTB; ++q) {
+              const int64_t t = tb + 32 * q;
+              if (t < r.y) {
+                const float zt = a.z[t];
+                const float yt = y[q] + __ldg(a.ta.alpha + t) * zt;
+                const float rt = a.r[t];
+                const float rrv = dinv_of<false>(a, t) * (rt - yt);
+                const float dt = c1 * a.d[t] + c2 * rrv;
+                a.d[t] = dt;
+                const float zn = zt + dt;
+                a.z[t] = zn;
+                acc += rt * zn;
+              }
+            }
+          }
+          const double s = warp_sum_d(acc);
+          if (lane == 0) b.cp[2LL * b.nch + c] = s;
+        }
+      }
+      if (!grid_sync(a, gen)) return false;
+    }
+    return true;
+  };
+
+  if (!finished && m > 1) {
+    if (!cheb_steps()) return;
+    for (int64_t k = gwarp(); k < b.nb; k += nwarps()) {
+      const double sz = body_total(b, 2, k);
+      if (lane == 0 && !b.done[k]) {
+        b.sc[1 * b.nb + k] = sz;
+        if (!isfinite(sz)) {
+          atomicOr(&status, (uint32_t)MGPBD_STATUS_NAN);
+          b.done[k] = 1;
+          atomicAdd(b.ndone, 1u);
+        }
+      }
+    }
+    if (!grid_sync(a, gen)) return;
+    finished = all_stopped();
+  }
+
+  int32_t iters = 0;
+  while (!finished) {
+    // u = W J^T (z + beta_b p)
+    vphase_body_zbp(a, b);
+    if (!grid_sync(a, gen)) return;
+    // p = z + beta_b p; ap = A p; chunk partials of p.Ap (stopped bodies
+    // skipped)
+    for (int64_t c = gwarp(); c < b.nch; c += nwarps()) {
+      const int2 r = __ldg(b.ch + c);
+      const int32_t k = __ldg(b.chb + c);
+      if (b.done[k]) continue;
+      const float bf = b.fb[k];
+      float acc = 0.0f;
+      for (int64_t tb = r.x + lane; tb < r.y; tb += 32 * kTB) {
+        float y[kTB];
+#pragma unroll
+        for (int q = 0; q < kTB; ++q) {
+          const int64_t t = tb + 32 * q;
+          y[q] = t < r.y ? tdot_any<false>(a, o, t) : 0.0f;
+        }
+#pragma unroll
+        for (int q = 0; q < kTB; ++q) {
+          const int64_t t = tb + 32 * q;
+          if (t < r.y) {
+            const float pt = a.z[t] + bf * a.p[t];
+            const float yt = y[q] + __ldg(a.ta.alpha + t) * pt;
+            a.p[t] = pt;
+            a.ap[t] = yt;
+            acc += pt * yt;
+          }
+        }
+      }
+      const double s = warp_sum_d(acc);
+      if (lane == 0) b.cp[c] = s;
+    }
+    if (!grid_sync(a, gen)) return;
+    // body alphas
+    for (int64_t k = gwarp(); k < b.nb; k += nwarps()) {
+      if (b.done[k]) continue;  // warp-uniform
+      const double pap = body_total(b, 0, k);
+      if (lane == 0) {
+        b.sc[3 * b.nb + k] = pap;
+        if (!isfinite(pap)) atomicOr(&status, (uint32_t)MGPBD_STATUS_NAN);
+        if (!(fabs(pap) >= 1e-30) || !isfinite(pap)) {
+          b.done[k] = 1;
+          b.fa[k] = 0.0f;
+          atomicAdd(b.ndone, 1u);
+        } else {
+          if (pap <= 0.0) atomicOr(&status, (uint32_t)MGPBD_STATUS_PAP_NONPOS);
+          b.fa[k] = (float)(b.sc[1 * b.nb + k] / pap);
+        }
+      }
+    }
+    if (!grid_sync(a, gen)) return;
+    // x += alpha_b p (compensated); r -= alpha_b Ap; z = d = D^-1 r / theta;
+    // chunk partials of r.r (plane 1) and, degree 1, r.z (plane 2)
+    for (int64_t c = gwarp(); c < b.nch; c += nwarps()) {
+      const int2 r = __ldg(b.ch + c);
+      const int32_t k = __ldg(b.chb + c);
+      if (b.done[k]) continue;
+      const float al = b.fa[k];
+      float acc_rr = 0.0f, acc_rz = 0.0f;
+      for (int64_t t = r.x + lane; t < r.y; t += 32) {
+        const float pt = a.p[t], apt = a.ap[t];
+        const float s = a.x[t];
+        const float y = al * pt - a.xc[t];
+        const float sn = s + y;
+        a.xc[t] = (sn - s) - y;
+        a.x[t] = sn;
+        const float rt = a.r[t] - al * apt;
+        a.r[t] = rt;
+        const float zt = dinv_of<false>(a, t) * rt * it;
+        a.z[t] = zt;
+        a.d[t] = zt;
+        acc_rr += rt * rt;
+        acc_rz += rt * zt;
+      }
+      const double srr = warp_sum_d(acc_rr), srz = warp_sum_d(acc_rz);
+      if (lane == 0) {
+        b.cp[b.nch + c] = srr;
+        if (m == 1) b.cp[2LL * b.nch + c] = srz;
+      }
+    }
+    if (!grid_sync(a, gen)) return;
+    // body residuals and stopping tests
+    for (int64_t k = gwarp(); k < b.nb; k += nwarps()) {
+      if (b.done[k]) continue;
+      const double rr = body_total(b, 1, k);
+      if (lane == 0) {
+        b.sc[2 * b.nb + k] = rr;
+        int stop = 0;
+        if (!isfinite(rr)) {
+          atomicOr(&status, (uint32_t)MGPBD_STATUS_NAN);
+          stop = 1;
+        } else if (rr < b.sc[4 * b.nb + k]) {
+          b.iters[k] += 1;
+          stop = 1;
+        }
+        if (stop) {
+          b.done[k] = 1;
+          atomicAdd(b.ndone, 1u);
+        }
+      }
+    }
+    if (!grid_sync(a, gen)) return;
+    iters += 1;
+    if (all_stopped()) break;
+    // (the barrier between every block's read of the stopped count and the
+    // next change of it: the Chebyshev steps' own, or one for degree 1)
+    if (m > 1) {
+      if (!cheb_steps()) return;
+    } else if (!grid_sync(a, gen)) {
+      return;
+    }
+    // body betas
+    for (int64_t k = gwarp(); k < b.nb; k += nwarps()) {
+      if (b.done[k]) continue;
+      const double sz = body_total(b, 2, k);
+      if (lane == 0) {
+        b.iters[k] += 1;
+        const double rz = b.sc[1 * b.nb + k];
+        int stop = 0;
+        if (fabs(rz) < 1e-30) {
+          stop = 1;
+        } else {
+          b.fb[k] = (float)(sz / rz);
+          b.sc[1 * b.nb + k] = sz;
+          if (b.iters[k] >= maxiter) {
+            atomicOr(&status, (uint32_t)MGPBD_STATUS_CG_MAXITER);
+            stop = 1;
+          }
+        }
+        if (stop) {
+          b.done[k] = 1;
+          atomicAdd(b.ndone, 1u);
+        }
+      }
+    }
+    if (!grid_sync(a, gen)) return;
+    finished = all_stopped();
+  }
+
+  // the compensated sums, rounded once (xc keeps what the rounding dropped)
+  for (int64_t t = o.tbeg; t < o.tend; t += o.tstep) {
+    const float s = a.x[t], c = a.xc[t];
+    const float hi = s - c;
+    a.xc[t] = (s - hi) - c;
+    a.x[t] = hi;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    CgState* st = a.st;
+    if (status) atomicOr(reinterpret_cast<unsigned int*>(&st->status), status);
+    if (blockIdx.x == 0) {
+      st->iters = iters;
+      st->done = 1;
+      st->maxiter = maxiter;
+      st->body_runs = 1;
+    }
+  }
+}
+
 int64_t staged_smem_bytes(int32_t emax, int32_t tmax, int32_t vmax) {
   const int64_t b = 16LL * (emax + vmax) + 16LL * tmax + 4LL * (vmax + 1) + 4LL * vmax;
   return (b + 15) / 16 * 16;
@@ -719,14 +1110,10 @@ JcgPlan jcg_plan(const std::vector<int32_t>& inc_ptr, int32_t nv, int32_t nt, bo
   return p;
 }
 
-void launch_jcg_persistent(const JView& j, const JcgVecs& v, const JcgPlan& plan,
-                           const int32_t* part_dev, const JState* js, CgState* st, double tol_abs,
-                           double tol_rel, int maxiter, int degree, bool warm, double spin_limit_s,
-                           cudaStream_t s, const JcgCtl* ctl) {
-  require(degree >= 1 && degree <= kMaxCheb, MGPBD_EINVAL, "Chebyshev degree out of range");
-  require(plan.grid > 0, MGPBD_ESTATE, "persistent CG plan not built");
-  require(3LL * plan.grid <= v.partials_capacity, MGPBD_ERANGE, "partials buffer too small");
-  require(!plan.staged || part_dev != nullptr, MGPBD_ESTATE, "staged plan without partition");
+// the kernel arguments of one persistent dual CG launch
+static PArgs pargs_of(const JView& j, const JcgVecs& v, const JState* js, CgState* st,
+                      double tol_abs, double tol_rel, int maxiter, int degree, bool warm,
+                      double spin_limit_s, const JcgCtl* ctl) {
   PArgs a;
   a.ta.t_i = reinterpret_cast<const int4*>(j.t_i);
   require(j.gT != nullptr, MGPBD_ESTATE, "persistent CG needs the gradient planes");
@@ -757,11 +1144,9 @@ void launch_jcg_persistent(const JView& j, const JcgVecs& v, const JcgPlan& plan
   a.gs = v.gs;
   a.st = st;
   a.js = js;
-  a.part_v = plan.staged ? part_dev : nullptr;
-  a.part_t = plan.staged ? part_dev + plan.grid + 1 : nullptr;
-  a.emax = plan.emax;
-  a.tmax = plan.tmax;
-  a.vmax = plan.vmax;
+  a.part_v = nullptr;
+  a.part_t = nullptr;
+  a.emax = a.tmax = a.vmax = 0;
   a.tol_abs = tol_abs;
   a.tol_rel = tol_rel;
   a.maxiter = maxiter;
@@ -771,6 +1156,23 @@ void launch_jcg_persistent(const JView& j, const JcgVecs& v, const JcgPlan& plan
   a.ctl = ctl;
   require(!(warm || ctl) || v.ulo != nullptr, MGPBD_EINVAL, "warm start needs the ulo scratch");
   a.spin_ns = static_cast<unsigned long long>(spin_limit_s * 1e9);
+  return a;
+}
+
+void launch_jcg_persistent(const JView& j, const JcgVecs& v, const JcgPlan& plan,
+                           const int32_t* part_dev, const JState* js, CgState* st, double tol_abs,
+                           double tol_rel, int maxiter, int degree, bool warm, double spin_limit_s,
+                           cudaStream_t s, const JcgCtl* ctl) {
+  require(degree >= 1 && degree <= kMaxCheb, MGPBD_EINVAL, "Chebyshev degree out of range");
+  require(plan.grid > 0, MGPBD_ESTATE, "persistent CG plan not built");
+  require(3LL * plan.grid <= v.partials_capacity, MGPBD_ERANGE, "partials buffer too small");
+  require(!plan.staged || part_dev != nullptr, MGPBD_ESTATE, "staged plan without partition");
+  PArgs a = pargs_of(j, v, js, st, tol_abs, tol_rel, maxiter, degree, warm, spin_limit_s, ctl);
+  a.part_v = plan.staged ? part_dev : nullptr;
+  a.part_t = plan.staged ? part_dev + plan.grid + 1 : nullptr;
+  a.emax = plan.emax;
+  a.tmax = plan.tmax;
+  a.vmax = plan.vmax;
   MGPBD_CUDA(cudaMemsetAsync(v.gs, 0, sizeof(GridSync), s));
   MGPBD_CUDA(cudaMemsetAsync(st, 0, sizeof(CgState), s));
   void* args[] = {&a};
@@ -783,6 +1185,30 @@ void launch_jcg_persistent(const JView& j, const JcgVecs& v, const JcgPlan& plan
                                     plan.smem));
   MGPBD_CUDA(cudaLaunchCooperativeKernel(fn, dim3(plan.grid), dim3(kPT), args,
                                          static_cast<size_t>(plan.smem), s));
+  MGPBD_CHECK_LAUNCH();
+}
+
+void launch_jcg_bodies(const JView& j, const JcgVecs& v, const BodyCg& bc, const JState* js,
+                       CgState* st, double tol_abs, double tol_rel, int maxiter, int degree,
+                       bool warm, double spin_limit_s, cudaStream_t s, const JcgCtl* ctl) {
+  require(degree >= 1 && degree <= kMaxCheb, MGPBD_EINVAL, "Chebyshev degree out of range");
+  require(bc.nb > 0 && bc.nch > 0 && bc.ch && bc.chb && bc.bptr && bc.bidx && bc.cbody &&
+              bc.cp && bc.sc && bc.fa && bc.fb && bc.done && bc.iters && bc.ndone,
+          MGPBD_ESTATE, "per-body CG arrays not prepared");
+  PArgs a = pargs_of(j, v, js, st, tol_abs, tol_rel, maxiter, degree, warm, spin_limit_s, ctl);
+  int dev = 0, sms = 0, occ = 0;
+  MGPBD_CUDA(cudaGetDevice(&dev));
+  MGPBD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  MGPBD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_jcg_bodies, kPT, 0));
+  require(occ >= 1, MGPBD_ESTATE, "per-body CG kernel cannot be resident");
+  const int grid = std::min(occ, 2) * sms;
+  MGPBD_CUDA(cudaMemsetAsync(v.gs, 0, sizeof(GridSync), s));
+  MGPBD_CUDA(cudaMemsetAsync(st, 0, sizeof(CgState), s));
+  MGPBD_CUDA(cudaMemsetAsync(bc.ndone, 0, sizeof(uint32_t), s));
+  BodyCg b = bc;
+  void* args[] = {&a, &b};
+  MGPBD_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(k_jcg_bodies), dim3(grid),
+                                         dim3(kPT), args, 0, s));
   MGPBD_CHECK_LAUNCH();
 }
 

@@ -170,6 +170,35 @@ void launch_jcg_persistent(const JView& j, const JcgVecs& v, const JcgPlan& plan
                            double tol_rel, int maxiter, int degree, bool warm, double spin_limit_s,
                            cudaStream_t s, const JcgCtl* ctl = nullptr);
 
+// Packed bodies: the per-body CG of launch_jcg_bodies (A block diagonal
+// over the bodies).  Device arrays; the chunks and body lists are constant
+// per pack, the scalars are the kernel's scratch.
+struct BodyCg {
+  int32_t nb = 0, nch = 0;
+  const int2* ch = nullptr;        // CG chunks (begin, end), each inside one body
+  const int32_t* chb = nullptr;    // body of each chunk
+  const int32_t* bptr = nullptr;   // per body: its chunks, ascending (nb + 1)
+  const int32_t* bidx = nullptr;
+  const int32_t* cbody = nullptr;  // body of each constraint
+  double* cp = nullptr;            // 3 planes of nch chunk partials
+  double* sc = nullptr;            // 5 planes of nb per-body scalars
+  float* fa = nullptr;             // per-body alpha
+  float* fb = nullptr;             // per-body beta
+  int32_t* done = nullptr;         // per body: its CG has stopped
+  int32_t* iters = nullptr;        // per body: CG iterations
+  uint32_t* ndone = nullptr;       // bodies stopped (zeroed by the launch)
+};
+// One CG per body in one cooperative launch (unstaged phases, own grid):
+// each body's dot products, alpha, beta and stopping test (|r_b| below
+// max(tol_abs, tol_rel |b_b|)) are its own; a stopped body keeps x and r.
+// st->iters = the iterations of the longest body; status bits as
+// launch_jcg_persistent (CG_MAXITER when a body reached maxiter).  ctl as
+// there.
+void launch_jcg_bodies(const JView& j, const JcgVecs& v, const BodyCg& bc, const JState* js,
+                       CgState* st, double tol_abs, double tol_rel, int maxiter, int degree,
+                       bool warm, double spin_limit_s, cudaStream_t s,
+                       const JcgCtl* ctl = nullptr);
+
 // Work vectors of the primal persistent CG (pcg.cu): vertex vectors are
 // float4 per vertex (xyz used), s is per tet.
 struct PcgVecs {

@@ -1515,6 +1515,7 @@ int32_t Solver::run_dual(const float* b, float* x, double tol_abs, double tol_re
 
 namespace {
 constexpr int32_t kBodyChunk = 4096;  // constraints per reduction chunk
+constexpr int32_t kCgChunk = 256;     // constraints per chunk of the per-body CG
 constexpr int kBodyTrials = 10;       // line-search steps 1, 1/2, ..., 1/512
 }  // namespace
 
@@ -1593,6 +1594,35 @@ void Solver::init_bodies(const std::vector<int32_t>& t_host) {
   }
   upload(body_chunk_ptr_, cp, s);
   upload(body_chunk_idx_, ci, s);
+  // the per-body CG's chunks (at most kCgChunk constraints, inside one body)
+  // and each body's chunk list
+  {
+    std::vector<int32_t> gch, gchb, gp(nb_ + 1, 0), gi;
+    for (size_t k = 0; k < body_segs_.size(); k += 3) {
+      const int32_t lo = body_segs_[k], hi = body_segs_[k + 1], body = body_segs_[k + 2];
+      for (int32_t c = lo; c < hi; c += kCgChunk) {
+        gch.push_back(c);
+        gch.push_back(std::min(hi, c + kCgChunk));
+        gchb.push_back(body);
+      }
+    }
+    for (int32_t b : gchb) gp[b + 1]++;
+    for (int32_t b = 0; b < nb_; ++b) gp[b + 1] += gp[b];
+    gi.resize(gchb.size());
+    std::vector<int32_t> cur(gp.begin(), gp.end() - 1);
+    for (size_t c = 0; c < gchb.size(); ++c) gi[cur[gchb[c]]++] = static_cast<int32_t>(c);
+    upload(bcg_ch_, gch, s);
+    upload(bcg_chb_, gchb, s);
+    upload(bcg_bptr_, gp, s);
+    upload(bcg_bidx_, gi, s);
+    bcg_cp_.alloc(3LL * static_cast<int64_t>(gchb.size()));
+    bcg_sc_.alloc(5LL * nb_);
+    bcg_fa_.alloc(nb_);
+    bcg_fb_.alloc(nb_);
+    bcg_done_.alloc(nb_);
+    bcg_iters_.alloc(nb_);
+    bcg_ndone_.alloc(1);
+  }
   body_newton_d_.alloc(nb_);
   body_r0_d_.alloc(nb_);
   body_r_d_.alloc(nb_);
@@ -1643,7 +1673,66 @@ BodyLimits Solver::body_limits() const {
   lim.rel_tol_cg = p_.rel_tol_cg;
   lim.maxiter = p_.maxiter;
   lim.maxiter_cg = p_.maxiter_cg;
+  lim.per_body_cg = p_.body_cg ? 1 : 0;
   return lim;
+}
+
+BodyCg Solver::body_cg() {
+  BodyCg b;
+  b.nb = nb_;
+  b.nch = static_cast<int32_t>(bcg_chb_.n);
+  b.ch = reinterpret_cast<const int2*>(bcg_ch_.p);
+  b.chb = bcg_chb_.p;
+  b.bptr = bcg_bptr_.p;
+  b.bidx = bcg_bidx_.p;
+  b.cbody = cons_body_.p;
+  b.cp = bcg_cp_.p;
+  b.sc = bcg_sc_.p;
+  b.fa = bcg_fa_.p;
+  b.fb = bcg_fb_.p;
+  b.done = bcg_done_.p;
+  b.iters = bcg_iters_.p;
+  b.ndone = bcg_ndone_.p;
+  return b;
+}
+
+JcgVecs Solver::dual_vecs(const float* b, float* x) {
+  JcgVecs v;
+  v.b = b;
+  v.x = x;
+  v.xc = jxc_.p;
+  v.r = jrf_.p;
+  v.z = jz_.p;
+  v.d = jd_.p;
+  v.p = jp_.p;
+  v.ap = jap_.p;
+  v.partials = partials_.p;
+  v.partials_capacity = static_cast<int64_t>(kMaxReduceBlocks) * 16;
+  v.gs = jgs_.p;
+  v.ulo = ulo_.p;
+  return v;
+}
+
+// One CG per body (launch_jcg_bodies) to each body's own bound
+// max(tol_cg, rel_tol_cg |b_b|).
+int32_t Solver::run_dual_bodies(const float* b, float* x, int32_t maxit) {
+  cudaStream_t outer = stream_;
+  const JcgVecs v = dual_vecs(b, x);
+  MGPBD_CUDA(cudaEventRecord(ev_[0], outer));
+  dual_x_ = nullptr;
+  launch_jcg_bodies(jview(), v, body_cg(), jst_.p, cg_state_.p, p_.tol_cg, p_.rel_tol_cg, maxit,
+                    p_.cheb_degree, false, barrier_limit_s_, outer);
+  dual_x_ = x;
+  MGPBD_CUDA(cudaEventRecord(ev_[1], outer));
+  sync_read(h_state_, cg_state_.p, sizeof(CgState));
+  stats_.ms_dual += event_ms(ev_[0], ev_[1]);
+  stats_.cg_launches += 1;
+  if (static_cast<uint32_t>(h_state_->status) & MGPBD_STATUS_SYNC_TIMEOUT) {
+    status_ |= MGPBD_STATUS_SYNC_TIMEOUT;
+    throw Error(MGPBD_ECUDA, "persistent CG kernel: a grid barrier wait timed out");
+  }
+  status_ |= static_cast<uint32_t>(h_state_->status);
+  return h_state_->iters;
 }
 
 // out[k * nb + b] = sum of the chunk partials k of body b, in chunk order
@@ -1664,6 +1753,7 @@ void Solver::chunk_body_sums(int count, std::vector<double>& out) {
 // from its iterate (float64 restart residual) to the smallest missing
 // body's bound.  bnorm[b] = |b_b| (0 for bodies whose loop has ended).
 int32_t Solver::pcg_bodies(const float* b, float* x, const std::vector<double>& bnorm) {
+  if (p_.body_cg) return run_dual_bodies(b, x, p_.maxiter_cg);
   const double rel = p_.rel_tol_cg;
   const int32_t n_ch = static_cast<int32_t>(chunk_body_.size());
   double bn2 = 0.0;
@@ -1874,11 +1964,17 @@ void Solver::capture_body_graph() {
     stream_ = bs;
     launch_mask_rhs(rhs_.p, cons_body_.p, body_active_.p, nt_, bs);
     jform_setup(&L->status);
-    for (int pass = 0; pass < 6; ++pass) {
-      launch_jcg_persistent(jview(), v, jplan_, jpart_.p, jst_.p, cg_state_.p, p_.tol_cg, 0.0,
-                            p_.maxiter_cg, p_.cheb_degree, false, barrier_limit_s_, bs, &L->jc);
-      launch_chunk_dual_sq(jrf_.p, nullptr, nullptr, chunks_.p, n_ch, chunk_partials_.p, bs);
+    if (p_.body_cg) {
+      launch_jcg_bodies(jview(), v, body_cg(), jst_.p, cg_state_.p, p_.tol_cg, p_.rel_tol_cg,
+                        p_.maxiter_cg, p_.cheb_degree, false, barrier_limit_s_, bs, &L->jc);
       launch_bodies_verify(ba, L, cg_state_.p, lim, bs);
+    } else {
+      for (int pass = 0; pass < 6; ++pass) {
+        launch_jcg_persistent(jview(), v, jplan_, jpart_.p, jst_.p, cg_state_.p, p_.tol_cg, 0.0,
+                              p_.maxiter_cg, p_.cheb_degree, false, barrier_limit_s_, bs, &L->jc);
+        launch_chunk_dual_sq(jrf_.p, nullptr, nullptr, chunks_.p, n_ch, chunk_partials_.p, bs);
+        launch_bodies_verify(ba, L, cg_state_.p, lim, bs);
+      }
     }
     dual_x_ = dlam_.p;
     scatter(dlam_.p);

@@ -148,6 +148,9 @@ class Solver {
   void drop_body_graph();
   BodyArrays body_arrays();
   BodyLimits body_limits() const;
+  BodyCg body_cg();
+  JcgVecs dual_vecs(const float* b, float* x);
+  int32_t run_dual_bodies(const float* b, float* x, int32_t maxit);
   int32_t run_dual(const float* b, float* x, double tol_abs, double tol_rel, int32_t maxit,
                    bool warm, float4* ulo);
   // the per-mesh stages need set_mesh (not a caller's matrix)
@@ -212,6 +215,11 @@ class Solver {
   DevBuf<BodyLoop> body_loop_;
   DevBuf<BodyLogEntry> body_log_;
   BodyLoop* h_body_loop_ = nullptr;  // pinned
+  // per-body CG (body_cg): chunks of at most 256 constraints inside one body
+  DevBuf<int32_t> bcg_ch_, bcg_chb_, bcg_bptr_, bcg_bidx_, bcg_done_, bcg_iters_;
+  DevBuf<double> bcg_cp_, bcg_sc_;
+  DevBuf<float> bcg_fa_, bcg_fb_;
+  DevBuf<uint32_t> bcg_ndone_;
   cudaGraphExec_t body_exec_ = nullptr;
   double body_exec_limit_ = -1.0;  // barrier limit baked into the captured launches
   long long body_graph_init_launches_ = 0, body_graph_body_launches_ = 0;

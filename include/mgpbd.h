@@ -164,6 +164,14 @@ typedef struct mgpbd_params {
    * band sits at the bottom of the spectrum, where CG pays for it.  No
    * counterpart in the reference. */
   int32_t cheb_scale;
+  /* Packed bodies (mgpbd_set_bodies): 1 (default) solves each Newton system
+   * with one CG per body in one persistent launch (each body's dot
+   * products, alpha, beta and stopping test its own, |r_b| below
+   * max(tol_cg, rel_tol_cg |b_b|)); 0 runs one CG over the whole pack to
+   * rel_tol_cg of the pack's |b| and then checks each body, continuing from
+   * the iterate while some body misses its bound.  No counterpart in the
+   * reference (one body per solver). */
+  int32_t body_cg;
 } mgpbd_params;
 
 #define MGPBD_CHEB_JACOBI 0

@@ -50,6 +50,7 @@ def test_params_struct_layout():
   assert abs(p.mu - 1e6) < 1 and p.maxiter == 20 and p.maxiter_cg == 100
   assert abs(p.omega_jacobi - 2.0 / 3.0) < 1e-7 and p.use_line_search == 1
   assert p.mode == N.MGPBD_MODE_PARITY and p.cg_alias == 0
+  assert p.body_cg == 1
 
 
 def test_error_codes_and_strings():
