@@ -983,7 +983,8 @@ def run_batch(args):
   torch.cuda.set_device(0)
   hbm, kind = peaks()
   t_setup = time.perf_counter()
-  bodies = random_bodies(BATCH_BODIES, seed=0, dims=BATCH_DIMS, compliance=BATCH_COMPLIANCE)
+  n_bodies = args.batch_bodies or BATCH_BODIES
+  bodies = random_bodies(n_bodies, seed=0, dims=BATCH_DIMS, compliance=BATCH_COMPLIANCE)
   batch = BodyBatch(bodies, [0.0, -9.8, 0.0], DT, constraints='edge_volume', **fast_kw(args))
   batch.init()
   s = batch.solver
@@ -1006,7 +1007,7 @@ def run_batch(args):
       'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(t * 1e3 / args.steps, 1),
       'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
       'data': 'synthetic (seeded hex-grid bodies)',
-      'config': {'workload': f'{BATCH_BODIES} independent bodies, cells per axis uniform in '
+      'config': {'workload': f'{n_bodies} independent bodies, cells per axis uniform in '
                              f'{BATCH_DIMS[0]}..{BATCH_DIMS[1]}, 5 tets/hex, packed block-diagonal',
                  'n_verts': s.n_verts, 'n_tets': batch.n_tets,
                  'constraints': CONSTRAINT_NAMES['edge_volume'], 'n_constraints': s.n_tets,
@@ -1134,6 +1135,9 @@ def main():
   # same kernels launched from a host loop instead of one CUDA graph per
   # CG solve (ncu cannot profile kernels inside conditional graphs)
   ap.add_argument('--no-graph', action='store_true')
+  # --workload batch: fewer bodies than the configuration's 128 (the first
+  # bodies of the same seeded draw), for profiler captures
+  ap.add_argument('--batch-bodies', type=int, default=0)
   ap.add_argument('--profile-solve', action='store_true')
   ap.add_argument('--profile-rap', action='store_true')
   ap.add_argument('--profile-precond', default='cheb', choices=['cheb', 'vcycle'])
