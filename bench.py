@@ -751,6 +751,14 @@ def run_ours(args):
     out['speedup_vs_plain'] = round(value / ws / plain['value'], 2)
   if not args.no_mixed and cons == 'edge_volume':
     out['mixed_multilevel_amg_pcg'] = mixed_leg(torch, args, cons)
+  if not args.no_batch and ws == 1 and cons == 'edge_volume':
+    # the batched configuration, one timed substep after one warm-up
+    bl = batch_line(args, 1, 1)
+    out['batched'] = {k: bl[k] for k in ('value', 'unit', 'steps', 'warmup', 'ms_per_step',
+                                         'newton_iters_per_step', 'cg_iters_per_step',
+                                         'status', 'solver', 'roofline', 'clocks',
+                                         'gpu_launches')}
+    out['batched']['config'] = bl['config']
   if not args.no_learned:
     lrn = learned_leg(torch, args, hbm, kind)
     if plain is not None:
@@ -964,18 +972,20 @@ def run_slab(args):
 
 
 BATCH_BODIES = 128
+SOLVER_BODY_CG = True  # one CG per body (the library default)
 BATCH_DIMS = (6, 30)
 BATCH_COMPLIANCE = (1e-8, 1e-5)
 
 
-def run_batch(args):
+def batch_line(args, steps, warmup):
   """The batched configuration: 128 independent bodies, hex-grid cells per
   axis uniform in 6..30 (5 tets per hex, cell size 1/40, top face pinned,
   1 % jitter), each with its own compliance log-uniform in [1e-8, 1e-5],
   length + volume constraints, packed into one block-diagonal system.
   The FAST step with per-body Newton loops (own residual, stopping test
-  and line-search step per body) over one CG solve per Newton iteration,
-  verified per body.  One JSON line, fast step only (the plain AMG-PCG on
+  and line-search step per body) and one CG per body in one persistent
+  launch, each substep one replay of the captured graph (`--no-graph`: the
+  host loop).  Returns the JSON dict (fast step only: the plain AMG-PCG on
   the stiffest of these bodies does not reach 1e-6 within the cap)."""
   import torch
   from controllable_pbd_3d_gb300 import _native as N
@@ -989,22 +999,22 @@ def run_batch(args):
   batch.init()
   s = batch.solver
   t_setup = time.perf_counter() - t_setup
-  for i in range(args.warmup):
+  for i in range(warmup):
     batch.step(i)
   torch.cuda.synchronize()
   L = N.lib()
   c0 = L.mgpbd_launch_count()
   flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device='cuda')
   with ClockSampler(0) as clk:
-    t, st = time_steps(torch, s, args.steps, args.warmup, flush)
+    t, st = time_steps(torch, s, steps, warmup, flush)
   launches = L.mgpbd_launch_count() - c0
   bst = s.body_stats()
   roof = roofline_from_steps(st, s.n_tets, s.n_verts, FAST_KW['cheb_degree'], hbm, kind, 0,
                              'edge_volume', operator_shape(s))
   comp = np.array([b.compliance for b in bodies])
   out = {
-      'metric': METRIC, 'value': round(args.steps / t, 4), 'unit': UNIT, 'n_gpus': 1,
-      'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(t * 1e3 / args.steps, 1),
+      'metric': METRIC, 'value': round(steps / t, 4), 'unit': UNIT, 'n_gpus': 1,
+      'steps': steps, 'warmup': warmup, 'ms_per_step': round(t * 1e3 / steps, 1),
       'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
       'data': 'synthetic (seeded hex-grid bodies)',
       'config': {'workload': f'{n_bodies} independent bodies, cells per axis uniform in '
@@ -1017,17 +1027,27 @@ def run_batch(args):
                  'dt': DT, 'rel_res_cg': 1e-6,
                  'l2': 'flushed between timed substeps (256 MB write, inside the timed region)',
                  'setup_s': round(t_setup, 1)},
-      'solver': 'FAST, per-body Newton loops: dual persistent Chebyshev-8 CG on A, '
-                'verified per body',
-      'newton_iters_per_step': sum(r['newton_iters'] for r in st) / args.steps,
-      'cg_iters_per_step': sum(r['cg_iters_total'] for r in st) / args.steps,
-      'cg_launches_per_step': sum(r['cg_launches'] for r in st) / args.steps,
+      'solver': ('FAST, per-body Newton loops, one CG per body in one persistent launch '
+                 '(Chebyshev-8 on A)' if SOLVER_BODY_CG else
+                 'FAST, per-body Newton loops: one Chebyshev-8 CG on A over the pack, verified '
+                 'per body') + (', the substep one captured CUDA graph' if not args.no_graph
+                                else ', host loop'),
+      'newton_iters_per_step': sum(r['newton_iters'] for r in st) / steps,
+      'cg_iters_per_step': sum(r['cg_iters_total'] for r in st) / steps,
+      'cg_launches_per_step': sum(r['cg_launches'] for r in st) / steps,
       'body_newton_iters_last_step': {'min': int(bst['newton_iters'].min()),
                                       'median': float(np.median(bst['newton_iters'])),
                                       'max': int(bst['newton_iters'].max())},
       'maxiter_cg': SOLVER_KW['maxiter_cg'], 'status': st[-1]['status'],
       'gpu_launches': int(launches), 'clocks': clk.summary(), 'roofline': roof}
-  print(json.dumps(out), flush=True)
+  del batch, s, flush
+  torch.cuda.empty_cache()
+  return out
+
+
+def run_batch(args):
+  """`--workload batch`: the batched configuration's own JSON line."""
+  print(json.dumps(batch_line(args, args.steps, args.warmup)), flush=True)
 
 
 TRAIN_SET_BODIES = 256  # the training-set configuration
@@ -1084,7 +1104,14 @@ def run_train(args):
          'held_out': f'{args.size}^3 benchmark body, 32 pairs',
          'held_out_coarse_energy': {'network': e_net, 'one_jacobi_sweep': e_one},
          'network_over_one_sweep': round(e_net / e_one, 4) if e_one else None}
-  print(json.dumps(out), flush=True)
+  del batch, s, flush
+  torch.cuda.empty_cache()
+  return out
+
+
+def run_batch(args):
+  """`--workload batch`: the batched configuration's own JSON line."""
+  print(json.dumps(batch_line(args, args.steps, args.warmup)), flush=True)
 
 
 def run_reference(args):
@@ -1126,6 +1153,7 @@ def main():
   ap.add_argument('--size', type=int, default=40)
   ap.add_argument('--no-cpu-baseline', action='store_true')
   ap.add_argument('--no-mixed', action='store_true')
+  ap.add_argument('--no-batch', action='store_true')
   ap.add_argument('--no-plain', action='store_true')
   ap.add_argument('--plain-steps', type=int, default=3)
   ap.add_argument('--no-learned', action='store_true')
