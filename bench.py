@@ -1011,6 +1011,9 @@ def batch_line(args, steps, warmup):
   bst = s.body_stats()
   roof = roofline_from_steps(st, s.n_tets, s.n_verts, FAST_KW['cheb_degree'], hbm, kind, 0,
                              'edge_volume', operator_shape(s))
+  if SOLVER_BODY_CG:
+    roof['kernel'] = 'k_jcg_bodies (one dual persistent Chebyshev-8 CG per body, one launch)'
+
   comp = np.array([b.compliance for b in bodies])
   out = {
       'metric': METRIC, 'value': round(steps / t, 4), 'unit': UNIT, 'n_gpus': 1,
