@@ -1480,18 +1480,7 @@ void Solver::solve(int32_t frame) {
 int32_t Solver::run_dual(const float* b, float* x, double tol_abs, double tol_rel, int32_t maxit,
                          bool warm, float4* ulo) {
   cudaStream_t outer = stream_;
-  JcgVecs v;
-  v.b = b;
-  v.x = x;
-  v.xc = jxc_.p;
-  v.r = jrf_.p;
-  v.z = jz_.p;
-  v.d = jd_.p;
-  v.p = jp_.p;
-  v.ap = jap_.p;
-  v.partials = partials_.p;
-  v.partials_capacity = static_cast<int64_t>(kMaxReduceBlocks) * 16;
-  v.gs = jgs_.p;
+  JcgVecs v = dual_vecs(b, x);
   v.ulo = ulo;
   MGPBD_CUDA(cudaEventRecord(ev_[0], outer));
   dual_x_ = nullptr;
@@ -1921,19 +1910,7 @@ void Solver::capture_body_graph() {
   const BodyArrays ba = body_arrays();
   const BodyLimits lim = body_limits();
   BodyLoop* L = body_loop_.p;
-  JcgVecs v;
-  v.b = rhs_.p;
-  v.x = dlam_.p;
-  v.xc = jxc_.p;
-  v.r = jrf_.p;
-  v.z = jz_.p;
-  v.d = jd_.p;
-  v.p = jp_.p;
-  v.ap = jap_.p;
-  v.partials = partials_.p;
-  v.partials_capacity = static_cast<int64_t>(kMaxReduceBlocks) * 16;
-  v.gs = jgs_.p;
-  v.ulo = ulo_.p;
+  const JcgVecs v = dual_vecs(rhs_.p, dlam_.p);
   try {
     long long c0 = g_launches.load();
     MGPBD_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
