@@ -61,7 +61,7 @@ class Params(C.Structure):
       ('max_coarse', i32), ('kinematic_pins', i32), ('coarse_sweeps', i32), ('cg_alias', i32),
       ('compliance', f32), ('precond', i32), ('cheb_degree', i32), ('cheb_lo', f32),
       ('use_graph', i32), ('persistent', i32), ('primal', i32), ('primal_tol', f32),
-      ('learned_accept', f32), ('learned_stall', i32), ('cheb_scale', i32), ('body_cg', i32),
+      ('learned_accept', f32), ('learned_stall', i32), ('cheb_scale', i32), ('body_cg', i32), ('warm_substep', i32),
   ]
 
 

@@ -119,6 +119,7 @@ void mgpbd_default_params(mgpbd_params* p) {
   p->learned_stall = 1000;
   p->cheb_scale = MGPBD_CHEB_JACOBI;
   p->body_cg = 1;
+  p->warm_substep = 0;
 }
 
 const char* mgpbd_strerror(int code) {

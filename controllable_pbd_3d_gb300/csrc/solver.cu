@@ -308,6 +308,7 @@ void Solver::set_mesh(const float* x_ref, const float* invm, const int32_t* t_i,
     jcg_exec_ = nullptr;
   }
   drop_body_graph();
+  have_prev_ = false;
 }
 
 void Solver::sync_read(void* host, const void* dev, size_t bytes) {
@@ -324,6 +325,7 @@ double Solver::finalize_read(const double* partials, int blocks) {
 // ---------------------------------------------------------------------------
 // MGPBDSolverGPU.init (cons/mgpbd_gpu.py:92-114)
 void Solver::init() {
+  have_prev_ = false;
   if (matrix_mode_) {
     init_matrix();
     return;
@@ -803,7 +805,10 @@ int32_t Solver::pcg_cheb(const float* b, float* x) {
         return its;
       }
     }
-    // one cooperative kernel for the (rest of the) solve
+    // one cooperative kernel for the (rest of the) solve; warm_substep: x
+    // holds the previous substep's first solution
+    if (warm_next_) warm = true;
+    warm_next_ = false;
     return its + run_dual(b, x, p_.tol_cg, p_.rel_tol_cg, left, warm, ulo_.p);
   }
   if (!p_.use_graph) {
@@ -1461,7 +1466,21 @@ void Solver::solve(int32_t frame) {
       break;
     }
     fill_matrices();
+    const bool warm_sub = ite == 0 && p_.warm_substep && cheb() && p_.persistent && !primal() &&
+                          p_.mode == MGPBD_MODE_FAST;
+    if (warm_sub && have_prev_) {
+      MGPBD_CUDA(cudaMemcpyAsync(dlam_.p, dlam_prev_.p, sizeof(float) * nt_,
+                                 cudaMemcpyDeviceToDevice, stream_));
+      warm_next_ = true;
+    }
     int32_t it = pcg(rhs_.p, dlam_.p);
+    warm_next_ = false;
+    if (warm_sub && !(status_ & (MGPBD_STATUS_NAN | MGPBD_STATUS_CG_MAXITER))) {
+      if (dlam_prev_.n != nt_) dlam_prev_.alloc(nt_);
+      MGPBD_CUDA(cudaMemcpyAsync(dlam_prev_.p, dlam_.p, sizeof(float) * nt_,
+                                 cudaMemcpyDeviceToDevice, stream_));
+      have_prev_ = true;
+    }
     scatter(dlam_.p);
     double omega = p_.use_line_search ? line_search() : 1.0;
     apply_dpos(omega);

@@ -200,6 +200,11 @@ class Solver {
   bool matrix_mode_ = false;     // set_matrix: a caller's level-0 matrix, no mesh
   double barrier_limit_s_ = 4.0; // grid-barrier wait limit of the persistent kernels
   const float* dual_x_ = nullptr;  // x of the last persistent dual solve (its low part in jxc_)
+  // warm_substep: the first solution of the last substep, and whether the
+  // next dual solve starts from what x holds
+  DevBuf<float> dlam_prev_;
+  bool have_prev_ = false;
+  bool warm_next_ = false;
   // packed bodies (set_bodies)
   int32_t nb_ = 0;
   std::vector<int32_t> body_vert_off_, body_segs_, chunk_body_;

@@ -99,6 +99,8 @@ class MGPBDSolverGPU:
                    bodies, one graph per substep;
     body_cg        packed bodies: one CG per body in one launch (True) or one
                    CG over the pack, verified per body (False);
+    warm_substep   FAST dual persistent CG, one body: start each substep's
+                   first solve from the previous substep's solution;
     constraints    'arap' (the reference: one ARAP constraint per tet) or
                    'edge_volume' (one length constraint per unique tet edge
                    and one volume constraint det F - 1 per tet, alpha~ =
@@ -120,7 +122,7 @@ class MGPBDSolverGPU:
                coarse_solver='jacobi', smoother='jacobi', max_levels=0, max_coarse=400,
                kinematic_pins=False, coarse_sweeps=0, cg_alias=False, compliance=0.0,
                precond='vcycle', cheb_degree=8, cheb_lo=0.01, cheb_scale='jacobi',
-               use_graph=True, body_cg=True,
+               use_graph=True, body_cg=True, warm_substep=False,
                persistent=True, primal=False, primal_tol=1e-2, learned_accept=0.1, learned_stall=1000,
                constraints='arap', check_finite=True):
     if aggregation != 'tet':
@@ -210,6 +212,7 @@ class MGPBDSolverGPU:
     p.cheb_scale = {'jacobi': 0, 'none': 1}[cheb_scale]
     p.use_graph = int(bool(use_graph))
     p.body_cg = int(bool(body_cg))
+    p.warm_substep = int(bool(warm_substep))
     p.persistent = int(persistent)  # True / 1, 2 (unstaged) or False / 0
     p.primal = int(bool(primal))
     p.primal_tol = float(primal_tol)

@@ -172,6 +172,12 @@ typedef struct mgpbd_params {
    * the iterate while some body misses its bound.  No counterpart in the
    * reference (one body per solver). */
   int32_t body_cg;
+  /* FAST mode, MGPBD_PRECOND_CHEB, persistent, dual (primal 0), one body:
+   * 1 starts the first Newton iteration's CG of each substep from the
+   * previous substep's first solution (its residual b - A x formed in
+   * float64) instead of 0; the stopping test is unchanged (relative to
+   * |b|).  0 (default): from 0, as the reference (cons/mgpcg_gpu.py:272). */
+  int32_t warm_substep;
 } mgpbd_params;
 
 #define MGPBD_CHEB_JACOBI 0
