@@ -3,7 +3,8 @@ float64 oracle with exact linear solves.
 
 The solver is `bench.py`'s FAST step exactly (`SOLVER_KW` + `FAST_KW`:
 dual persistent CG preconditioned by a Chebyshev-8 polynomial in A, CG to
-relative residual 1e-6, Newton maxiter 20 / atol 1e-4 / rtol 1e-2, no
+relative residual 1e-6, each substep's first solve started from the
+previous substep's solution, Newton maxiter 20 / atol 1e-4 / rtol 1e-2, no
 damping, pinned vertices kinematic) on the length + volume constraint
 system.  The oracle
 (`oracle/mgpbd_oracle.py`, `linear='exact'`) runs the same Newton loop and
