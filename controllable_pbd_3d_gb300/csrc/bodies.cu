@@ -5,6 +5,8 @@
 // multiply-add), as the host compiles them.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "bodies.cuh"
 
 namespace mgpbd {
@@ -211,7 +213,39 @@ __global__ void __launch_bounds__(kBT)
   }
 }
 
+__global__ void k_bodies_warm_in(BodyLoop* L, const int32_t* have_prev, float* x,
+                                 const float* prev, int32_t n) {
+  if (L->ite != 0 || !*have_prev) return;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = prev[i];
+  if (blockIdx.x == 0 && threadIdx.x == 0) L->jc.warm = 1;
+}
+
+__global__ void k_bodies_warm_out(const BodyLoop* L, int32_t* have_prev, const float* x,
+                                  float* prev, int32_t n) {
+  if (L->ite != 0 || (L->status & (MGPBD_STATUS_NAN | MGPBD_STATUS_CG_MAXITER))) return;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    prev[i] = x[i];
+  if (blockIdx.x == 0 && threadIdx.x == 0) *have_prev = 1;
+}
+
 }  // namespace
+
+void launch_bodies_warm_in(BodyLoop* L, const int32_t* have_prev, float* x, const float* prev,
+                           int32_t n, cudaStream_t s) {
+  k_bodies_warm_in<<<std::max(1, std::min((n + kBT - 1) / kBT, 4096)), kBT, 0, s>>>(L, have_prev, x,
+                                                                                 prev, n);
+  MGPBD_CHECK_LAUNCH();
+}
+
+void launch_bodies_warm_out(const BodyLoop* L, int32_t* have_prev, const float* x, float* prev,
+                            int32_t n, cudaStream_t s) {
+  k_bodies_warm_out<<<std::max(1, std::min((n + kBT - 1) / kBT, 4096)), kBT, 0, s>>>(L, have_prev,
+                                                                                  x, prev, n);
+  MGPBD_CHECK_LAUNCH();
+}
 
 void launch_bodies_reset(const BodyArrays& ba, BodyLoop* L, cudaStream_t s) {
   k_bodies_reset<<<1, kBT, 0, s>>>(ba, L);

@@ -77,6 +77,13 @@ void launch_bodies_verify(const BodyArrays& ba, BodyLoop* L, const CgState* st,
 void launch_bodies_cur(const BodyArrays& ba, cudaStream_t s);
 // From chunk partials of n_trials trial norms: each active body's step,
 // its iteration count, the log entry; ite += 1
+// warm_substep: at the first Newton iteration, x = the previous substep's
+// first solution and the next CG pass starts from it (when *have_prev)
+void launch_bodies_warm_in(BodyLoop* L, const int32_t* have_prev, float* x, const float* prev,
+                           int32_t n, cudaStream_t s);
+// ... and after that iteration's solve (no NaN, no cap), keep it
+void launch_bodies_warm_out(const BodyLoop* L, int32_t* have_prev, const float* x, float* prev,
+                            int32_t n, cudaStream_t s);
 void launch_bodies_omega(const BodyArrays& ba, BodyLoop* L, const BodyLimits& lim, int n_trials,
                          cudaStream_t s);
 

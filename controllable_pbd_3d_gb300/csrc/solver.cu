@@ -1630,6 +1630,10 @@ void Solver::init_bodies(const std::vector<int32_t>& t_host) {
     bcg_done_.alloc(nb_);
     bcg_iters_.alloc(nb_);
     bcg_ndone_.alloc(1);
+    dlam_prev_.alloc(nt_);
+    body_have_prev_.alloc(1);
+    MGPBD_CUDA(cudaMemsetAsync(body_have_prev_.p, 0, sizeof(int32_t), s));
+    have_prev_ = false;
   }
   body_newton_d_.alloc(nb_);
   body_r0_d_.alloc(nb_);
@@ -1723,13 +1727,13 @@ JcgVecs Solver::dual_vecs(const float* b, float* x) {
 
 // One CG per body (launch_jcg_bodies) to each body's own bound
 // max(tol_cg, rel_tol_cg |b_b|).
-int32_t Solver::run_dual_bodies(const float* b, float* x, int32_t maxit) {
+int32_t Solver::run_dual_bodies(const float* b, float* x, int32_t maxit, bool warm) {
   cudaStream_t outer = stream_;
   const JcgVecs v = dual_vecs(b, x);
   MGPBD_CUDA(cudaEventRecord(ev_[0], outer));
   dual_x_ = nullptr;
   launch_jcg_bodies(jview(), v, body_cg(), jst_.p, cg_state_.p, p_.tol_cg, p_.rel_tol_cg, maxit,
-                    p_.cheb_degree, false, barrier_limit_s_, outer);
+                    p_.cheb_degree, warm, barrier_limit_s_, outer);
   dual_x_ = x;
   MGPBD_CUDA(cudaEventRecord(ev_[1], outer));
   sync_read(h_state_, cg_state_.p, sizeof(CgState));
@@ -1761,7 +1765,11 @@ void Solver::chunk_body_sums(int count, std::vector<double>& out) {
 // from its iterate (float64 restart residual) to the smallest missing
 // body's bound.  bnorm[b] = |b_b| (0 for bodies whose loop has ended).
 int32_t Solver::pcg_bodies(const float* b, float* x, const std::vector<double>& bnorm) {
-  if (p_.body_cg) return run_dual_bodies(b, x, p_.maxiter_cg);
+  if (p_.body_cg) {
+    const bool warm = warm_next_;
+    warm_next_ = false;
+    return run_dual_bodies(b, x, p_.maxiter_cg, warm);
+  }
   const double rel = p_.rel_tol_cg;
   const int32_t n_ch = static_cast<int32_t>(chunk_body_.size());
   double bn2 = 0.0;
@@ -1857,7 +1865,19 @@ void Solver::solve_bodies() {
     launch_mask_rhs(rhs_.p, cons_body_.p, body_active_.p, nt_, s);
     fill_matrices();
     dual_x_ = nullptr;
+    const bool warm_sub = ite == 0 && p_.warm_substep && p_.body_cg;
+    if (warm_sub && have_prev_) {
+      MGPBD_CUDA(cudaMemcpyAsync(dlam_.p, dlam_prev_.p, sizeof(float) * nt_,
+                                 cudaMemcpyDeviceToDevice, s));
+      warm_next_ = true;
+    }
     const int32_t it = pcg_bodies(rhs_.p, dlam_.p, bnorm);
+    warm_next_ = false;
+    if (warm_sub && !(status_ & (MGPBD_STATUS_NAN | MGPBD_STATUS_CG_MAXITER))) {
+      MGPBD_CUDA(cudaMemcpyAsync(dlam_prev_.p, dlam_.p, sizeof(float) * nt_,
+                                 cudaMemcpyDeviceToDevice, s));
+      have_prev_ = true;
+    }
     scatter(dlam_.p);
     // per-body line search (cons/mgpbd_gpu.py:379-391): the first of 1,
     // 1/2, ..., 1/512 whose dual norm (updated lambda) beats the current one
@@ -1961,9 +1981,13 @@ void Solver::capture_body_graph() {
     launch_mask_rhs(rhs_.p, cons_body_.p, body_active_.p, nt_, bs);
     jform_setup(&L->status);
     if (p_.body_cg) {
+      if (p_.warm_substep)
+        launch_bodies_warm_in(L, body_have_prev_.p, dlam_.p, dlam_prev_.p, nt_, bs);
       launch_jcg_bodies(jview(), v, body_cg(), jst_.p, cg_state_.p, p_.tol_cg, p_.rel_tol_cg,
                         p_.maxiter_cg, p_.cheb_degree, false, barrier_limit_s_, bs, &L->jc);
       launch_bodies_verify(ba, L, cg_state_.p, lim, bs);
+      if (p_.warm_substep)
+        launch_bodies_warm_out(L, body_have_prev_.p, dlam_.p, dlam_prev_.p, nt_, bs);
     } else {
       for (int pass = 0; pass < 6; ++pass) {
         launch_jcg_persistent(jview(), v, jplan_, jpart_.p, jst_.p, cg_state_.p, p_.tol_cg, 0.0,

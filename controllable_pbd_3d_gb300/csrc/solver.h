@@ -150,7 +150,7 @@ class Solver {
   BodyLimits body_limits() const;
   BodyCg body_cg();
   JcgVecs dual_vecs(const float* b, float* x);
-  int32_t run_dual_bodies(const float* b, float* x, int32_t maxit);
+  int32_t run_dual_bodies(const float* b, float* x, int32_t maxit, bool warm);
   int32_t run_dual(const float* b, float* x, double tol_abs, double tol_rel, int32_t maxit,
                    bool warm, float4* ulo);
   // the per-mesh stages need set_mesh (not a caller's matrix)
@@ -225,6 +225,7 @@ class Solver {
   DevBuf<double> bcg_cp_, bcg_sc_;
   DevBuf<float> bcg_fa_, bcg_fb_;
   DevBuf<uint32_t> bcg_ndone_;
+  DevBuf<int32_t> body_have_prev_;  // warm_substep: dlam_prev_ holds a solution
   cudaGraphExec_t body_exec_ = nullptr;
   double body_exec_limit_ = -1.0;  // barrier limit baked into the captured launches
   long long body_graph_init_launches_ = 0, body_graph_body_launches_ = 0;

@@ -145,8 +145,8 @@ def test_set_bodies_validates_its_ranges():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize('body_cg', [True, False])
-def test_per_body_newton_equals_separate_substeps(cuda, body_cg):
+@pytest.mark.parametrize('body_cg,warm', [(True, False), (False, False), (True, True)])
+def test_per_body_newton_equals_separate_substeps(cuda, body_cg, warm):
   """Packed bodies with per-body Newton loops (own residual, stopping test
   and line-search step; the shared CG solve verified per body) land where
   each body's own substeps land: positions within 1e-5 relative after three
@@ -164,7 +164,7 @@ def test_per_body_newton_equals_separate_substeps(cuda, body_cg):
   g, dt = [0.0, -9.8, 0.0], 1 / 300
   kw = dict(mode='fast', precond='cheb', cheb_scale='none', cheb_lo=1e-3, primal=False,
             rel_tol_cg=1e-7, tol_cg=1e-14, maxiter_cg=6000, maxiter=10, atol=1e-9, rtol=3e-3,
-            kinematic_pins=True, constraints=constraints)
+            kinematic_pins=True, constraints=constraints, warm_substep=warm)
   bodies = random_bodies(4, seed=2, dims=(3, 7), compliance=(1e-8, 1e-5))
   batch = BodyBatch(bodies, g, dt, body_cg=body_cg, **kw)
   assert batch.per_body
@@ -191,8 +191,8 @@ def test_per_body_newton_equals_separate_substeps(cuda, body_cg):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize('body_cg', [True, False])
-def test_captured_substep_equals_host_loop(cuda, body_cg):
+@pytest.mark.parametrize('body_cg,warm', [(True, False), (False, False), (True, True)])
+def test_captured_substep_equals_host_loop(cuda, body_cg, warm):
   """The packed-body substep as one captured CUDA graph (use_graph: the
   Newton loop a device-side while loop, every decision taken on the device)
   and the same substep driven by the host loop take the same decisions in
@@ -200,7 +200,8 @@ def test_captured_substep_equals_host_loop(cuda, body_cg):
   and the Newton log agree bit for bit over three substeps, and the graph
   replays (one capture, three launches).  Both linear solves: one CG per
   body in one launch (body_cg), and one CG over the pack verified per
-  body."""
+  body; and the per-body CG with each substep's first solve started from
+  the previous substep's solution (warm_substep)."""
   from controllable_pbd_3d_gb300.batch import BodyBatch
   g, dt = [0.0, -9.8, 0.0], 1 / 300
   kw = dict(mode='fast', precond='cheb', cheb_scale='none', cheb_lo=1e-3, primal=False,
@@ -209,7 +210,7 @@ def test_captured_substep_equals_host_loop(cuda, body_cg):
   bodies = random_bodies(5, seed=3, dims=(3, 7), compliance=(1e-8, 1e-5))
   runs = {}
   for graph in (True, False):
-    batch = BodyBatch(bodies, g, dt, use_graph=graph, body_cg=body_cg, **kw)
+    batch = BodyBatch(bodies, g, dt, use_graph=graph, body_cg=body_cg, warm_substep=warm, **kw)
     batch.init()
     hist = []
     for k in range(3):
