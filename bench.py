@@ -1164,7 +1164,7 @@ def run_reference(args):
   print(json.dumps(out), flush=True)
 
 
-def main():
+def arg_parser():
   ap = argparse.ArgumentParser()
   ap.add_argument('--gpus', type=int, default=1)
   ap.add_argument('--steps', type=int, default=10)
@@ -1197,10 +1197,15 @@ def main():
   # the coarse network's weights pass alone (for ncu)
   ap.add_argument('--profile-net', action='store_true')
   ap.add_argument('--profile-reps', type=int, default=5)
-  # the 40^3 cube (headline) or the stiff-drag slab (one line, fast step only)
-  # C3: the learned correction's training set (one line, no timed substeps)
+  # cube: the 40^3 headline line with its legs; slab: the stiff-drag slab,
+  # batch: the 128-body configuration (one line each, fast step only);
+  # train: the learned correction's 256-body training set (no timed substeps)
   ap.add_argument('--workload', default='cube', choices=['cube', 'slab', 'batch', 'train'])
-  args = ap.parse_args()
+  return ap
+
+
+def main():
+  args = arg_parser().parse_args()
   if args.profile_net:
     run_profile_net(args)
   elif args.workload == 'slab' and args.impl == 'ours':

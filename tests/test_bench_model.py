@@ -126,3 +126,18 @@ def test_cpu_substeps_load_no_product_library():
   out = subprocess.run([sys.executable, '-c', code], cwd=ROOT, capture_output=True, text=True,
                        timeout=600, check=True).stdout.strip().splitlines()
   assert out[-1] == '0'
+
+
+def test_bench_defaults_and_legs():
+  """The driver's plain `python bench.py` runs the headline with every leg
+  (N = 1, 10 timed substeps after 3 warm-up); each leg can be left out."""
+  import bench
+  a = bench.arg_parser().parse_args([])
+  assert (a.gpus, a.steps, a.warmup, a.impl, a.workload, a.size) == (1, 10, 3, 'ours', 'cube', 40)
+  assert a.constraints == 'edge_volume'
+  assert not (a.no_plain or a.no_mixed or a.no_learned or a.no_arap or a.no_batch or
+              a.no_cpu_baseline or a.no_graph)
+  b = bench.arg_parser().parse_args(['--workload', 'batch', '--batch-bodies', '16', '--no-graph'])
+  assert b.workload == 'batch' and b.batch_bodies == 16 and b.no_graph
+  assert bench.FAST_KW['warm_substep'] and bench.FAST_KW['cheb_scale'] == 'none'
+  assert bench.MIXED_KW['coarse_solver'] == 'dense' and bench.MIXED_KW['max_levels'] >= 2
