@@ -155,12 +155,13 @@ class ExactDualSolve:
 
 
 def chebyshev_pcg(apply_A, b, degree=8, lo=1e-3, scale=None, rel_tol=1e-6, tol_abs=0.0,
-                  maxiter=6000, lmax=None):
+                  maxiter=6000, lmax=None, x0=None):
   """CG preconditioned by a degree-`degree` Chebyshev polynomial in S A
   (S = diag(scale), or the identity) on [lo * 1.02 lmax, 1.02 lmax], lmax
   the largest eigenvalue of S A (Lanczos to 1e-10 unless given), from
-  x = 0, until |r| < max(tol_abs, rel_tol |b|): the linear solve of the
-  library's FAST mode in float64.  Returns (x, iterations)."""
+  x = 0 (or x0: the library's warm start), until |r| < max(tol_abs,
+  rel_tol |b|): the linear solve of the library's FAST mode in float64.
+  Returns (x, iterations)."""
   b = np.asarray(b, np.float64)
   n = len(b)
   sc = np.ones(n) if scale is None else np.asarray(scale, np.float64)
@@ -186,8 +187,8 @@ def chebyshev_pcg(apply_A, b, degree=8, lo=1e-3, scale=None, rel_tol=1e-6, tol_a
       rho = rho_n
     return x
 
-  x = np.zeros(n)
-  r = b.copy()
+  x = np.zeros(n) if x0 is None else np.array(x0, np.float64)
+  r = b.copy() if x0 is None else b - apply_A(x)
   tol = max(tol_abs, rel_tol * np.linalg.norm(b))
   if np.linalg.norm(r) < tol:
     return x, 0

@@ -475,20 +475,24 @@ class MGPBDOracle:
                use_line_search=True, dtype=np.float32, kinematic_pins=False, rel_tol_cg=0.0,
                smoother='jacobi', coarse='jacobi', extra_levels=0, max_coarse=400,
                coarse_sweeps=0, hierarchy=None, cg_alias=False, compliance=0.0, ctype=None,
-               linear='pcg', exact_tol=1e-11):
+               linear='pcg', exact_tol=1e-11, warm_substep=False):
     """linear='pcg': the reference's V-cycle PCG; 'exact': each Newton
     system solved to a float64 dual residual of exact_tol |b|
     (oracle/exact_solve.py), for checking positions against the step with
     an exact linear solve; 'cheb': the library's FAST linear solve (CG
     with a Chebyshev-8 polynomial in A, lo 1e-3, to rel_tol_cg) in float64,
     the same algorithm as the CUDA path in exact arithmetic's stead (both
-    float64 only)."""
+    float64 only); warm_substep (with 'cheb'): each substep's first solve
+    starts from the previous substep's first solution, as the library's
+    warm_substep option does."""
     if linear not in ('pcg', 'exact', 'cheb'):
       raise ValueError("linear must be 'pcg', 'exact' or 'cheb'")
     if linear != 'pcg' and dtype != np.float64:
       raise ValueError(f"linear='{linear}' is a float64 oracle")
     self.linear = linear
     self.exact_tol = exact_tol
+    self.warm_substep = bool(warm_substep)
+    self.dlam_prev = None
     self.exact_log = []
     self.dtype = dtype
     f = dtype
@@ -764,9 +768,12 @@ class MGPBDOracle:
         Jt = J.T.tocsr()
         w3 = np.repeat(np.asarray(self.invm, np.float64), 3)
         al = np.asarray(self.alpha, np.float64)
+        x0 = self.dlam_prev if (self.warm_substep and ite == 0) else None
         dlam, it = chebyshev_pcg(lambda v: al * v + J @ (w3 * (Jt @ v)), b,
                                  rel_tol=self.rel_tol_cg, tol_abs=self.tol_cg,
-                                 maxiter=self.maxiter_cg)
+                                 maxiter=self.maxiter_cg, x0=x0)
+        if self.warm_substep and ite == 0:
+          self.dlam_prev = dlam.copy()
       else:
         self.fill_matrices()
         dlam, it = self.pcg(b)
