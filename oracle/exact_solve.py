@@ -207,3 +207,66 @@ def chebyshev_pcg(apply_A, b, degree=8, lo=1e-3, scale=None, rel_tol=1e-6, tol_a
     p = z + (rz_new / rz) * p
     rz = rz_new
   return x, maxiter
+
+
+def chebyshev_pcg_bodies(apply_A, b, bodies, degree=8, lo=1e-3, rel_tol=1e-6, tol_abs=0.0,
+                         maxiter=6000, lmax=None):
+  """One Chebyshev-preconditioned CG per body on a block-diagonal A, in
+  lockstep with one shared polynomial (lmax of the whole A), as the
+  library's per-body kernel runs them: each body's dot products, alpha,
+  beta and stopping test (|r_b| < max(tol_abs, rel_tol |b_b|)) are its own,
+  and a body that stops keeps its x and r.  bodies: one index array per
+  body (together a partition).  Returns (x, per-body iterations)."""
+  b = np.asarray(b, np.float64)
+  n = len(b)
+  if lmax is None:
+    op = sla.LinearOperator((n, n), matvec=apply_A, dtype=np.float64)
+    lmax = float(sla.eigsh(op, k=1, which='LA', tol=1e-10, return_eigenvectors=False)[0])
+  hi = 1.02 * lmax
+  a_ = lo * hi
+  theta, delta = 0.5 * (hi + a_), 0.5 * (hi - a_)
+  sigma = theta / delta
+
+  def precond(r):
+    x = np.zeros_like(r)
+    rr = r.copy()
+    d = rr / theta
+    rho = 1.0 / sigma
+    for _ in range(degree):
+      x += d
+      rr -= apply_A(d)
+      rho_n = 1.0 / (2.0 * sigma - rho)
+      d = rho_n * rho * d + 2.0 * rho_n / delta * rr
+      rho = rho_n
+    return x
+
+  nb = len(bodies)
+  x = np.zeros(n)
+  r = b.copy()
+  tol = [max(tol_abs, rel_tol * np.linalg.norm(b[ix])) for ix in bodies]
+  done = [bool(np.linalg.norm(r[ix]) < tol[k]) for k, ix in enumerate(bodies)]
+  its = [0] * nb
+  z = precond(r)
+  p = z.copy()
+  rz = [r[ix] @ z[ix] for ix in bodies]
+  for _ in range(maxiter):
+    if all(done):
+      break
+    ap = apply_A(p)
+    for k, ix in enumerate(bodies):
+      if done[k]:
+        continue
+      alpha = rz[k] / (p[ix] @ ap[ix])
+      x[ix] += alpha * p[ix]
+      r[ix] -= alpha * ap[ix]
+      its[k] += 1
+      if np.linalg.norm(r[ix]) < tol[k]:
+        done[k] = True
+    z = precond(r)
+    for k, ix in enumerate(bodies):
+      if done[k]:
+        continue
+      rz_new = r[ix] @ z[ix]
+      p[ix] = z[ix] + (rz_new / rz[k]) * p[ix]
+      rz[k] = rz_new
+  return x, its

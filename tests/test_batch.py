@@ -228,3 +228,50 @@ def test_captured_substep_equals_host_loop(cuda, body_cg, warm):
     assert sg == sh
     assert lg == lh
   assert runs[True][-1][2]['status'] == 0
+
+
+def _block_system(n_bodies=4, seed=1, dims=(4, 8)):
+  """The first Newton system of each of `n_bodies` packed bodies (length +
+  volume constraints, float64): the blocks, their right-hand sides."""
+  import scipy.sparse as sp
+  from oracle import mgpbd_oracle as MO
+  from oracle.exact_solve import constraint_jacobian
+  As, bs = [], []
+  for b in random_bodies(n_bodies, seed=seed, dims=dims, compliance=(1e-8, 1e-5)):
+    c, ctype, _, _ = MO.edge_volume_system(b.t_i)
+    dm, rest, alpha = MO.rest_shape(b.x_ref, c, 0.0, 1 / 300, np.float64, compliance=b.compliance,
+                                    ctype=ctype)
+    C, g = MO.constraints(b.x0, c, dm, np.float64, ctype=ctype, rest=rest)
+    J = constraint_jacobian(c, g, len(b.x_ref))
+    w = np.repeat(np.asarray(b.invm, np.float64), 3)
+    As.append((J @ sp.diags(w) @ J.T + sp.diags(np.asarray(alpha, np.float64))).tocsr())
+    bs.append(-np.asarray(C, np.float64))
+  return As, bs
+
+
+def test_per_body_cg_restated_in_float64():
+  """The per-body CG of packed bodies (`k_jcg_bodies`) restated in float64
+  (`oracle.exact_solve.chebyshev_pcg_bodies`): on a block-diagonal pack of
+  four bodies each body's solution is its own CG's (same shared polynomial)
+  to 1e-7, with its iteration count within 2 % (summation order of the
+  packed product aside), every body meets its own bound, and one CG over
+  the pack run to the smallest body bound needs over 1.5 x the iterations
+  of the slowest body."""
+  import scipy.sparse as sp
+  import scipy.sparse.linalg as sla
+  from oracle.exact_solve import chebyshev_pcg, chebyshev_pcg_bodies
+  As, bs = _block_system()
+  Ab = sp.block_diag(As).tocsr()
+  bb = np.concatenate(bs)
+  offs = np.cumsum([0] + [len(b) for b in bs])
+  idx = [np.arange(offs[k], offs[k + 1]) for k in range(len(bs))]
+  lmax = float(sla.eigsh(Ab, k=1, which='LA', tol=1e-10, return_eigenvectors=False)[0])
+  x, its = chebyshev_pcg_bodies(lambda v: Ab @ v, bb, idx, lmax=lmax)
+  for k, (A, b) in enumerate(zip(As, bs)):
+    xs, it = chebyshev_pcg(lambda v, A=A: A @ v, b, lmax=lmax)
+    assert np.abs(x[idx[k]] - xs).max() <= 1e-7 * np.abs(xs).max(), k
+    assert abs(its[k] - it) <= 0.02 * it, (k, its[k], it)
+    assert np.linalg.norm(b - A @ x[idx[k]]) <= 1.01e-6 * np.linalg.norm(b), k
+  bound = min(1e-6 * np.linalg.norm(b) for b in bs)
+  _, itc = chebyshev_pcg(lambda v: Ab @ v, bb, lmax=lmax, rel_tol=0.0, tol_abs=bound)
+  assert itc > 1.5 * max(its), (itc, its)
