@@ -382,6 +382,11 @@ def roofline_from_steps(st, nt, nv, degree, hbm_peak, peak_kind, size=40, constr
   if roof['traffic'] is not None:
     roof['traffic_over_algorithmic'] = round(roof['traffic'] /
                                              max(roof['algorithmic_bytes_per_launch'], 1), 4)
+    # the DRAM rate itself (ncu bytes over the same launch time): most of the
+    # algorithmic bytes are served by L2, so this is far below `frac`
+    dram_gbs = roof['traffic'] / (roof['launch_us'] * 1e-6) / 1e9
+    roof['dram_gbs'] = round(dram_gbs, 1)
+    roof['dram_frac'] = round(dram_gbs / hbm_peak, 4)
   if len(out) > 1:
     roof['other'] = out[1]
   return roof

@@ -83,6 +83,9 @@ def test_roofline_from_steps_picks_the_dominant_kernel():
   assert r['traffic_over_algorithmic'] == pytest.approx(r['traffic'] / per_launch, abs=1e-4)
   assert r['share_of_cg_gpu_time'] + r['other']['share_of_cg_gpu_time'] == pytest.approx(1, abs=2e-3)
   assert np.isclose(r['frac'], r['achieved'] / 6701.2, atol=1e-4)
+  # the DRAM rate over the same launch time, far below the algorithmic one
+  assert r['dram_gbs'] == pytest.approx(r['traffic'] / 0.1 / 1e9, rel=1e-3)
+  assert r['dram_frac'] < 0.5 * r['frac']
 
 
 def test_reference_arm_prints_one_contract_line():
