@@ -121,3 +121,21 @@ def test_dot_noalloc_rejects_bad_sizes_with_a_message():
   assert b'67,108,864' in L.mgpbd_last_error()
   assert L.mgpbd_dot_noalloc(-1, None, None, C.byref(out), None) == -1  # MGPBD_EINVAL
   assert b'mgpbd_dot_noalloc' in L.mgpbd_last_error()
+
+
+def test_integration_stub_mirrors_the_params_struct():
+  """The ctypes stub a maintainer would copy
+  lists the fields of mgpbd_params in the header's order, as the binding
+  does."""
+  import os
+  import re
+  here = os.path.dirname(os.path.abspath(__file__))
+  text = open(os.path.join(here, '..', 'INTEGRATION.md')).read()
+  block = text[text.index('class Params(C.Structure)'):]
+  block = block[:block.index(']\n') + 1]
+  names = re.findall(r"\('([a-z_0-9]+)',", block)
+  assert names == [f[0] for f in N.Params._fields_]
+  header = open(os.path.join(here, '..', 'include', 'mgpbd.h')).read()
+  struct = header[header.index('typedef struct mgpbd_params {'):header.index('} mgpbd_params;')]
+  fields = re.findall(r'^\s+(?:float|int32_t)\s+([a-z_0-9]+)(?:\[3\])?;', struct, re.M)
+  assert fields == names
